@@ -1,0 +1,318 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 BioFVM reaction-diffusion step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+A step is one `solve(1)` of the large single-domain workload (320^3 voxels x 8
+substrates, FP32 field, 1,000,000 agents, Dirichlet on the x faces and 10,000
+interior voxels): three ADI sweeps, Dirichlet, cells.  The metric is
+voxel-substrate-steps per second (VSS/s) = voxels * substrates * steps / time.
+
+Arms
+  gb300      (default) the hand-written sm_103a kernels through the C ABI.  Inputs
+             are resident in HBM when the timed region starts; the field (1.05 GB)
+             is larger than L2, so no flush is needed between steps.  `e2e` repeats
+             the step through the same C ABI with host buffers: per step the agent
+             positions/activity go host->device from pinned memory and the whole
+             field comes back device->host.
+  reference  the reference's CPU algorithm (the OpenMP restatement in oracle/,
+             FP64, all host threads) on the same workload, a bounded number of
+             steps.  Under torchrun only rank 0 runs it.
+Multi-GPU: every rank steps its own replica (the path does not shard a single
+domain); value = all ranks' VSS / max-over-ranks time; scaling "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "voxel-substrate-steps/s + % HBM roofline, batched vs plain; serve p50/p99"
+UNIT = "voxel-substrate-steps/s"
+WORKLOAD = dict(n=320, S=8, agents=1_000_000, interior=10_000, seed=1)
+FALLBACK_HBM_GBS = 6800.0
+
+
+def workload_config(w):
+    n = w["n"]
+    return {"workload": f"large_{n}: {n}^3 voxels of 20 um x {w['S']} substrates, FP32 field, "
+                        f"{w['agents']:,} agents (internalized tracking on), Dirichlet x faces + "
+                        f"{w['interior']:,} interior voxels, D log-uniform [10,1e5], decay log-uniform [1e-4,1]",
+            "grid": [n, n, n], "substrates": w["S"], "agents": w["agents"], "seed": w["seed"],
+            "l2": "inputs larger than L2 (field %.2f GB > 129 MB L2); no flush" % (n ** 3 * w["S"] * 4 / 1e9),
+            "step": "solve(1): x/y/z Thomas sweeps, Dirichlet faces+interior, cell secretion/uptake"}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            return float(d["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (of measured)"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback 6.8 TB/s (of fallback)"
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch from the committed ncu summary, when one exists."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    try:
+        d = json.load(open(p))
+        return d.get(kernel, {}).get("bytes_per_launch")
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[3 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def build_problem(w):
+    from physicore_gb300 import workloads as W
+    return W.large(seed=w["seed"], n=w["n"], S=w["S"], agents=w["agents"], interior=w["interior"])
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def time_reference(p, steps, warmup, threads, budget_s=60.0):
+    """The reference algorithm on the host: FP64, OpenMP over `threads` threads."""
+    from oracle import oracle
+    from physicore_gb300 import workloads as W
+    o = W.apply(oracle.OracleSolver(threads=threads), p)
+    o.solve(1)  # the first solve call rebuilds the ballots (openmp_solver.cpp:39)
+    for _ in range(max(0, warmup - 1)):
+        o.solve(1)
+    done, t0 = 0, time.perf_counter()
+    while done < steps:
+        o.solve(1)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    n, S = p["bbmax"][0] // p["voxel"][0], len(p["D"])
+    return n ** 3 * S * done / dt, done, dt
+
+
+def run_reference(args, w):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    p = build_problem(w)
+    threads = cpu_threads()
+    value, done, secs = time_reference(p, args.steps, min(args.warmup, 1), threads,
+                                       budget_s=float(os.environ.get("PCG_REF_BUDGET_S", "90")))
+    sample = f"{done} timed steps (after 1 warm-up) of the {args.steps}-step request, {secs:.1f} s"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": done, "warmup": 1, "ms_per_step": 1e3 * secs / max(done, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
+            "config": workload_config(w),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, w):
+    import torch
+
+    import physicore_gb300 as pcg
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    p = build_problem(w)
+    from physicore_gb300 import workloads as W
+    s = W.apply(pcg.Solver(pcg.FP32, device=local), p)
+    n, S = w["n"], w["S"]
+    vss_step = n ** 3 * S
+    s.solve(1)  # first call: ballots rebuilt
+    for _ in range(max(0, args.warmup - 1)):
+        s.solve(1)
+    s.synchronize()
+
+    stream = torch.cuda.ExternalStream(s.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.set_kernel_timing(True)
+    s.reset_kernel_stats()
+    launches0 = s.launch_count()
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            s.solve(1)
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    launches = s.launch_count() - launches0
+    stats = s.kernel_stats()
+    s.set_kernel_timing(False)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = vss_step * args.steps * world / (ms / 1e3)
+
+    # roofline of the dominant kernel (largest share of device time)
+    peak, peak_src = measured_peaks()
+    timed = {k: v for k, v in stats.items() if v["launches"] and v["ms"] > 0}
+    dom = max(timed, key=lambda k: timed[k]["ms"])
+    d = timed[dom]
+    per_launch_bytes = d["bytes"] / d["launches"]
+    achieved = per_launch_bytes / (d["ms"] / d["launches"] / 1e3) / 1e9
+    step_bytes = sum(v["bytes"] for v in stats.values()) / args.steps
+    kernels = {k: {"launches": v["launches"], "ms_total": round(v["ms"], 4),
+                   "share": round(v["ms"] / sum(x["ms"] for x in timed.values()), 4),
+                   "gbps": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] > 0 else None}
+               for k, v in timed.items()}
+
+    # end to end through the C ABI with host buffers
+    A = p["agents"]["volumes"].size
+    pos_h = torch.empty((A, 3), dtype=torch.float64, pin_memory=True)
+    act_h = torch.empty(A, dtype=torch.uint8, pin_memory=True)
+    pos_h.numpy()[:] = p["agents"]["positions"]
+    act_h.numpy()[:] = p["agents"]["is_active"]
+    field_h = torch.empty((S, n, n, n), dtype=torch.float32, pin_memory=True)
+    pos_np, act_np, field_np = pos_h.numpy(), act_h.numpy(), field_h.numpy()
+    e2e_steps = max(3, min(args.steps, args.e2e_steps))
+    s.update_agents(pos_np, act_np)
+    s.solve(1)
+    s.get_field(layout=pcg.LAYOUT_PLANAR, dtype=np.float32, out=field_np)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.update_agents(pos_np, act_np)
+        s.solve(1)
+        s.get_field(layout=pcg.LAYOUT_PLANAR, dtype=np.float32, out=field_np)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": vss_step * e2e_steps * world / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(pos_np.nbytes + act_np.nbytes),
+           "d2h_bytes_per_step": int(field_np.nbytes), "steps": e2e_steps,
+           "path": "pcg_update_agents(pinned) -> pcg_solve(1) -> pcg_get_field(pinned, planar f32)"}
+    s.close()
+
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        threads = cpu_threads()
+        v, done, secs = time_reference(p, args.cpu_steps, 1, threads, budget_s=30.0)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{done} steps of large_{n} on the oracle (FP64 OpenMP restatement), {secs:.1f} s"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded PCG64)",
+            "config": dict(workload_config(w), parallelism=f"replicas x{world}"),
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": ncu_traffic(dom),
+                         "algorithmic_bytes_per_launch": per_launch_bytes, "peak_source": peak_src},
+            "step_roofline": {"achieved": round(step_bytes / (ms / args.steps / 1e3) / 1e9, 1), "peak": peak,
+                              "frac": round(step_bytes / (ms / args.steps / 1e3) / 1e9 / peak, 4),
+                              "algorithmic_bytes_per_step": step_bytes},
+            "kernels": kernels, "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e,
+            "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n", type=int, default=WORKLOAD["n"], help="grid side (default: the 320^3 workload)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    w = dict(WORKLOAD, n=args.n)
+    if args.impl == "reference":
+        run_reference(args, w)
+    else:
+        run_gb300(args, w)
+
+
+if __name__ == "__main__":
+    main()

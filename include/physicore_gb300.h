@@ -1,0 +1,190 @@
+/*
+ * physicore_gb300.h -- C ABI of the GB300 BioFVM reaction-diffusion backend.
+ *
+ * One pcg_context is one BioFVM problem (mesh, substrates, Dirichlet sets, bulk
+ * tables, agents) resident on one GPU.  The entry points replace the reference's
+ * solver plugin surface, reactions-diffusion/biofvm/include/biofvm/solver.h:12-39,
+ * and read the same microenvironment fields the reference solvers read
+ * (include/biofvm/microenvironment.h:46-81).  A C++ `solver` subclass that
+ * forwards to these calls is in physicore_gb300/csrc/host/gb300_solver.{h,cpp}.
+ *
+ * Conventions
+ *  - Every function returns 0 (PCG_OK) on success or a PCG_ERR_* code; the text
+ *    of the last error on the calling thread is returned by pcg_last_error().
+ *    The reference reports these conditions with exceptions/asserts
+ *    (microenvironment_builder.cpp:153-204, mesh.cpp:39-44).
+ *  - Host arrays are plain C arrays; all scalars are double/uint64_t as in the
+ *    reference (common/include/common/types.h:7-9).  Nothing is retained: every
+ *    setter copies its input.
+ *  - Work is queued on the context's CUDA stream; functions that return data to
+ *    the host synchronise that stream first.
+ *  - Kernels never trap: device-side faults (agent outside the mesh, a bounded
+ *    wait that ran out) set a device error word that the next synchronising call
+ *    reports as PCG_ERR_DEVICE.
+ */
+#ifndef PHYSICORE_GB300_H
+#define PHYSICORE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PCG_OK 0
+#define PCG_ERR_INVALID 1     /* bad argument or call order */
+#define PCG_ERR_CUDA 2        /* CUDA runtime error */
+#define PCG_ERR_NOMEM 3       /* device or host allocation failed / admission refused */
+#define PCG_ERR_DEVICE 4      /* a kernel flagged a fault (see pcg_last_error) */
+#define PCG_ERR_UNSUPPORTED 5 /* size beyond this build's limits */
+
+/* Arithmetic of the device field: the reference is FP64 throughout
+ * (types.h:7); the FP32 build keeps FP64 coefficients/positions/internalized
+ * substrates and stores the substrate field in FP32. */
+#define PCG_FP32 0
+#define PCG_FP64 1
+
+/* Host buffer layouts for pcg_get_field / pcg_set_field.
+ * INTERLEAVED is the reference's layout without row padding
+ * (openmp_solver/src/diffusion_solver.h:64-83): index = s + S*(x + nx*(y + ny*z)).
+ * PLANAR is substrate-major: index = x + nx*(y + ny*(z + nz*s)). */
+#define PCG_LAYOUT_INTERLEAVED 0
+#define PCG_LAYOUT_PLANAR 1
+
+/* Host element types for pcg_get_field / pcg_set_field. */
+#define PCG_DTYPE_F64 0
+#define PCG_DTYPE_F32 1
+
+/* Phases of one step, in the reference's order (openmp_solver.cpp:27-37). */
+#define PCG_PHASE_DIFFUSION 1u
+#define PCG_PHASE_DIRICHLET 2u
+#define PCG_PHASE_BULK 4u
+#define PCG_PHASE_CELLS 8u
+#define PCG_PHASE_ALL 15u
+
+/* Bulk supply/uptake tables: the reference's virtual bulk_functor
+ * (include/biofvm/bulk_functor.h:8-14) evaluated into device tables. */
+#define PCG_BULK_NONE 0
+#define PCG_BULK_UNIFORM 1   /* supply/uptake/target arrays of length S */
+#define PCG_BULK_PER_VOXEL 2 /* arrays of length S*V, planar [s][z][y][x] */
+
+typedef struct pcg_context pcg_context;
+
+/* Per-kernel timing record (pcg_get_kernel_stats). */
+typedef struct pcg_kernel_stat
+{
+	char name[32];
+	uint64_t launches;
+	double total_ms;          /* CUDA-event time summed over launches (0 when timing is off) */
+	double algorithmic_bytes; /* bytes the kernel must move per the roofline model, summed */
+} pcg_kernel_stat;
+
+/* ---- lifetime ---------------------------------------------------------- */
+
+/* Creates a context on `device` with its own CUDA stream.  Replaces the
+ * registry factory call solver_registry::get (src/solver_registry.cpp:20-29). */
+int pcg_create(pcg_context** out, int precision, int device);
+/* Releases every device buffer of the context (solver destructor, solver.h:35). */
+int pcg_destroy(pcg_context* ctx);
+/* Text of the last error raised on this thread ("" when none). */
+const char* pcg_last_error(void);
+/* Runs later work of this context on `stream` (a cudaStream_t); NULL restores
+ * the context's own stream. */
+int pcg_set_stream(pcg_context* ctx, void* stream);
+int pcg_get_stream(pcg_context* ctx, void** stream);
+
+/* ---- problem description (microenvironment fields) --------------------- */
+
+/* cartesian_mesh(dims, bounding_box_mins, bounding_box_maxs, voxel_shape)
+ * (include/biofvm/mesh.h:11-32, src/mesh.cpp:8-28). */
+int pcg_set_mesh(pcg_context* ctx, int dims, const int64_t bbox_min[3], const int64_t bbox_max[3],
+				 const uint64_t voxel_shape[3]);
+int pcg_get_grid(pcg_context* ctx, uint64_t grid_shape[3]);
+/* substrates_count, diffusion_timestep, diffusion_coefficients, decay_rates,
+ * initial_conditions (microenvironment.h:53-63). */
+int pcg_set_substrates(pcg_context* ctx, uint64_t substrates, double dt, const double* diffusion,
+					   const double* decay, const double* initial);
+/* dirichlet_interior_voxels [K*dims], _values [K*S], _conditions [K*S]
+ * (microenvironment.h:65-69).  Re-callable after initialize: this is the upload
+ * half of solver::reinitialize_dirichlet (thrust_solver.cpp:61). */
+int pcg_set_dirichlet_interior(pcg_context* ctx, uint64_t count, const uint64_t* voxels, const double* values,
+							   const uint8_t* conditions);
+/* dirichlet_{min,max}_boundary_{values,conditions}[axis] (microenvironment.h:72-75).
+ * side 0 = min, 1 = max; values == NULL removes the face. */
+int pcg_set_dirichlet_boundary(pcg_context* ctx, int axis, int side, const double* values,
+							   const uint8_t* conditions);
+/* bulk_fnc (microenvironment.h:78) tabulated; see PCG_BULK_*. */
+int pcg_set_bulk(pcg_context* ctx, int mode, const double* supply, const double* uptake, const double* target);
+/* Agent SoA (agent_data_generic_storage.h:16-31, base_agent_data_generic_storage.h:66):
+ * positions [A*dims], rates [A*S], volumes [A], is_active [A]; internalized and
+ * fraction_released may be NULL (zeros).  Marks positional data for recompute. */
+int pcg_set_agents(pcg_context* ctx, uint64_t count, const double* positions, const double* secretion,
+				   const double* saturation, const double* uptake, const double* net_export, const double* volumes,
+				   const uint8_t* is_active, const double* internalized, const double* fraction_released,
+				   int compute_internalized);
+/* Uploads moved positions and/or activity flags (either may be NULL) of the
+ * current agents; the host side of transfer_to_device (data_manager.cpp:61-93). */
+int pcg_update_agents(pcg_context* ctx, const double* positions, const uint8_t* is_active);
+int pcg_set_internalized(pcg_context* ctx, const double* internalized);
+
+/* ---- the solver plugin surface (solver.h:12-39) ------------------------- */
+
+/* solver::initialize: allocates the field, fills it with the initial
+ * conditions, precomputes the Thomas coefficients in FP64
+ * (openmp_solver.cpp:8-21, diffusion_solver.cpp:29-113).  Idempotent. */
+int pcg_initialize(pcg_context* ctx);
+/* solver::solve(m, iterations) (openmp_solver.cpp:23-40): diffusion x->y->z,
+ * Dirichlet, bulk, cells per iteration; ballots are rebuilt during every
+ * iteration of a call that follows initialize or pcg_recompute_positional_data. */
+int pcg_solve(pcg_context* ctx, uint64_t iterations);
+/* Runs the selected phases once (the reference's unit tests drive the
+ * sub-solvers this way, e.g. openmp_solver/tests/test_cell_solver.cpp:159-187). */
+int pcg_run_phases(pcg_context* ctx, uint32_t phases, int recompute_cells);
+/* solver::recompute_positional_data (openmp_solver.cpp:64). */
+int pcg_recompute_positional_data(pcg_context* ctx);
+/* cell_solver::release_internalized_substrates (cell_solver.cpp:351-374). */
+int pcg_release_internalized(pcg_context* ctx, uint64_t agent);
+
+/* ---- host access (get_substrate_density, transfer_to_host) ------------- */
+
+/* Copies the whole field to `host` in the requested layout and element type
+ * (transfer_to_host, data_manager.cpp:35-59; get_substrate_density,
+ * openmp_solver.cpp:42-56).  Synchronises the stream. */
+int pcg_get_field(pcg_context* ctx, void* host, int layout, int dtype);
+/* Overwrites the field from `host` (transfer_to_device of the densities). */
+int pcg_set_field(pcg_context* ctx, const void* host, int layout, int dtype);
+/* One density, synchronising (the const get_substrate_density). */
+int pcg_get_density(pcg_context* ctx, uint64_t s, uint64_t x, uint64_t y, uint64_t z, double* value);
+int pcg_get_internalized(pcg_context* ctx, double* host);
+/* Active agents per voxel after the last ballot, [V] in x-fastest order.
+ * Integer, bit-exact with the reference's ballot (cell_solver.cpp:79-129). */
+int pcg_get_counts(pcg_context* ctx, uint32_t* host);
+/* 1 when the last ballot found a voxel with more than one agent. */
+int pcg_get_conflict(pcg_context* ctx, int* conflict);
+/* Total mass per substrate, summed on the device in FP64. */
+int pcg_mass(pcg_context* ctx, double* host);
+int pcg_synchronize(pcg_context* ctx);
+
+/* ---- device-resident access (benchmarks, zero-copy integration) -------- */
+
+/* Device pointer of the field, its element size and row pitch (elements).
+ * Device layout: planar, row-padded: element (s,x,y,z) is at
+ * ptr[((s*nz + z)*ny + y)*pitch + x]. */
+int pcg_get_field_device(pcg_context* ctx, void** ptr, uint64_t* elem_bytes, uint64_t* pitch);
+
+/* ---- measurement -------------------------------------------------------- */
+
+/* Wraps every kernel launch in CUDA events (per-kernel time) when enabled. */
+int pcg_set_kernel_timing(pcg_context* ctx, int enable);
+/* Copies up to `cap` per-kernel records; *count receives how many exist. */
+int pcg_get_kernel_stats(pcg_context* ctx, pcg_kernel_stat* stats, uint64_t cap, uint64_t* count);
+int pcg_reset_kernel_stats(pcg_context* ctx);
+/* Kernels launched by this context since creation or the last reset. */
+int pcg_get_launch_count(pcg_context* ctx, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

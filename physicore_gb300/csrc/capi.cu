@@ -1,0 +1,942 @@
+// capi.cu -- the extern "C" surface of include/physicore_gb300.h.
+//
+// The context owns every device buffer of one BioFVM problem and queues all work
+// on one CUDA stream.  Step orchestration follows openmp_solver::solve
+// (openmp_solver.cpp:23-40): diffusion (x, then y and z when the mesh has them,
+// diffusion_solver.cpp:797-843), Dirichlet, bulk, cells; the ballot is rebuilt on
+// every iteration of a solve call that follows initialize or
+// recompute_positional_data, and the flag is cleared when the call returns.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "pcg_internal.cuh"
+
+namespace pcg {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int code, const std::string& msg)
+{
+	set_error(msg);
+	return code;
+}
+
+const char* kernel_name(int id)
+{
+	static const char* names[K_COUNT] = { "sweep_x",	  "sweep_y",		"sweep_z",	   "dirichlet_faces",
+										  "dirichlet_interior", "bulk", "cells_locate", "cells_ballot",
+										  "cells_reduce", "cells_apply", "cells_internalize", "cells_release",
+										  "mass",		  "layout" };
+	return (id >= 0 && id < K_COUNT) ? names[id] : "?";
+}
+
+int dalloc(Context* c, DeviceBuffer& b, size_t bytes)
+{
+	(void)c;
+	if (b.ptr && b.bytes >= bytes)
+		return PCG_OK;
+	dfree(b);
+	if (bytes == 0)
+		return PCG_OK;
+	cudaError_t e = cudaMalloc(&b.ptr, bytes);
+	if (e != cudaSuccess)
+	{
+		b.ptr = nullptr;
+		cudaGetLastError();
+		return fail(PCG_ERR_NOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
+	}
+	b.bytes = bytes;
+	return PCG_OK;
+}
+
+void dfree(DeviceBuffer& b)
+{
+	if (b.ptr)
+		cudaFree(b.ptr);
+	b.ptr = nullptr;
+	b.bytes = 0;
+}
+
+static cudaEvent_t get_event(Context* c)
+{
+	if (!c->event_pool.empty())
+	{
+		cudaEvent_t e = c->event_pool.back();
+		c->event_pool.pop_back();
+		return e;
+	}
+	cudaEvent_t e = nullptr;
+	cudaEventCreate(&e);
+	return e;
+}
+
+void launch_begin(Context* c, int kid, double bytes, cudaEvent_t* ev)
+{
+	c->launches++;
+	c->stats[kid].launches++;
+	c->stats[kid].bytes += bytes;
+	*ev = nullptr;
+	if (c->timing)
+	{
+		*ev = get_event(c);
+		cudaEventRecord(*ev, c->stream);
+	}
+}
+
+void launch_end(Context* c, int kid, cudaEvent_t ev)
+{
+	if (!c->timing || !ev)
+		return;
+	cudaEvent_t stop = get_event(c);
+	cudaEventRecord(stop, c->stream);
+	c->pending.push_back({ kid, ev, stop });
+}
+
+void collect_timings(Context* c)
+{
+	for (auto& p : c->pending)
+	{
+		cudaEventSynchronize(p.b);
+		float ms = 0;
+		cudaEventElapsedTime(&ms, p.a, p.b);
+		c->stats[p.kid].total_ms += ms;
+		c->event_pool.push_back(p.a);
+		c->event_pool.push_back(p.b);
+	}
+	c->pending.clear();
+}
+
+// ------------------------------------------------------------------ helpers
+
+static uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
+
+struct DeviceGuard
+{
+	int prev = -1;
+	explicit DeviceGuard(int dev)
+	{
+		cudaGetDevice(&prev);
+		if (prev != dev)
+			cudaSetDevice(dev);
+	}
+	~DeviceGuard()
+	{
+		if (prev >= 0)
+			cudaSetDevice(prev);
+	}
+};
+
+// Reads and clears the device error word after synchronising the stream.
+static int check_device(Context* c)
+{
+	cudaError_t e = cudaStreamSynchronize(c->stream);
+	if (e != cudaSuccess)
+		return fail(PCG_ERR_CUDA, std::string("stream synchronise: ") + cudaGetErrorString(e));
+	collect_timings(c);
+	uint32_t word = 0;
+	PCG_CUDA_TRY(cudaMemcpy(&word, c->err.ptr, sizeof(word), cudaMemcpyDeviceToHost));
+	if (word)
+	{
+		PCG_CUDA_TRY(cudaMemset(c->err.ptr, 0, sizeof(uint32_t)));
+		std::string msg = "device fault:";
+		if (word & DEV_ERR_AGENT_OUTSIDE)
+			msg += " an active agent lies outside the mesh;";
+		if (word & DEV_ERR_WAIT_TIMEOUT)
+			msg += " a bounded shared-memory wait timed out;";
+		if (word & DEV_ERR_DIRICHLET_INDEX)
+			msg += " a Dirichlet voxel lies outside the mesh;";
+		if (word & DEV_ERR_BAD_TILE)
+			msg += " a batched tile descriptor was invalid;";
+		return fail(PCG_ERR_DEVICE, msg);
+	}
+	return PCG_OK;
+}
+
+// diffusion_solver::precompute_values (openmp_solver/src/diffusion_solver.cpp:29-86),
+// evaluated in FP64 for one axis.  Outputs b'[i*S+s], e[(i-1)*S+s], c[s].
+static void precompute_axis(uint64_t n, uint64_t S, uint64_t shape, uint64_t dims, double dt, const double* D,
+							const double* decay, std::vector<double>& b, std::vector<double>& e,
+							std::vector<double>& cc)
+{
+	const double h2 = (double)(shape * shape);
+	b.assign(n * S, 0.0);
+	e.assign((n > 0 ? n - 1 : 0) * S, 0.0);
+	cc.assign(S, 0.0);
+	for (uint64_t s = 0; s < S; s++)
+		cc[s] = -1 * -dt * D[s] / h2; // c = dt*D/h^2 (the reference stores -a_i)
+	for (uint64_t i = 0; i < n; i++)
+		for (uint64_t s = 0; s < S; s++)
+		{
+			double v = 1 + decay[s] * dt / (double)dims + 2 * dt * D[s] / h2;
+			if (i == 0 || i == n - 1) // Neumann rows; a single subtraction when n == 1
+				v -= dt * D[s] / h2;
+			b[i * S + s] = v;
+		}
+	for (uint64_t s = 0; s < S; s++)
+		b[s] = 1 / b[s];
+	for (uint64_t i = 1; i < n; i++)
+		for (uint64_t s = 0; s < S; s++)
+		{
+			b[i * S + s] = 1 / (b[i * S + s] - cc[s] * cc[s] * b[(i - 1) * S + s]);
+			e[(i - 1) * S + s] = cc[s] * b[(i - 1) * S + s];
+		}
+}
+
+template <typename T>
+static int upload_coefficients(Context* c)
+{
+	for (int axis = 0; axis < c->dims; axis++)
+	{
+		const uint64_t n = c->n[axis];
+		std::vector<double> b, e, cc;
+		precompute_axis(n, c->S, c->voxel[axis], (uint64_t)c->dims, c->dt, c->D.data(), c->decay.data(), b, e, cc);
+		const uint64_t npad = round_up(n, 16 / sizeof(T));
+		c->coef_pitch[axis] = 2 * npad;
+		std::vector<T> tab(c->S * 2 * npad, T(0));
+		std::vector<T> tc(c->S);
+		for (uint64_t s = 0; s < c->S; s++)
+		{
+			T* B = tab.data() + s * 2 * npad;
+			T* E = B + npad;
+			for (uint64_t i = 0; i < n; i++)
+			{
+				B[i] = (T)b[i * c->S + s];
+				E[i] = i == 0 ? T(0) : (T)e[(i - 1) * c->S + s];
+			}
+			tc[s] = (T)cc[s];
+		}
+		int rc = dalloc(c, c->coef[axis], tab.size() * sizeof(T));
+		if (rc)
+			return rc;
+		if ((rc = dalloc(c, c->coef_c[axis], tc.size() * sizeof(T))))
+			return rc;
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->coef[axis].ptr, tab.data(), tab.size() * sizeof(T), cudaMemcpyHostToDevice,
+									 c->stream));
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->coef_c[axis].ptr, tc.data(), tc.size() * sizeof(T), cudaMemcpyHostToDevice,
+									 c->stream));
+		PCG_CUDA_TRY(cudaStreamSynchronize(c->stream)); // host vectors die at scope exit
+	}
+	return PCG_OK;
+}
+
+template <typename T>
+static int upload_dirichlet(Context* c)
+{
+	const uint64_t S = c->S;
+	int rc;
+	// faces
+	std::vector<T> fv(6 * S, T(0));
+	std::vector<uint8_t> fc(6 * S, 0);
+	for (int axis = 0; axis < 3; axis++)
+		for (int side = 0; side < 2; side++)
+			if (c->face_on[axis][side])
+				for (uint64_t s = 0; s < S; s++)
+				{
+					fv[(axis * 2 + side) * S + s] = (T)c->h_face_values[axis][side][s];
+					fc[(axis * 2 + side) * S + s] = c->h_face_conds[axis][side][s] ? 1 : 0;
+				}
+	if ((rc = dalloc(c, c->face_values, fv.size() * sizeof(T))))
+		return rc;
+	if ((rc = dalloc(c, c->face_conds, fc.size())))
+		return rc;
+	PCG_CUDA_TRY(cudaMemcpyAsync(c->face_values.ptr, fv.data(), fv.size() * sizeof(T), cudaMemcpyHostToDevice,
+								 c->stream));
+	PCG_CUDA_TRY(cudaMemcpyAsync(c->face_conds.ptr, fc.data(), fc.size(), cudaMemcpyHostToDevice, c->stream));
+	// interior
+	std::vector<uint64_t> off(c->K);
+	std::vector<T> iv(c->K * S);
+	std::vector<uint8_t> ic(c->K * S);
+	for (uint64_t k = 0; k < c->K; k++)
+	{
+		uint64_t idx[3] = { 0, 0, 0 };
+		for (int d = 0; d < c->dims; d++)
+			idx[d] = c->h_dir_voxels[k * c->dims + d];
+		off[k] = (idx[2] * c->n[1] + idx[1]) * c->pitch + idx[0];
+		for (uint64_t s = 0; s < S; s++)
+		{
+			iv[k * S + s] = (T)c->h_dir_values[k * S + s];
+			ic[k * S + s] = c->h_dir_conds[k * S + s] ? 1 : 0;
+		}
+	}
+	if (c->K)
+	{
+		if ((rc = dalloc(c, c->dir_offsets, off.size() * sizeof(uint64_t))))
+			return rc;
+		if ((rc = dalloc(c, c->dir_values, iv.size() * sizeof(T))))
+			return rc;
+		if ((rc = dalloc(c, c->dir_conds, ic.size())))
+			return rc;
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->dir_offsets.ptr, off.data(), off.size() * sizeof(uint64_t),
+									 cudaMemcpyHostToDevice, c->stream));
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->dir_values.ptr, iv.data(), iv.size() * sizeof(T), cudaMemcpyHostToDevice,
+									 c->stream));
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->dir_conds.ptr, ic.data(), ic.size(), cudaMemcpyHostToDevice, c->stream));
+	}
+	PCG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+	c->dirichlet_dirty = false;
+	return PCG_OK;
+}
+
+template <typename T>
+static int upload_bulk(Context* c)
+{
+	if (c->bulk_mode == PCG_BULK_NONE)
+	{
+		c->bulk_dirty = false;
+		return PCG_OK;
+	}
+	const bool pv = c->bulk_mode == PCG_BULK_PER_VOXEL;
+	const uint64_t cnt = pv ? c->S * c->plane : c->S;
+	std::vector<T> tab(cnt, T(0));
+	for (int k = 0; k < 3; k++)
+	{
+		if (pv)
+		{
+			const uint64_t nx = c->n[0], rows = c->n[1] * c->n[2];
+			for (uint64_t s = 0; s < c->S; s++)
+				for (uint64_t r = 0; r < rows; r++)
+					for (uint64_t x = 0; x < nx; x++)
+						tab[s * c->plane + r * c->pitch + x] = (T)c->h_bulk[k][(s * rows + r) * nx + x];
+		}
+		else
+			for (uint64_t s = 0; s < c->S; s++)
+				tab[s] = (T)c->h_bulk[k][s];
+		int rc = dalloc(c, c->bulk[k], cnt * sizeof(T));
+		if (rc)
+			return rc;
+		PCG_CUDA_TRY(cudaMemcpy(c->bulk[k].ptr, tab.data(), cnt * sizeof(T), cudaMemcpyHostToDevice));
+	}
+	c->bulk_dirty = false;
+	return PCG_OK;
+}
+
+static int run_phases(Context* c, uint32_t phases, bool recompute)
+{
+	int rc;
+	if (phases & PCG_PHASE_DIFFUSION)
+	{
+		if ((rc = launch_sweep_x(c)))
+			return rc;
+		if (c->dims >= 2 && (rc = launch_sweep_yz(c, 1)))
+			return rc;
+		if (c->dims >= 3 && (rc = launch_sweep_yz(c, 2)))
+			return rc;
+	}
+	if ((phases & PCG_PHASE_DIRICHLET) && (rc = launch_dirichlet(c)))
+		return rc;
+	if ((phases & PCG_PHASE_BULK) && (rc = launch_bulk(c)))
+		return rc;
+	if ((phases & PCG_PHASE_CELLS) && (rc = launch_cells(c, recompute)))
+		return rc;
+	return PCG_OK;
+}
+
+static int do_initialize(Context* c)
+{
+	if (c->initialized)
+		return PCG_OK;
+	if (!c->mesh_set || c->S == 0)
+		return fail(PCG_ERR_INVALID, "mesh and substrates must be set before initialize");
+	int rc;
+	if ((rc = dalloc(c, c->field, c->plane * c->S * c->wsize)))
+		return rc;
+	if ((rc = dalloc(c, c->mass, std::max<uint64_t>(c->S, 2) * sizeof(double))))
+		return rc;
+	if ((rc = launch_fill_initial(c)))
+		return rc;
+	rc = c->wsize == 4 ? upload_coefficients<float>(c) : upload_coefficients<double>(c);
+	if (rc)
+		return rc;
+	rc = c->wsize == 4 ? upload_dirichlet<float>(c) : upload_dirichlet<double>(c);
+	if (rc)
+		return rc;
+	rc = c->wsize == 4 ? upload_bulk<float>(c) : upload_bulk<double>(c);
+	if (rc)
+		return rc;
+	// shared-memory feasibility of the sweeps, checked once here
+	if (sweep_x_smem_bytes(c) > kMaxSmemBytes)
+		return fail(PCG_ERR_UNSUPPORTED, "x extent exceeds the shared-memory sweep limit");
+	for (int axis = 1; axis < c->dims; axis++)
+		if (sweep_yz_smem_bytes(c, axis) > kMaxSmemBytes)
+			return fail(PCG_ERR_UNSUPPORTED, "line length exceeds the shared-memory sweep limit");
+	c->initialized = true;
+	return check_device(c);
+}
+
+static int alloc_agents(Context* c, uint64_t A)
+{
+	const uint64_t S = c->S;
+	int rc;
+	const size_t w = c->wsize;
+	DeviceBuffer* f64[] = { &c->a_sec, &c->a_sat, &c->a_upt, &c->a_net, &c->a_internal, &c->a_frac };
+	for (DeviceBuffer* b : f64)
+		if ((rc = dalloc(c, *b, std::max<uint64_t>(A * S, 1) * sizeof(double))))
+			return rc;
+	if ((rc = dalloc(c, c->a_pos, std::max<uint64_t>(A * c->dims, 1) * sizeof(double))))
+		return rc;
+	if ((rc = dalloc(c, c->a_vol, std::max<uint64_t>(A, 1) * sizeof(double))))
+		return rc;
+	if ((rc = dalloc(c, c->a_active, std::max<uint64_t>(A, 1))))
+		return rc;
+	if ((rc = dalloc(c, c->a_foff, std::max<uint64_t>(A, 1) * sizeof(uint32_t))))
+		return rc;
+	DeviceBuffer* rs[] = { &c->a_num, &c->a_den, &c->a_fac, &c->a_rnum, &c->a_rden, &c->a_rfac };
+	for (DeviceBuffer* b : rs)
+		if ((rc = dalloc(c, *b, std::max<uint64_t>(A * S, 1) * w)))
+			return rc;
+	if ((rc = dalloc(c, c->owner, c->plane * sizeof(uint32_t))))
+		return rc;
+	if ((rc = dalloc(c, c->counts, c->plane * sizeof(uint32_t))))
+		return rc;
+	return PCG_OK;
+}
+
+} // namespace pcg
+
+using pcg::Context;
+using pcg::fail;
+
+struct pcg_context : Context
+{};
+
+#define CTX_CHECK(ctx)                                                                                       \
+	do                                                                                                       \
+	{                                                                                                        \
+		if (!(ctx))                                                                                          \
+			return fail(PCG_ERR_INVALID, "null context");                                                    \
+	} while (0)
+
+extern "C" {
+
+const char* pcg_last_error(void) { return pcg::g_last_error.c_str(); }
+
+int pcg_create(pcg_context** out, int precision, int device)
+{
+	if (!out)
+		return fail(PCG_ERR_INVALID, "null output pointer");
+	if (precision != PCG_FP32 && precision != PCG_FP64)
+		return fail(PCG_ERR_INVALID, "precision must be PCG_FP32 or PCG_FP64");
+	int ndev = 0;
+	cudaError_t e = cudaGetDeviceCount(&ndev);
+	if (e != cudaSuccess || ndev == 0)
+	{
+		cudaGetLastError();
+		return fail(PCG_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+	}
+	if (device < 0 || device >= ndev)
+		return fail(PCG_ERR_INVALID, "device index out of range");
+	pcg::DeviceGuard g(device);
+	auto* c = new pcg_context();
+	c->device = device;
+	c->precision = precision;
+	c->wsize = precision == PCG_FP32 ? 4 : 8;
+	if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+	{
+		delete c;
+		return fail(PCG_ERR_CUDA, "cudaStreamCreate failed");
+	}
+	c->stream = c->own_stream;
+	int rc = pcg::dalloc(c, c->err, sizeof(uint32_t) * 4);
+	if (!rc)
+		rc = pcg::dalloc(c, c->flags, sizeof(uint32_t) * 4);
+	if (rc)
+	{
+		pcg_destroy(c);
+		return rc;
+	}
+	cudaMemset(c->err.ptr, 0, sizeof(uint32_t) * 4);
+	cudaMemset(c->flags.ptr, 0, sizeof(uint32_t) * 4);
+	*out = c;
+	return PCG_OK;
+}
+
+int pcg_destroy(pcg_context* c)
+{
+	if (!c)
+		return PCG_OK;
+	pcg::DeviceGuard g(c->device);
+	if (c->stream)
+		cudaStreamSynchronize(c->stream);
+	pcg::collect_timings(c);
+	pcg::DeviceBuffer* all[] = { &c->field,		 &c->coef[0],	&c->coef[1],	&c->coef[2],	 &c->coef_c[0],
+								 &c->coef_c[1],	 &c->coef_c[2], &c->err,		&c->flags,		 &c->mass,
+								 &c->staging,	 &c->dir_offsets, &c->dir_values, &c->dir_conds, &c->face_values,
+								 &c->face_conds, &c->bulk[0],	&c->bulk[1],	&c->bulk[2],	 &c->a_pos,
+								 &c->a_sec,		 &c->a_sat,		&c->a_upt,		&c->a_net,		 &c->a_vol,
+								 &c->a_active,	 &c->a_internal, &c->a_frac,	&c->a_foff,		 &c->a_num,
+								 &c->a_den,		 &c->a_fac,		&c->a_rnum,		&c->a_rden,		 &c->a_rfac,
+								 &c->owner,		 &c->counts };
+	for (auto* b : all)
+		pcg::dfree(*b);
+	for (cudaEvent_t e : c->event_pool)
+		cudaEventDestroy(e);
+	if (c->own_stream)
+		cudaStreamDestroy(c->own_stream);
+	delete c;
+	return PCG_OK;
+}
+
+int pcg_set_stream(pcg_context* c, void* stream)
+{
+	CTX_CHECK(c);
+	c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+	return PCG_OK;
+}
+
+int pcg_get_stream(pcg_context* c, void** stream)
+{
+	CTX_CHECK(c);
+	*stream = c->stream;
+	return PCG_OK;
+}
+
+int pcg_set_mesh(pcg_context* c, int dims, const int64_t bbmin[3], const int64_t bbmax[3], const uint64_t voxel[3])
+{
+	CTX_CHECK(c);
+	if (c->initialized)
+		return fail(PCG_ERR_INVALID, "the mesh cannot change after initialize");
+	if (dims < 1 || dims > 3)
+		return fail(PCG_ERR_INVALID, "dims must be 1, 2 or 3");
+	uint64_t n[3] = { 1, 1, 1 };
+	for (int a = 0; a < 3; a++)
+		if (a < dims)
+		{
+			if (voxel[a] == 0)
+				return fail(PCG_ERR_INVALID, "voxel shape must be positive on every mesh axis");
+			if (bbmax[a] <= bbmin[a])
+				return fail(PCG_ERR_INVALID, "bounding box max must exceed min on every mesh axis");
+			n[a] = (uint64_t)((bbmax[a] - bbmin[a] + (int64_t)voxel[a] - 1) / (int64_t)voxel[a]); // mesh.cpp:16-27
+		}
+	for (int a = 0; a < 3; a++)
+	{
+		c->bbmin[a] = bbmin[a];
+		c->bbmax[a] = bbmax[a];
+		c->voxel[a] = voxel[a];
+		c->n[a] = n[a];
+	}
+	c->dims = dims;
+	c->mesh_set = true;
+	c->V = n[0] * n[1] * n[2];
+	c->pitch = pcg::round_up(n[0], 32 / c->wsize); // rows start on 32-byte sectors
+	c->plane = n[2] * n[1] * c->pitch;
+	if (c->plane >= 0xffffffffull)
+		return fail(PCG_ERR_UNSUPPORTED, "a substrate plane beyond 2^32 elements is not supported");
+	return PCG_OK;
+}
+
+int pcg_get_grid(pcg_context* c, uint64_t grid[3])
+{
+	CTX_CHECK(c);
+	for (int a = 0; a < 3; a++)
+		grid[a] = c->n[a];
+	return PCG_OK;
+}
+
+int pcg_set_substrates(pcg_context* c, uint64_t S, double dt, const double* D, const double* decay,
+					   const double* initial)
+{
+	CTX_CHECK(c);
+	if (c->initialized)
+		return fail(PCG_ERR_INVALID, "substrates cannot change after initialize");
+	if (S == 0 || !D || !decay || !initial)
+		return fail(PCG_ERR_INVALID, "at least one substrate with D, decay and initial values is required");
+	c->S = S;
+	c->dt = dt;
+	c->D.assign(D, D + S);
+	c->decay.assign(decay, decay + S);
+	c->init.assign(initial, initial + S);
+	return PCG_OK;
+}
+
+int pcg_set_dirichlet_interior(pcg_context* c, uint64_t K, const uint64_t* voxels, const double* values,
+							   const uint8_t* conditions)
+{
+	CTX_CHECK(c);
+	if (!c->mesh_set || c->S == 0)
+		return fail(PCG_ERR_INVALID, "mesh and substrates must be set before Dirichlet nodes");
+	if (K && (!voxels || !values || !conditions))
+		return fail(PCG_ERR_INVALID, "null Dirichlet arrays");
+	for (uint64_t k = 0; k < K; k++)
+		for (int d = 0; d < c->dims; d++)
+			if (voxels[k * c->dims + d] >= c->n[d])
+				return fail(PCG_ERR_INVALID, "Dirichlet node " + std::to_string(k) + " lies outside the mesh");
+	pcg::DeviceGuard g(c->device);
+	c->K = K;
+	c->h_dir_voxels.assign(voxels, voxels + K * c->dims);
+	c->h_dir_values.assign(values, values + K * c->S);
+	c->h_dir_conds.assign(conditions, conditions + K * c->S);
+	c->dirichlet_dirty = true;
+	if (c->initialized)
+		return c->wsize == 4 ? pcg::upload_dirichlet<float>(c) : pcg::upload_dirichlet<double>(c);
+	return PCG_OK;
+}
+
+int pcg_set_dirichlet_boundary(pcg_context* c, int axis, int side, const double* values, const uint8_t* conditions)
+{
+	CTX_CHECK(c);
+	if (axis < 0 || axis > 2 || side < 0 || side > 1)
+		return fail(PCG_ERR_INVALID, "axis must be 0..2 and side 0 (min) or 1 (max)");
+	if (c->S == 0)
+		return fail(PCG_ERR_INVALID, "substrates must be set before boundary conditions");
+	if (values && !conditions)
+		return fail(PCG_ERR_INVALID, "boundary values need conditions");
+	pcg::DeviceGuard g(c->device);
+	c->face_on[axis][side] = values != nullptr;
+	if (values)
+	{
+		c->h_face_values[axis][side].assign(values, values + c->S);
+		c->h_face_conds[axis][side].assign(conditions, conditions + c->S);
+	}
+	c->dirichlet_dirty = true;
+	if (c->initialized)
+		return c->wsize == 4 ? pcg::upload_dirichlet<float>(c) : pcg::upload_dirichlet<double>(c);
+	return PCG_OK;
+}
+
+int pcg_set_bulk(pcg_context* c, int mode, const double* supply, const double* uptake, const double* target)
+{
+	CTX_CHECK(c);
+	if (mode != PCG_BULK_NONE && mode != PCG_BULK_UNIFORM && mode != PCG_BULK_PER_VOXEL)
+		return fail(PCG_ERR_INVALID, "unknown bulk mode");
+	if (mode != PCG_BULK_NONE && (!supply || !uptake || !target))
+		return fail(PCG_ERR_INVALID, "bulk tables must not be null");
+	if (mode != PCG_BULK_NONE && (!c->mesh_set || c->S == 0))
+		return fail(PCG_ERR_INVALID, "mesh and substrates must be set before bulk tables");
+	pcg::DeviceGuard g(c->device);
+	c->bulk_mode = mode;
+	const uint64_t cnt = mode == PCG_BULK_PER_VOXEL ? c->S * c->V : c->S;
+	const double* src[3] = { supply, uptake, target };
+	for (int k = 0; k < 3; k++)
+	{
+		if (mode == PCG_BULK_NONE)
+			c->h_bulk[k].clear();
+		else
+			c->h_bulk[k].assign(src[k], src[k] + cnt);
+	}
+	c->bulk_dirty = true;
+	if (c->initialized)
+		return c->wsize == 4 ? pcg::upload_bulk<float>(c) : pcg::upload_bulk<double>(c);
+	return PCG_OK;
+}
+
+int pcg_set_agents(pcg_context* c, uint64_t A, const double* positions, const double* secretion,
+				   const double* saturation, const double* uptake, const double* net_export, const double* volumes,
+				   const uint8_t* is_active, const double* internalized, const double* fraction_released,
+				   int compute_internalized)
+{
+	CTX_CHECK(c);
+	if (!c->mesh_set || c->S == 0)
+		return fail(PCG_ERR_INVALID, "mesh and substrates must be set before agents");
+	if (A >= 0xffffffffull)
+		return fail(PCG_ERR_UNSUPPORTED, "at most 2^32-2 agents are supported");
+	if (A && (!positions || !secretion || !saturation || !uptake || !net_export || !volumes || !is_active))
+		return fail(PCG_ERR_INVALID, "null agent arrays");
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::alloc_agents(c, A);
+	if (rc)
+		return rc;
+	c->A = A;
+	c->compute_internalized = compute_internalized != 0;
+	const uint64_t S = c->S;
+	if (A)
+	{
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_pos.ptr, positions, A * c->dims * sizeof(double), cudaMemcpyHostToDevice,
+									 c->stream));
+		const double* rates[4] = { secretion, saturation, uptake, net_export };
+		pcg::DeviceBuffer* dst[4] = { &c->a_sec, &c->a_sat, &c->a_upt, &c->a_net };
+		for (int k = 0; k < 4; k++)
+			PCG_CUDA_TRY(cudaMemcpyAsync(dst[k]->ptr, rates[k], A * S * sizeof(double), cudaMemcpyHostToDevice,
+										 c->stream));
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_vol.ptr, volumes, A * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_active.ptr, is_active, A, cudaMemcpyHostToDevice, c->stream));
+		if (internalized)
+			PCG_CUDA_TRY(cudaMemcpyAsync(c->a_internal.ptr, internalized, A * S * sizeof(double),
+										 cudaMemcpyHostToDevice, c->stream));
+		else
+			PCG_CUDA_TRY(cudaMemsetAsync(c->a_internal.ptr, 0, A * S * sizeof(double), c->stream));
+		if (fraction_released)
+			PCG_CUDA_TRY(cudaMemcpyAsync(c->a_frac.ptr, fraction_released, A * S * sizeof(double),
+										 cudaMemcpyHostToDevice, c->stream));
+		else
+			PCG_CUDA_TRY(cudaMemsetAsync(c->a_frac.ptr, 0, A * S * sizeof(double), c->stream));
+		PCG_CUDA_TRY(cudaMemsetAsync(c->counts.ptr, 0, c->plane * sizeof(uint32_t), c->stream));
+		PCG_CUDA_TRY(cudaStreamSynchronize(c->stream)); // the caller may free its arrays on return
+	}
+	c->recompute_cells = true;
+	return PCG_OK;
+}
+
+int pcg_update_agents(pcg_context* c, const double* positions, const uint8_t* is_active)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	if (c->A == 0)
+		return PCG_OK;
+	if (positions)
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_pos.ptr, positions, c->A * c->dims * sizeof(double),
+									 cudaMemcpyHostToDevice, c->stream));
+	if (is_active)
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_active.ptr, is_active, c->A, cudaMemcpyHostToDevice, c->stream));
+	PCG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+	return PCG_OK;
+}
+
+int pcg_set_internalized(pcg_context* c, const double* internalized)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	if (c->A == 0)
+		return PCG_OK;
+	PCG_CUDA_TRY(cudaMemcpyAsync(c->a_internal.ptr, internalized, c->A * c->S * sizeof(double),
+								 cudaMemcpyHostToDevice, c->stream));
+	PCG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+	return PCG_OK;
+}
+
+int pcg_initialize(pcg_context* c)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	return pcg::do_initialize(c);
+}
+
+int pcg_run_phases(pcg_context* c, uint32_t phases, int recompute_cells)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::do_initialize(c);
+	if (rc)
+		return rc;
+	return pcg::run_phases(c, phases, recompute_cells != 0);
+}
+
+int pcg_solve(pcg_context* c, uint64_t iterations)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::do_initialize(c);
+	if (rc)
+		return rc;
+	for (uint64_t it = 0; it < iterations; it++)
+		if ((rc = pcg::run_phases(c, PCG_PHASE_ALL, c->recompute_cells)))
+			return rc;
+	c->recompute_cells = false;
+	return PCG_OK;
+}
+
+int pcg_recompute_positional_data(pcg_context* c)
+{
+	CTX_CHECK(c);
+	c->recompute_cells = true;
+	return PCG_OK;
+}
+
+int pcg_release_internalized(pcg_context* c, uint64_t agent)
+{
+	CTX_CHECK(c);
+	if (!c->compute_internalized)
+		return PCG_OK; // cell_solver.cpp:353-354
+	if (agent >= c->A)
+		return fail(PCG_ERR_INVALID, "agent index out of range");
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::do_initialize(c);
+	if (rc)
+		return rc;
+	return pcg::launch_release(c, agent);
+}
+
+int pcg_get_field(pcg_context* c, void* host, int layout, int dtype)
+{
+	CTX_CHECK(c);
+	if (!host)
+		return fail(PCG_ERR_INVALID, "null host buffer");
+	if ((layout != PCG_LAYOUT_INTERLEAVED && layout != PCG_LAYOUT_PLANAR) ||
+		(dtype != PCG_DTYPE_F32 && dtype != PCG_DTYPE_F64))
+		return fail(PCG_ERR_INVALID, "bad layout or dtype");
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::do_initialize(c);
+	if (rc)
+		return rc;
+	const size_t hw = dtype == PCG_DTYPE_F32 ? 4 : 8;
+	const size_t bytes = c->V * c->S * hw;
+	if ((rc = pcg::dalloc(c, c->staging, bytes)))
+		return rc;
+	if ((rc = pcg::launch_to_host_layout(c, c->staging.ptr, layout, dtype)))
+		return rc;
+	PCG_CUDA_TRY(cudaMemcpyAsync(host, c->staging.ptr, bytes, cudaMemcpyDeviceToHost, c->stream));
+	return pcg::check_device(c);
+}
+
+int pcg_set_field(pcg_context* c, const void* host, int layout, int dtype)
+{
+	CTX_CHECK(c);
+	if (!host)
+		return fail(PCG_ERR_INVALID, "null host buffer");
+	if ((layout != PCG_LAYOUT_INTERLEAVED && layout != PCG_LAYOUT_PLANAR) ||
+		(dtype != PCG_DTYPE_F32 && dtype != PCG_DTYPE_F64))
+		return fail(PCG_ERR_INVALID, "bad layout or dtype");
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::do_initialize(c);
+	if (rc)
+		return rc;
+	const size_t hw = dtype == PCG_DTYPE_F32 ? 4 : 8;
+	const size_t bytes = c->V * c->S * hw;
+	if ((rc = pcg::dalloc(c, c->staging, bytes)))
+		return rc;
+	PCG_CUDA_TRY(cudaMemcpyAsync(c->staging.ptr, host, bytes, cudaMemcpyHostToDevice, c->stream));
+	if ((rc = pcg::launch_from_host_layout(c, c->staging.ptr, layout, dtype)))
+		return rc;
+	return pcg::check_device(c);
+}
+
+int pcg_get_density(pcg_context* c, uint64_t s, uint64_t x, uint64_t y, uint64_t z, double* value)
+{
+	CTX_CHECK(c);
+	if (!c->initialized)
+		return fail(PCG_ERR_INVALID, "not initialized");
+	if (s >= c->S || x >= c->n[0] || y >= c->n[1] || z >= c->n[2])
+		return fail(PCG_ERR_INVALID, "density index out of range");
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::check_device(c);
+	if (rc)
+		return rc;
+	const uint64_t off = s * c->plane + (z * c->n[1] + y) * c->pitch + x;
+	if (c->wsize == 4)
+	{
+		float v;
+		PCG_CUDA_TRY(cudaMemcpy(&v, static_cast<float*>(c->field.ptr) + off, 4, cudaMemcpyDeviceToHost));
+		*value = v;
+	}
+	else
+		PCG_CUDA_TRY(cudaMemcpy(value, static_cast<double*>(c->field.ptr) + off, 8, cudaMemcpyDeviceToHost));
+	return PCG_OK;
+}
+
+int pcg_get_internalized(pcg_context* c, double* host)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::check_device(c);
+	if (rc)
+		return rc;
+	if (c->A)
+		PCG_CUDA_TRY(cudaMemcpy(host, c->a_internal.ptr, c->A * c->S * sizeof(double), cudaMemcpyDeviceToHost));
+	return PCG_OK;
+}
+
+int pcg_get_counts(pcg_context* c, uint32_t* host)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::check_device(c);
+	if (rc)
+		return rc;
+	if (!c->counts.ptr)
+	{
+		memset(host, 0, c->V * sizeof(uint32_t));
+		return PCG_OK;
+	}
+	std::vector<uint32_t> full(c->plane);
+	PCG_CUDA_TRY(cudaMemcpy(full.data(), c->counts.ptr, c->plane * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+	const uint64_t rows = c->n[1] * c->n[2];
+	for (uint64_t r = 0; r < rows; r++)
+		memcpy(host + r * c->n[0], full.data() + r * c->pitch, c->n[0] * sizeof(uint32_t));
+	return PCG_OK;
+}
+
+int pcg_get_conflict(pcg_context* c, int* conflict)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::check_device(c);
+	if (rc)
+		return rc;
+	uint32_t f = 0;
+	PCG_CUDA_TRY(cudaMemcpy(&f, c->flags.ptr, sizeof(f), cudaMemcpyDeviceToHost));
+	*conflict = f != 0;
+	return PCG_OK;
+}
+
+int pcg_mass(pcg_context* c, double* host)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::do_initialize(c);
+	if (rc)
+		return rc;
+	if ((rc = pcg::launch_mass(c, static_cast<double*>(c->mass.ptr))))
+		return rc;
+	PCG_CUDA_TRY(cudaMemcpyAsync(host, c->mass.ptr, c->S * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+	return pcg::check_device(c);
+}
+
+int pcg_synchronize(pcg_context* c)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	return pcg::check_device(c);
+}
+
+int pcg_get_field_device(pcg_context* c, void** ptr, uint64_t* elem_bytes, uint64_t* pitch)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::do_initialize(c);
+	if (rc)
+		return rc;
+	*ptr = c->field.ptr;
+	*elem_bytes = c->wsize;
+	*pitch = c->pitch;
+	return PCG_OK;
+}
+
+int pcg_set_kernel_timing(pcg_context* c, int enable)
+{
+	CTX_CHECK(c);
+	c->timing = enable != 0;
+	return PCG_OK;
+}
+
+int pcg_get_kernel_stats(pcg_context* c, pcg_kernel_stat* stats, uint64_t cap, uint64_t* count)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	cudaStreamSynchronize(c->stream);
+	pcg::collect_timings(c);
+	*count = pcg::K_COUNT;
+	for (uint64_t k = 0; k < cap && k < (uint64_t)pcg::K_COUNT; k++)
+	{
+		memset(&stats[k], 0, sizeof(pcg_kernel_stat));
+		snprintf(stats[k].name, sizeof(stats[k].name), "%s", pcg::kernel_name((int)k));
+		stats[k].launches = c->stats[k].launches;
+		stats[k].total_ms = c->stats[k].total_ms;
+		stats[k].algorithmic_bytes = c->stats[k].bytes;
+	}
+	return PCG_OK;
+}
+
+int pcg_reset_kernel_stats(pcg_context* c)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	cudaStreamSynchronize(c->stream);
+	pcg::collect_timings(c);
+	for (auto& s : c->stats)
+		s = pcg::KernelStat {};
+	c->launches = 0;
+	return PCG_OK;
+}
+
+int pcg_get_launch_count(pcg_context* c, uint64_t* launches)
+{
+	CTX_CHECK(c);
+	*launches = c->launches;
+	return PCG_OK;
+}
+
+} // extern "C"

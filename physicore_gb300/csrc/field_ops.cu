@@ -1,0 +1,386 @@
+// field_ops.cu -- Dirichlet, bulk source/sink, mass and layout kernels.
+//
+// Dirichlet (openmp_solver/src/dirichlet_solver.cpp:22-93): the reference writes
+// the x-min, x-max, y-min, y-max, z-min, z-max faces one after another (a later
+// face wins on shared edges) and then the interior voxels.  Here one launch covers
+// all six faces: a thread owns one (substrate, face voxel) and applies the face
+// with the highest precedence whose condition holds, so edges resolve exactly as
+// the sequential order does; a second launch writes the interior list.
+//
+// Bulk (openmp_solver/src/bulk_solver.cpp:12-49): D = (D + dt*S*T)/(1 + dt*(U+S))
+// with S, U, T read from device tables instead of three virtual calls per element.
+#include "pcg_internal.cuh"
+
+namespace pcg {
+
+namespace {
+
+struct FaceArgs
+{
+	void* field;
+	const void* values; // real [6*S]: face f = axis*2 + side
+	const uint8_t* conds;
+	uint32_t face_mask; // bit f set when face f exists
+	uint64_t S, nx, ny, nz, pitch, plane;
+	uint64_t cnt_x, cnt_y, cnt_z; // voxels on each pair of faces
+	uint64_t total;               // per substrate
+};
+
+template <typename T>
+__global__ void dirichlet_faces_kernel(FaceArgs a)
+{
+	const T* vals = static_cast<const T*>(a.values);
+	T* f = static_cast<T*>(a.field);
+	for (uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; idx < a.total * a.S;
+		 idx += (uint64_t)gridDim.x * blockDim.x)
+	{
+		const uint64_t s = idx / a.total;
+		uint64_t k = idx % a.total;
+		uint64_t x, y, z;
+		if (k < a.cnt_x)
+		{ // x faces: k -> (side, y, z)
+			const uint64_t per = a.ny * a.nz;
+			x = (k / per) ? a.nx - 1 : 0;
+			y = (k % per) % a.ny;
+			z = (k % per) / a.ny;
+		}
+		else if ((k -= a.cnt_x) < a.cnt_y)
+		{
+			const uint64_t per = a.nx * a.nz;
+			y = (k / per) ? a.ny - 1 : 0;
+			x = (k % per) % a.nx;
+			z = (k % per) / a.nx;
+		}
+		else
+		{
+			k -= a.cnt_y;
+			const uint64_t per = a.nx * a.ny;
+			z = (k / per) ? a.nz - 1 : 0;
+			x = (k % per) % a.nx;
+			y = (k % per) / a.nx;
+		}
+		// precedence: the reference applies faces 0..5 in order, so scan 5..0
+		const uint64_t coord[3] = { x, y, z };
+		const uint64_t last[3] = { a.nx - 1, a.ny - 1, a.nz - 1 };
+		for (int fi = 5; fi >= 0; fi--)
+		{
+			if (!(a.face_mask & (1u << fi)))
+				continue;
+			const int axis = fi >> 1, side = fi & 1;
+			if (coord[axis] != (side ? last[axis] : 0))
+				continue;
+			if (a.conds[fi * a.S + s])
+			{
+				f[s * a.plane + (z * a.ny + y) * a.pitch + x] = vals[fi * a.S + s];
+				break;
+			}
+		}
+	}
+}
+
+template <typename T>
+__global__ void dirichlet_interior_kernel(T* field, const uint64_t* offsets, const T* values, const uint8_t* conds,
+										  uint64_t K, uint64_t S, uint64_t plane)
+{
+	for (uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; idx < K * S;
+		 idx += (uint64_t)gridDim.x * blockDim.x)
+	{
+		const uint64_t k = idx / S, s = idx % S;
+		if (conds[idx])
+			field[s * plane + offsets[k]] = values[idx];
+	}
+}
+
+// One CTA row-block: blockDim.x threads walk x of `rows_per_block` rows.
+template <typename T, bool PER_VOXEL>
+__global__ void bulk_kernel(T* field, const T* supply, const T* uptake, const T* target, uint64_t nx,
+							uint64_t pitch, uint64_t rows_per_s, uint64_t S, T dt)
+{
+	const uint64_t total_rows = rows_per_s * S;
+	for (uint64_t r = blockIdx.x * (uint64_t)blockDim.y + threadIdx.y; r < total_rows;
+		 r += (uint64_t)gridDim.x * blockDim.y)
+	{
+		const uint64_t s = r / rows_per_s;
+		T* row = field + r * pitch;
+		T Sr = T(0), U = T(0), Tt = T(0);
+		if (!PER_VOXEL)
+		{
+			Sr = supply[s];
+			U = uptake[s];
+			Tt = target[s];
+		}
+		for (uint64_t x = threadIdx.x; x < nx; x += blockDim.x)
+		{
+			if (PER_VOXEL)
+			{
+				const uint64_t o = r * pitch + x;
+				Sr = supply[o];
+				U = uptake[o];
+				Tt = target[o];
+			}
+			row[x] = (row[x] + dt * Sr * Tt) / (T(1) + dt * (U + Sr));
+		}
+	}
+}
+
+// FP64 mass per substrate: each warp accumulates rows with compensated FP32/FP64
+// sums, then one double atomic per warp.
+template <typename T>
+__global__ void mass_kernel(const T* field, double* out, uint64_t nx, uint64_t pitch, uint64_t rows_per_s,
+							uint64_t S)
+{
+	const uint64_t total_rows = rows_per_s * S;
+	const int lane = threadIdx.x & 31;
+	const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+	// a warp handles a contiguous run of rows of a single substrate at a time
+	for (uint64_t r = warp; r < total_rows; r += nwarps)
+	{
+		const uint64_t s = r / rows_per_s;
+		double acc = 0.0;
+		const T* row = field + r * pitch;
+		for (uint64_t x = lane; x < nx; x += 32)
+			acc += (double)row[x];
+		for (int o = 16; o > 0; o >>= 1)
+			acc += __shfl_xor_sync(0xffffffffu, acc, o);
+		if (lane == 0)
+			atomicAdd(out + s, acc);
+	}
+}
+
+template <typename T>
+__global__ void fill_kernel(T* field, const T* init, uint64_t nx, uint64_t pitch, uint64_t rows_per_s, uint64_t S)
+{
+	const uint64_t total = rows_per_s * S * pitch;
+	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+		 i += (uint64_t)gridDim.x * blockDim.x)
+	{
+		const uint64_t x = i % pitch;
+		const uint64_t s = i / (pitch * rows_per_s);
+		field[i] = x < nx ? init[s] : T(0);
+	}
+}
+
+// device field -> dense host-order buffer; OUT element type, planar or interleaved
+template <typename T, typename OUT, bool INTERLEAVED>
+__global__ void pack_kernel(const T* field, OUT* dst, uint64_t nx, uint64_t pitch, uint64_t rows_per_s, uint64_t S)
+{
+	const uint64_t V = nx * rows_per_s;
+	const uint64_t total = V * S;
+	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+		 i += (uint64_t)gridDim.x * blockDim.x)
+	{
+		uint64_t s, v;
+		if (INTERLEAVED)
+		{
+			s = i % S;
+			v = i / S;
+		}
+		else
+		{
+			s = i / V;
+			v = i % V;
+		}
+		const uint64_t x = v % nx, r = v / nx;
+		dst[i] = (OUT)field[s * rows_per_s * pitch + r * pitch + x];
+	}
+}
+
+template <typename T, typename IN, bool INTERLEAVED>
+__global__ void unpack_kernel(T* field, const IN* src, uint64_t nx, uint64_t pitch, uint64_t rows_per_s, uint64_t S)
+{
+	const uint64_t V = nx * rows_per_s;
+	const uint64_t total = V * S;
+	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+		 i += (uint64_t)gridDim.x * blockDim.x)
+	{
+		uint64_t s, v;
+		if (INTERLEAVED)
+		{
+			s = i % S;
+			v = i / S;
+		}
+		else
+		{
+			s = i / V;
+			v = i % V;
+		}
+		const uint64_t x = v % nx, r = v / nx;
+		field[s * rows_per_s * pitch + r * pitch + x] = (T)src[i];
+	}
+}
+
+unsigned grid_for(uint64_t work, unsigned block)
+{
+	uint64_t g = (work + block - 1) / block;
+	const uint64_t cap = 152ull * 16;
+	if (g > cap)
+		g = cap;
+	return (unsigned)(g ? g : 1);
+}
+
+} // namespace
+
+template <typename T>
+static int run_dirichlet(Context* c)
+{
+	const uint64_t nx = c->n[0], ny = c->n[1], nz = c->n[2];
+	FaceArgs a {};
+	uint32_t mask = 0;
+	for (int axis = 0; axis < c->dims; axis++)
+		for (int side = 0; side < 2; side++)
+			if (c->face_on[axis][side])
+				mask |= 1u << (axis * 2 + side);
+	if (mask)
+	{
+		a.field = c->field.ptr;
+		a.values = c->face_values.ptr;
+		a.conds = static_cast<const uint8_t*>(c->face_conds.ptr);
+		a.face_mask = mask;
+		a.S = c->S;
+		a.nx = nx, a.ny = ny, a.nz = nz;
+		a.pitch = c->pitch;
+		a.plane = c->plane;
+		a.cnt_x = (mask & 0x3) ? 2 * ny * nz : 0;
+		a.cnt_y = (mask & 0xc) ? 2 * nx * nz : 0;
+		a.cnt_z = (mask & 0x30) ? 2 * nx * ny : 0;
+		a.total = a.cnt_x + a.cnt_y + a.cnt_z;
+		cudaEvent_t ev;
+		launch_begin(c, K_DIRICHLET_FACES, (double)(a.total * c->S * sizeof(T)), &ev);
+		dirichlet_faces_kernel<T><<<grid_for(a.total * c->S, 256), 256, 0, c->stream>>>(a);
+		launch_end(c, K_DIRICHLET_FACES, ev);
+		PCG_CUDA_TRY(cudaGetLastError());
+	}
+	if (c->K)
+	{
+		cudaEvent_t ev;
+		launch_begin(c, K_DIRICHLET_INTERIOR, (double)(c->K * (8 + c->S * (2 * sizeof(T) + 1))), &ev);
+		dirichlet_interior_kernel<T><<<grid_for(c->K * c->S, 256), 256, 0, c->stream>>>(
+			static_cast<T*>(c->field.ptr), static_cast<const uint64_t*>(c->dir_offsets.ptr),
+			static_cast<const T*>(c->dir_values.ptr), static_cast<const uint8_t*>(c->dir_conds.ptr), c->K, c->S,
+			c->plane);
+		launch_end(c, K_DIRICHLET_INTERIOR, ev);
+		PCG_CUDA_TRY(cudaGetLastError());
+	}
+	return PCG_OK;
+}
+
+int launch_dirichlet(Context* c) { return c->wsize == 4 ? run_dirichlet<float>(c) : run_dirichlet<double>(c); }
+
+template <typename T>
+static int run_bulk(Context* c)
+{
+	if (c->bulk_mode == PCG_BULK_NONE)
+		return PCG_OK;
+	const uint64_t rows = c->n[1] * c->n[2];
+	dim3 block(64, 4);
+	const unsigned grid = grid_for(rows * c->S, 4);
+	const bool pv = c->bulk_mode == PCG_BULK_PER_VOXEL;
+	cudaEvent_t ev;
+	const double bytes = (double)(c->V * c->S * sizeof(T)) * (pv ? 5.0 : 2.0);
+	launch_begin(c, K_BULK, bytes, &ev);
+	const T* sp = static_cast<const T*>(c->bulk[0].ptr);
+	const T* up = static_cast<const T*>(c->bulk[1].ptr);
+	const T* tp = static_cast<const T*>(c->bulk[2].ptr);
+	if (pv)
+		bulk_kernel<T, true><<<grid, block, 0, c->stream>>>(static_cast<T*>(c->field.ptr), sp, up, tp, c->n[0],
+															c->pitch, rows, c->S, (T)c->dt);
+	else
+		bulk_kernel<T, false><<<grid, block, 0, c->stream>>>(static_cast<T*>(c->field.ptr), sp, up, tp, c->n[0],
+															 c->pitch, rows, c->S, (T)c->dt);
+	launch_end(c, K_BULK, ev);
+	PCG_CUDA_TRY(cudaGetLastError());
+	return PCG_OK;
+}
+
+int launch_bulk(Context* c) { return c->wsize == 4 ? run_bulk<float>(c) : run_bulk<double>(c); }
+
+template <typename T>
+static int run_mass(Context* c, double* out)
+{
+	PCG_CUDA_TRY(cudaMemsetAsync(out, 0, c->S * sizeof(double), c->stream));
+	const uint64_t rows = c->n[1] * c->n[2];
+	cudaEvent_t ev;
+	launch_begin(c, K_MASS, (double)(c->V * c->S * sizeof(T)), &ev);
+	mass_kernel<T><<<grid_for(rows * c->S * 32, 256), 256, 0, c->stream>>>(static_cast<const T*>(c->field.ptr), out,
+																			c->n[0], c->pitch, rows, c->S);
+	launch_end(c, K_MASS, ev);
+	PCG_CUDA_TRY(cudaGetLastError());
+	return PCG_OK;
+}
+
+int launch_mass(Context* c, double* out) { return c->wsize == 4 ? run_mass<float>(c, out) : run_mass<double>(c, out); }
+
+template <typename T>
+static int run_fill(Context* c)
+{
+	// initial conditions as T on the device, staged through the mass buffer (S doubles >= S T's)
+	std::vector<T> h(c->S);
+	for (uint64_t s = 0; s < c->S; s++)
+		h[s] = (T)c->init[s];
+	PCG_CUDA_TRY(cudaMemcpyAsync(c->mass.ptr, h.data(), c->S * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+	const uint64_t rows = c->n[1] * c->n[2];
+	cudaEvent_t ev;
+	launch_begin(c, K_LAYOUT, (double)(c->plane * c->S * sizeof(T)), &ev);
+	fill_kernel<T><<<grid_for(rows * c->S * c->pitch, 256), 256, 0, c->stream>>>(
+		static_cast<T*>(c->field.ptr), static_cast<const T*>(c->mass.ptr), c->n[0], c->pitch, rows, c->S);
+	launch_end(c, K_LAYOUT, ev);
+	PCG_CUDA_TRY(cudaGetLastError());
+	return PCG_OK;
+}
+
+int launch_fill_initial(Context* c) { return c->wsize == 4 ? run_fill<float>(c) : run_fill<double>(c); }
+
+template <typename T, typename H>
+static int run_pack(Context* c, void* dst, int layout)
+{
+	const uint64_t rows = c->n[1] * c->n[2];
+	const uint64_t total = c->V * c->S;
+	cudaEvent_t ev;
+	launch_begin(c, K_LAYOUT, (double)(total * (sizeof(T) + sizeof(H))), &ev);
+	if (layout == PCG_LAYOUT_INTERLEAVED)
+		pack_kernel<T, H, true><<<grid_for(total, 256), 256, 0, c->stream>>>(
+			static_cast<const T*>(c->field.ptr), static_cast<H*>(dst), c->n[0], c->pitch, rows, c->S);
+	else
+		pack_kernel<T, H, false><<<grid_for(total, 256), 256, 0, c->stream>>>(
+			static_cast<const T*>(c->field.ptr), static_cast<H*>(dst), c->n[0], c->pitch, rows, c->S);
+	launch_end(c, K_LAYOUT, ev);
+	PCG_CUDA_TRY(cudaGetLastError());
+	return PCG_OK;
+}
+
+template <typename T, typename H>
+static int run_unpack(Context* c, const void* src, int layout)
+{
+	const uint64_t rows = c->n[1] * c->n[2];
+	const uint64_t total = c->V * c->S;
+	cudaEvent_t ev;
+	launch_begin(c, K_LAYOUT, (double)(total * (sizeof(T) + sizeof(H))), &ev);
+	if (layout == PCG_LAYOUT_INTERLEAVED)
+		unpack_kernel<T, H, true><<<grid_for(total, 256), 256, 0, c->stream>>>(
+			static_cast<T*>(c->field.ptr), static_cast<const H*>(src), c->n[0], c->pitch, rows, c->S);
+	else
+		unpack_kernel<T, H, false><<<grid_for(total, 256), 256, 0, c->stream>>>(
+			static_cast<T*>(c->field.ptr), static_cast<const H*>(src), c->n[0], c->pitch, rows, c->S);
+	launch_end(c, K_LAYOUT, ev);
+	PCG_CUDA_TRY(cudaGetLastError());
+	return PCG_OK;
+}
+
+int launch_to_host_layout(Context* c, void* dst, int layout, int dtype)
+{
+	if (c->wsize == 4)
+		return dtype == PCG_DTYPE_F32 ? run_pack<float, float>(c, dst, layout) : run_pack<float, double>(c, dst, layout);
+	return dtype == PCG_DTYPE_F32 ? run_pack<double, float>(c, dst, layout) : run_pack<double, double>(c, dst, layout);
+}
+
+int launch_from_host_layout(Context* c, const void* src, int layout, int dtype)
+{
+	if (c->wsize == 4)
+		return dtype == PCG_DTYPE_F32 ? run_unpack<float, float>(c, src, layout)
+									  : run_unpack<float, double>(c, src, layout);
+	return dtype == PCG_DTYPE_F32 ? run_unpack<double, float>(c, src, layout)
+								  : run_unpack<double, double>(c, src, layout);
+}
+
+} // namespace pcg

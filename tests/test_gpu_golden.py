@@ -1,0 +1,48 @@
+"""Every reference golden case on the GB300 through the C ABI.
+
+FP64 build: the reference's own expected values and tolerances must hold, and
+every array must match the FP64 oracle to 1e-12 relative.
+FP32 build: every array must match the FP64 oracle to 1e-5 relative, where the
+normaliser is the largest |oracle| value of the same substrate (the last axis)
+and of the same array.
+"""
+import numpy as np
+import pytest
+
+import golden_checks as G
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-12
+FP32_RTOL = 1e-5
+
+
+def rel_err(got, ref):
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    if ref.ndim == 0:
+        return abs(got - ref) / max(abs(ref), 1e-300)
+    norm = np.max(np.abs(ref.reshape(-1, ref.shape[-1])), axis=0) if ref.ndim > 1 else np.max(np.abs(ref))
+    norm = np.maximum(norm, 1e-30)
+    err = np.abs(got - ref).reshape(-1, ref.shape[-1]) / norm if ref.ndim > 1 else np.abs(got - ref) / norm
+    return float(np.max(err)) if err.size else 0.0
+
+
+def compare(out_gpu, out_ref, rtol, name):
+    for k in out_ref:
+        e = rel_err(out_gpu[k], out_ref[k])
+        assert e <= rtol, f"{name}/{k}: relative error {e:.3e} > {rtol}"
+
+
+@pytest.mark.parametrize("name,fn", G.ALL, ids=[n for n, _ in G.ALL])
+def test_gpu_fp64_matches_reference_golden_and_oracle(pcg, oracle_mod, name, fn):
+    ref = fn(lambda: oracle_mod.OracleSolver(threads=2), check=False)
+    got = fn(lambda: pcg.Solver(pcg.FP64))
+    compare(got, ref, FP64_RTOL, name)
+
+
+@pytest.mark.parametrize("name,fn", G.ALL, ids=[n for n, _ in G.ALL])
+def test_gpu_fp32_matches_oracle(pcg, oracle_mod, name, fn):
+    ref = fn(lambda: oracle_mod.OracleSolver(threads=2), check=False)
+    got = fn(lambda: pcg.Solver(pcg.FP32), check=False)
+    compare(got, ref, FP32_RTOL, name)

@@ -1,0 +1,139 @@
+"""Randomised parity of the GB300 path against the FP64 oracle.
+
+Small random problems cover every branch (dims 1-3, n = 1 axes, 1-9 substrates,
+random faces and conditions, interior nodes, uniform and per-voxel bulk tables,
+colliding and inactive agents, internalized tracking on and off, multi-step solves,
+recompute after agent moves).  Tolerances: 1e-12 relative (FP64 build), 1e-5
+relative (FP32 build), normalised per substrate by max |oracle|.  Ballot counts
+and the conflict flag are integers and must be identical.
+"""
+import zlib
+
+import numpy as np
+import pytest
+
+from physicore_gb300 import workloads as W
+from test_gpu_golden import rel_err
+
+pytestmark = pytest.mark.gpu
+
+SEEDS = list(range(40))
+
+
+def run_both(pcg, oracle_mod, p, precision, steps=(1, 2, 1)):
+    g = W.apply(pcg.Solver(precision), p)
+    o = W.apply(oracle_mod.OracleSolver(threads=2), p)
+    rng = np.random.default_rng(1000 + zlib.crc32(p["name"].encode()) % 1000)
+    snaps = []
+    for k, n in enumerate(steps):
+        if k == 2 and g.A > 0:
+            # agents move, one toggles activity; both solvers are told to recompute
+            a = p["agents"]
+            pos = a["positions"].copy()
+            order = rng.permutation(g.A)
+            pos = pos[order]
+            act = a["is_active"].copy()
+            act[rng.integers(0, g.A)] ^= 1
+            for s in (g, o):
+                s.update_agents(positions=pos, is_active=act)
+                s.recompute_positional_data()
+        g.solve(n)
+        o.solve(n)
+        snap = dict(field=(g.get_field(), o.get_field()))
+        if g.A:
+            snap["internalized"] = (g.get_internalized(), o.get_internalized())
+            snap["counts"] = (g.get_counts(), o.get_counts())
+            snap["conflict"] = (g.get_conflict(), o.get_conflict())
+        snaps.append(snap)
+    return snaps
+
+
+def check(snaps, rtol, name):
+    for k, snap in enumerate(snaps):
+        for key, (got, ref) in snap.items():
+            if key in ("counts", "conflict"):
+                assert np.array_equal(np.asarray(got), np.asarray(ref)), f"{name} step {k}: {key} differ"
+            else:
+                e = rel_err(got, ref)
+                assert e <= rtol, f"{name} step {k}: {key} relative error {e:.3e} > {rtol}"
+
+
+@pytest.mark.parametrize("seed", SEEDS)
+def test_random_fp64(pcg, oracle_mod, seed):
+    p = W.random_small(seed)
+    check(run_both(pcg, oracle_mod, p, pcg.FP64), 1e-12, p["name"])
+
+
+@pytest.mark.parametrize("seed", SEEDS)
+def test_random_fp32(pcg, oracle_mod, seed):
+    p = W.random_small(seed)
+    check(run_both(pcg, oracle_mod, p, pcg.FP32), 1e-5, p["name"])
+
+
+@pytest.mark.parametrize("n,S", [(1, 1), (2, 3), (3, 5), (4, 2), (33, 7), (64, 1), (65, 4), (130, 2), (320, 1)])
+def test_sweep_line_lengths(pcg, oracle_mod, n, S):
+    """Line lengths around the 16-byte vector and 32-lane tile edges, in every axis."""
+    rng = np.random.default_rng(n * 31 + S)
+    for dims, shape in [(1, (n, 1, 1)), (2, (5, n, 1)), (3, (3, 4, n)), (3, (n, 3, 2))]:
+        p = dict(name=f"lines_{n}_{S}_{dims}", dims=dims, bbmin=(0, 0, 0),
+                 bbmax=tuple(shape[a] * 10 if a < dims else 0 for a in range(3)), voxel=(10, 10, 10), dt=0.05,
+                 D=W.log_uniform(rng, 1, 1e4, S), decay=W.log_uniform(rng, 1e-3, 1, S), initial=np.zeros(S),
+                 field=rng.random((shape[2], shape[1], shape[0], S)), field_layout="interleaved", boundary=[],
+                 interior=None, bulk=None, agents=None, compute_internalized=False)
+        for prec, tol in ((pcg.FP64, 1e-12), (pcg.FP32, 1e-5)):
+            g = W.apply(pcg.Solver(prec), p)
+            o = W.apply(oracle_mod.OracleSolver(threads=2), p)
+            g.solve(3)
+            o.solve(3)
+            e = rel_err(g.get_field(), o.get_field())
+            assert e <= tol, f"{p['name']} prec {prec}: {e:.3e}"
+
+
+def test_layouts_round_trip(pcg):
+    p = W.random_small(7)
+    g = W.apply(pcg.Solver(pcg.FP64), p)
+    f = g.get_field()
+    planar = g.get_field(layout=pcg.LAYOUT_PLANAR)
+    assert np.array_equal(np.moveaxis(planar, 0, -1), f)
+    g.set_field(planar, layout=pcg.LAYOUT_PLANAR)
+    assert np.array_equal(g.get_field(), f)
+    f32 = g.get_field(dtype=np.float32)
+    assert np.array_equal(f32, f.astype(np.float32))
+    nx, ny, nz = g.grid
+    for _ in range(5):
+        s, x, y, z = [int(np.random.randint(0, m)) for m in (g.S, nx, ny, nz)]
+        assert g.get_density(s, x, y, z) == f[z, y, x, s]
+
+
+def test_mass_identity_pure_diffusion(pcg):
+    """Without Dirichlet, bulk or agents each sweep scales the mass of substrate s by
+    exactly 1/(1 + decay*dt/dims) (column sums of the ADI matrix)."""
+    rng = np.random.default_rng(5)
+    S = 3
+    D = np.array([10.0, 1e3, 1e5])
+    decay = np.array([0.1, 0.5, 1e-3])
+    p = dict(name="mass", dims=3, bbmin=(0, 0, 0), bbmax=(400, 300, 200), voxel=(10, 10, 10), dt=0.01, D=D,
+             decay=decay, initial=np.zeros(S), field=rng.random((20, 30, 40, S)), field_layout="interleaved",
+             boundary=[], interior=None, bulk=None, agents=None, compute_internalized=False)
+    g = W.apply(pcg.Solver(pcg.FP64), p)
+    m0 = g.mass()
+    g.solve(4)
+    m1 = g.mass()
+    expect = m0 * (1.0 / (1.0 + decay * 0.01 / 3)) ** (3 * 4)
+    assert np.allclose(m1, expect, rtol=1e-12, atol=0)
+
+
+def test_agent_outside_mesh_reports_error(pcg):
+    p = W.random_small(3)
+    g = W.apply(pcg.Solver(pcg.FP64), p)
+    if g.A == 0:
+        pytest.skip("no agents in this draw")
+    pos = p["agents"]["positions"].copy()
+    act = np.ones(g.A, np.uint8)
+    pos[0, 0] = p["bbmax"][0] + 1e6  # far outside: the kernel flags it, never indexes with it
+    g.update_agents(positions=pos, is_active=act)
+    g.recompute_positional_data()
+    g.solve(1)
+    with pytest.raises(pcg.PcgError) as ei:
+        g.synchronize()
+    assert ei.value.code == 4 and "outside" in str(ei.value)
