@@ -237,8 +237,16 @@ uint64_t sweep_x_smem_pitch(const Context* c);
 #ifdef __CUDACC__
 namespace pcg::dev {
 
-// Bounded mbarrier wait: spins at most `limit` polls, then flags DEV_ERR_WAIT_TIMEOUT.
-constexpr uint32_t kWaitLimit = 1u << 26;
+// Bounded mbarrier wait: gives up after kWaitNs nanoseconds of %globaltimer time
+// (a tile load takes microseconds), and the caller flags DEV_ERR_WAIT_TIMEOUT.
+constexpr uint64_t kWaitNs = 50ull * 1000 * 1000;
+
+__device__ __forceinline__ uint64_t global_ns()
+{
+	uint64_t t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p)
 {
@@ -265,7 +273,8 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase)
 {
 	const uint32_t addr = smem_addr(bar);
-	for (uint32_t i = 0; i < kWaitLimit; i++)
+	const uint64_t t0 = global_ns();
+	for (;;)
 	{
 		uint32_t done;
 		asm volatile(
@@ -277,8 +286,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase)
 			: "memory");
 		if (done)
 			return true;
+		if (global_ns() - t0 > kWaitNs)
+			return false;
 	}
-	return false;
 }
 
 // Bulk copy global -> shared, completing on `bar` (size and both addresses 16-byte aligned).

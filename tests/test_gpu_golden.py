@@ -30,7 +30,13 @@ def rel_err(got, ref):
 
 def compare(out_gpu, out_ref, rtol, name):
     for k in out_ref:
-        e = rel_err(out_gpu[k], out_ref[k])
+        if k == "field3" and "field2" in out_ref:
+            # after release_internalized, D = D' + I*F/Vv cancels values of magnitude
+            # max|field2| down to ~1: the error scale is that of the operands
+            scale = float(np.max(np.abs(out_ref["field2"])))
+            e = float(np.max(np.abs(np.asarray(out_gpu[k]) - np.asarray(out_ref[k])))) / scale
+        else:
+            e = rel_err(out_gpu[k], out_ref[k])
         assert e <= rtol, f"{name}/{k}: relative error {e:.3e} > {rtol}"
 
 
@@ -41,8 +47,22 @@ def test_gpu_fp64_matches_reference_golden_and_oracle(pcg, oracle_mod, name, fn)
     compare(got, ref, FP64_RTOL, name)
 
 
+def compare_fp32(out_gpu, out_ref, name, voxel_volume=8000.0):
+    """Fields: 1e-5 relative per substrate.  Internalized amounts (FP64 in both builds)
+    accumulate Vv*(D - D') from FP32 densities, so their error scale is Vv times the
+    density magnitude: |dI| <= 1e-5 * Vv * max|field| of the substrate."""
+    fields = {k: v for k, v in out_ref.items() if not k.startswith("int")}
+    compare({k: out_gpu[k] for k in fields}, fields, FP32_RTOL, name)
+    dens = [v for k, v in out_ref.items() if not k.startswith("int") and np.ndim(v) >= 1]
+    for k in (k for k in out_ref if k.startswith("int")):
+        ref = np.asarray(out_ref[k], dtype=np.float64)
+        scale = voxel_volume * max(float(np.max(np.abs(d))) for d in dens)
+        e = float(np.max(np.abs(np.asarray(out_gpu[k]) - ref))) / scale if ref.size else 0.0
+        assert e <= FP32_RTOL, f"{name}/{k}: error {e:.3e} of Vv*max|D| > {FP32_RTOL}"
+
+
 @pytest.mark.parametrize("name,fn", G.ALL, ids=[n for n, _ in G.ALL])
 def test_gpu_fp32_matches_oracle(pcg, oracle_mod, name, fn):
     ref = fn(lambda: oracle_mod.OracleSolver(threads=2), check=False)
     got = fn(lambda: pcg.Solver(pcg.FP32), check=False)
-    compare(got, ref, FP32_RTOL, name)
+    compare_fp32(got, ref, name)
