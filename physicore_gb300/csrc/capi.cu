@@ -113,8 +113,6 @@ void collect_timings(Context* c)
 
 // ------------------------------------------------------------------ helpers
 
-static uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
-
 struct DeviceGuard
 {
 	int prev = -1;
@@ -187,39 +185,40 @@ static void precompute_axis(uint64_t n, uint64_t S, uint64_t shape, uint64_t dim
 		}
 }
 
+// Device coefficient table of one axis: [B | E | C], C[s] = c.  For x, B and E are
+// flat in the field's (i, s) order, B[i*S+s] = b'_i, E[i*S+s] = e_{i-1} (0 at i = 0),
+// so a 16-byte chunk of coefficients matches a chunk of a row.  For y and z they are
+// per-substrate rows, B[s*cp + i], padded to cp = a multiple of the solver block.
 template <typename T>
 static int upload_coefficients(Context* c)
 {
+	const uint64_t S = c->S;
 	for (int axis = 0; axis < c->dims; axis++)
 	{
 		const uint64_t n = c->n[axis];
 		std::vector<double> b, e, cc;
-		precompute_axis(n, c->S, c->voxel[axis], (uint64_t)c->dims, c->dt, c->D.data(), c->decay.data(), b, e, cc);
-		const uint64_t npad = round_up(n, 16 / sizeof(T));
-		c->coef_pitch[axis] = 2 * npad;
-		std::vector<T> tab(c->S * 2 * npad, T(0));
-		std::vector<T> tc(c->S);
-		for (uint64_t s = 0; s < c->S; s++)
-		{
-			T* B = tab.data() + s * 2 * npad;
-			T* E = B + npad;
-			for (uint64_t i = 0; i < n; i++)
+		precompute_axis(n, S, c->voxel[axis], (uint64_t)c->dims, c->dt, c->D.data(), c->decay.data(), b, e, cc);
+		const uint64_t cp = coef_row_pitch(n);
+		const uint64_t len = axis == 0 ? coef_table_len(n, S, sizeof(T)) : S * cp;
+		const uint64_t total = 2 * len + round_up(S, 16 / sizeof(T));
+		c->coef_len[axis] = len;
+		c->coef_elems[axis] = total;
+		std::vector<T> tab(total, T(0));
+		for (uint64_t i = 0; i < n; i++)
+			for (uint64_t s = 0; s < S; s++)
 			{
-				B[i] = (T)b[i * c->S + s];
-				E[i] = i == 0 ? T(0) : (T)e[(i - 1) * c->S + s];
+				const uint64_t at = axis == 0 ? i * S + s : s * cp + i;
+				tab[at] = (T)b[i * S + s];
+				tab[len + at] = i == 0 ? T(0) : (T)e[(i - 1) * S + s];
 			}
-			tc[s] = (T)cc[s];
-		}
+		for (uint64_t s = 0; s < S; s++)
+			tab[2 * len + s] = (T)cc[s];
 		int rc = dalloc(c, c->coef[axis], tab.size() * sizeof(T));
 		if (rc)
 			return rc;
-		if ((rc = dalloc(c, c->coef_c[axis], tc.size() * sizeof(T))))
-			return rc;
 		PCG_CUDA_TRY(cudaMemcpyAsync(c->coef[axis].ptr, tab.data(), tab.size() * sizeof(T), cudaMemcpyHostToDevice,
 									 c->stream));
-		PCG_CUDA_TRY(cudaMemcpyAsync(c->coef_c[axis].ptr, tc.data(), tc.size() * sizeof(T), cudaMemcpyHostToDevice,
-									 c->stream));
-		PCG_CUDA_TRY(cudaStreamSynchronize(c->stream)); // host vectors die at scope exit
+		PCG_CUDA_TRY(cudaStreamSynchronize(c->stream)); // the host table dies at scope exit
 	}
 	return PCG_OK;
 }
@@ -256,7 +255,7 @@ static int upload_dirichlet(Context* c)
 		uint64_t idx[3] = { 0, 0, 0 };
 		for (int d = 0; d < c->dims; d++)
 			idx[d] = c->h_dir_voxels[k * c->dims + d];
-		off[k] = (idx[2] * c->n[1] + idx[1]) * c->pitch + idx[0];
+		off[k] = (idx[2] * c->n[1] + idx[1]) * c->pitch + idx[0] * S;
 		for (uint64_t s = 0; s < S; s++)
 		{
 			iv[k * S + s] = (T)c->h_dir_values[k * S + s];
@@ -278,30 +277,28 @@ static int upload_dirichlet(Context* c)
 		PCG_CUDA_TRY(cudaMemcpyAsync(c->dir_conds.ptr, ic.data(), ic.size(), cudaMemcpyHostToDevice, c->stream));
 	}
 	PCG_CUDA_TRY(cudaStreamSynchronize(c->stream));
-	c->dirichlet_dirty = false;
 	return PCG_OK;
 }
 
+// Bulk tables: [S] (uniform) or shaped like the field (per voxel, interleaved rows)
+// from the host's planar [s][z][y][x] arrays.
 template <typename T>
 static int upload_bulk(Context* c)
 {
 	if (c->bulk_mode == PCG_BULK_NONE)
-	{
-		c->bulk_dirty = false;
 		return PCG_OK;
-	}
 	const bool pv = c->bulk_mode == PCG_BULK_PER_VOXEL;
-	const uint64_t cnt = pv ? c->S * c->plane : c->S;
+	const uint64_t cnt = pv ? c->rows * c->pitch : c->S;
 	std::vector<T> tab(cnt, T(0));
 	for (int k = 0; k < 3; k++)
 	{
 		if (pv)
 		{
-			const uint64_t nx = c->n[0], rows = c->n[1] * c->n[2];
-			for (uint64_t s = 0; s < c->S; s++)
+			const uint64_t nx = c->n[0], rows = c->rows, S = c->S;
+			for (uint64_t s = 0; s < S; s++)
 				for (uint64_t r = 0; r < rows; r++)
 					for (uint64_t x = 0; x < nx; x++)
-						tab[s * c->plane + r * c->pitch + x] = (T)c->h_bulk[k][(s * rows + r) * nx + x];
+						tab[r * c->pitch + x * S + s] = (T)c->h_bulk[k][(s * rows + r) * nx + x];
 		}
 		else
 			for (uint64_t s = 0; s < c->S; s++)
@@ -311,7 +308,6 @@ static int upload_bulk(Context* c)
 			return rc;
 		PCG_CUDA_TRY(cudaMemcpy(c->bulk[k].ptr, tab.data(), cnt * sizeof(T), cudaMemcpyHostToDevice));
 	}
-	c->bulk_dirty = false;
 	return PCG_OK;
 }
 
@@ -336,6 +332,18 @@ static int run_phases(Context* c, uint32_t phases, bool recompute)
 	return PCG_OK;
 }
 
+// Row geometry of the interleaved field: a row holds nx*S elements and is padded
+// to a multiple of 32 bytes.
+static int derive_layout(Context* c)
+{
+	c->row_len = c->n[0] * c->S;
+	c->pitch = round_up(c->row_len, 32 / c->wsize);
+	c->rows = c->n[1] * c->n[2];
+	if (c->rows * c->pitch >= 0xffffffffull)
+		return fail(PCG_ERR_UNSUPPORTED, "fields beyond 2^32 elements are not supported");
+	return PCG_OK;
+}
+
 static int do_initialize(Context* c)
 {
 	if (c->initialized)
@@ -343,7 +351,11 @@ static int do_initialize(Context* c)
 	if (!c->mesh_set || c->S == 0)
 		return fail(PCG_ERR_INVALID, "mesh and substrates must be set before initialize");
 	int rc;
-	if ((rc = dalloc(c, c->field, c->plane * c->S * c->wsize)))
+	if ((rc = derive_layout(c)))
+		return rc;
+	if ((rc = dalloc(c, c->field, c->rows * c->pitch * c->wsize)))
+		return rc;
+	if ((rc = prepare_sweep_maps(c)))
 		return rc;
 	if ((rc = dalloc(c, c->mass, std::max<uint64_t>(c->S, 2) * sizeof(double))))
 		return rc;
@@ -359,11 +371,10 @@ static int do_initialize(Context* c)
 	if (rc)
 		return rc;
 	// shared-memory feasibility of the sweeps, checked once here
-	if (sweep_x_smem_bytes(c) > kMaxSmemBytes)
-		return fail(PCG_ERR_UNSUPPORTED, "x extent exceeds the shared-memory sweep limit");
-	for (int axis = 1; axis < c->dims; axis++)
-		if (sweep_yz_smem_bytes(c, axis) > kMaxSmemBytes)
-			return fail(PCG_ERR_UNSUPPORTED, "line length exceeds the shared-memory sweep limit");
+	for (int axis = 0; axis < c->dims; axis++)
+		if (sweep_smem_bytes(c, axis) > kMaxSmemBytes)
+			return fail(PCG_ERR_UNSUPPORTED, "a line of axis " + std::to_string(axis) +
+												 " exceeds the shared-memory sweep limit");
 	c->initialized = true;
 	return check_device(c);
 }
@@ -385,13 +396,15 @@ static int alloc_agents(Context* c, uint64_t A)
 		return rc;
 	if ((rc = dalloc(c, c->a_foff, std::max<uint64_t>(A, 1) * sizeof(uint32_t))))
 		return rc;
+	if ((rc = dalloc(c, c->a_vox, std::max<uint64_t>(A, 1) * sizeof(uint32_t))))
+		return rc;
 	DeviceBuffer* rs[] = { &c->a_num, &c->a_den, &c->a_fac, &c->a_rnum, &c->a_rden, &c->a_rfac };
 	for (DeviceBuffer* b : rs)
 		if ((rc = dalloc(c, *b, std::max<uint64_t>(A * S, 1) * w)))
 			return rc;
-	if ((rc = dalloc(c, c->owner, c->plane * sizeof(uint32_t))))
+	if ((rc = dalloc(c, c->owner, c->V * sizeof(uint32_t))))
 		return rc;
-	if ((rc = dalloc(c, c->counts, c->plane * sizeof(uint32_t))))
+	if ((rc = dalloc(c, c->counts, c->V * sizeof(uint32_t))))
 		return rc;
 	return PCG_OK;
 }
@@ -435,6 +448,7 @@ int pcg_create(pcg_context** out, int precision, int device)
 	c->device = device;
 	c->precision = precision;
 	c->wsize = precision == PCG_FP32 ? 4 : 8;
+	cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
 	if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
 	{
 		delete c;
@@ -463,8 +477,8 @@ int pcg_destroy(pcg_context* c)
 	if (c->stream)
 		cudaStreamSynchronize(c->stream);
 	pcg::collect_timings(c);
-	pcg::DeviceBuffer* all[] = { &c->field,		 &c->coef[0],	&c->coef[1],	&c->coef[2],	 &c->coef_c[0],
-								 &c->coef_c[1],	 &c->coef_c[2], &c->err,		&c->flags,		 &c->mass,
+	pcg::DeviceBuffer* all[] = { &c->field,		 &c->coef[0],	&c->coef[1],	&c->coef[2],	 &c->a_vox,
+								 &c->err,		&c->flags,		 &c->mass,
 								 &c->staging,	 &c->dir_offsets, &c->dir_values, &c->dir_conds, &c->face_values,
 								 &c->face_conds, &c->bulk[0],	&c->bulk[1],	&c->bulk[2],	 &c->a_pos,
 								 &c->a_sec,		 &c->a_sat,		&c->a_upt,		&c->a_net,		 &c->a_vol,
@@ -522,10 +536,8 @@ int pcg_set_mesh(pcg_context* c, int dims, const int64_t bbmin[3], const int64_t
 	c->dims = dims;
 	c->mesh_set = true;
 	c->V = n[0] * n[1] * n[2];
-	c->pitch = pcg::round_up(n[0], 32 / c->wsize); // rows start on 32-byte sectors
-	c->plane = n[2] * n[1] * c->pitch;
-	if (c->plane >= 0xffffffffull)
-		return fail(PCG_ERR_UNSUPPORTED, "a substrate plane beyond 2^32 elements is not supported");
+	if (c->V >= 0xffffffffull)
+		return fail(PCG_ERR_UNSUPPORTED, "meshes beyond 2^32-1 voxels are not supported");
 	return PCG_OK;
 }
 
@@ -570,7 +582,6 @@ int pcg_set_dirichlet_interior(pcg_context* c, uint64_t K, const uint64_t* voxel
 	c->h_dir_voxels.assign(voxels, voxels + K * c->dims);
 	c->h_dir_values.assign(values, values + K * c->S);
 	c->h_dir_conds.assign(conditions, conditions + K * c->S);
-	c->dirichlet_dirty = true;
 	if (c->initialized)
 		return c->wsize == 4 ? pcg::upload_dirichlet<float>(c) : pcg::upload_dirichlet<double>(c);
 	return PCG_OK;
@@ -592,7 +603,6 @@ int pcg_set_dirichlet_boundary(pcg_context* c, int axis, int side, const double*
 		c->h_face_values[axis][side].assign(values, values + c->S);
 		c->h_face_conds[axis][side].assign(conditions, conditions + c->S);
 	}
-	c->dirichlet_dirty = true;
 	if (c->initialized)
 		return c->wsize == 4 ? pcg::upload_dirichlet<float>(c) : pcg::upload_dirichlet<double>(c);
 	return PCG_OK;
@@ -618,7 +628,6 @@ int pcg_set_bulk(pcg_context* c, int mode, const double* supply, const double* u
 		else
 			c->h_bulk[k].assign(src[k], src[k] + cnt);
 	}
-	c->bulk_dirty = true;
 	if (c->initialized)
 		return c->wsize == 4 ? pcg::upload_bulk<float>(c) : pcg::upload_bulk<double>(c);
 	return PCG_OK;
@@ -664,7 +673,7 @@ int pcg_set_agents(pcg_context* c, uint64_t A, const double* positions, const do
 										 cudaMemcpyHostToDevice, c->stream));
 		else
 			PCG_CUDA_TRY(cudaMemsetAsync(c->a_frac.ptr, 0, A * S * sizeof(double), c->stream));
-		PCG_CUDA_TRY(cudaMemsetAsync(c->counts.ptr, 0, c->plane * sizeof(uint32_t), c->stream));
+		PCG_CUDA_TRY(cudaMemsetAsync(c->counts.ptr, 0, c->V * sizeof(uint32_t), c->stream));
 		PCG_CUDA_TRY(cudaStreamSynchronize(c->stream)); // the caller may free its arrays on return
 	}
 	c->recompute_cells = true;
@@ -763,6 +772,13 @@ int pcg_get_field(pcg_context* c, void* host, int layout, int dtype)
 	if (rc)
 		return rc;
 	const size_t hw = dtype == PCG_DTYPE_F32 ? 4 : 8;
+	if (layout == PCG_LAYOUT_INTERLEAVED && hw == c->wsize)
+	{
+		// the device rows are the host rows plus padding: one strided copy, no kernel
+		PCG_CUDA_TRY(cudaMemcpy2DAsync(host, c->row_len * hw, c->field.ptr, c->pitch * hw, c->row_len * hw, c->rows,
+									   cudaMemcpyDeviceToHost, c->stream));
+		return pcg::check_device(c);
+	}
 	const size_t bytes = c->V * c->S * hw;
 	if ((rc = pcg::dalloc(c, c->staging, bytes)))
 		return rc;
@@ -785,6 +801,12 @@ int pcg_set_field(pcg_context* c, const void* host, int layout, int dtype)
 	if (rc)
 		return rc;
 	const size_t hw = dtype == PCG_DTYPE_F32 ? 4 : 8;
+	if (layout == PCG_LAYOUT_INTERLEAVED && hw == c->wsize)
+	{
+		PCG_CUDA_TRY(cudaMemcpy2DAsync(c->field.ptr, c->pitch * hw, host, c->row_len * hw, c->row_len * hw, c->rows,
+									   cudaMemcpyHostToDevice, c->stream));
+		return pcg::check_device(c);
+	}
 	const size_t bytes = c->V * c->S * hw;
 	if ((rc = pcg::dalloc(c, c->staging, bytes)))
 		return rc;
@@ -805,7 +827,7 @@ int pcg_get_density(pcg_context* c, uint64_t s, uint64_t x, uint64_t y, uint64_t
 	int rc = pcg::check_device(c);
 	if (rc)
 		return rc;
-	const uint64_t off = s * c->plane + (z * c->n[1] + y) * c->pitch + x;
+	const uint64_t off = (z * c->n[1] + y) * c->pitch + x * c->S + s;
 	if (c->wsize == 4)
 	{
 		float v;
@@ -841,11 +863,7 @@ int pcg_get_counts(pcg_context* c, uint32_t* host)
 		memset(host, 0, c->V * sizeof(uint32_t));
 		return PCG_OK;
 	}
-	std::vector<uint32_t> full(c->plane);
-	PCG_CUDA_TRY(cudaMemcpy(full.data(), c->counts.ptr, c->plane * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-	const uint64_t rows = c->n[1] * c->n[2];
-	for (uint64_t r = 0; r < rows; r++)
-		memcpy(host + r * c->n[0], full.data() + r * c->pitch, c->n[0] * sizeof(uint32_t));
+	PCG_CUDA_TRY(cudaMemcpy(host, c->counts.ptr, c->V * sizeof(uint32_t), cudaMemcpyDeviceToHost));
 	return PCG_OK;
 }
 

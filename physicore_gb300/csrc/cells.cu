@@ -22,9 +22,9 @@
 //    step never waits on the host (the Thrust backend copies it back every step,
 //    thrust_solver/src/cell_solver.cpp:251-252).
 //  * apply/internalize read the flag on the device and take the reference's
-//    fused or two-pass branch.
-//  Internalized substrates are kept in FP64 in both builds; the FP32 build
-//  differences densities in FP64 before accumulating them.
+//    fused or two-pass branch.  A voxel's substrates are adjacent in the field, so
+//    each agent touches one 32-byte sector of densities (S <= 8, FP32).
+//  Internalized substrates are kept in FP64 in both builds.
 #include "pcg_internal.cuh"
 
 namespace pcg {
@@ -40,11 +40,12 @@ struct CellArgs
 	uint64_t n[3];
 	double bbmin[3];
 	double voxel[3];
-	uint64_t pitch, plane;
+	uint64_t pitch;
 	double Vv, dt;
 	const double *pos, *sec, *sat, *upt, *net, *vol, *frac;
 	const uint8_t* active;
 	double* internal;
+	uint32_t* vox;
 	uint32_t* foff;
 	void *num, *den, *fac, *rnum, *rden, *rfac;
 	uint32_t* owner;
@@ -55,6 +56,20 @@ struct CellArgs
 	int internalized;
 };
 
+// cartesian_mesh::voxel_position (mesh.cpp:37-61); false when outside the grid.
+__device__ __forceinline__ bool locate(const CellArgs& a, uint64_t i, uint64_t idx[3])
+{
+	idx[0] = idx[1] = idx[2] = 0;
+	for (int d = 0; d < a.dims; d++)
+	{
+		const double q = (a.pos[i * a.dims + d] - a.bbmin[d]) / a.voxel[d];
+		if (!(q >= 0.0) || q >= (double)a.n[d])
+			return false;
+		idx[d] = (uint64_t)q;
+	}
+	return true;
+}
+
 // compute_intermediates + clear_ballots (cell_solver.cpp:22-77)
 template <typename T>
 __global__ void cells_locate_kernel(CellArgs a)
@@ -64,33 +79,22 @@ __global__ void cells_locate_kernel(CellArgs a)
 		a.flags[0] = 0;
 	if (i >= a.A)
 		return;
+	uint64_t idx[3];
 	if (!a.active[i])
 	{
-		a.foff[i] = kNoAgent;
+		a.vox[i] = kNoAgent;
 		return;
 	}
-	uint64_t idx[3] = { 0, 0, 0 };
-	bool inside = true;
-	for (int d = 0; d < a.dims; d++)
-	{
-		const double p = a.pos[i * a.dims + d];
-		const double q = (p - a.bbmin[d]) / a.voxel[d];
-		if (!(q >= 0.0) || q >= (double)a.n[d])
-		{
-			inside = false;
-			break;
-		}
-		idx[d] = (uint64_t)q;
-	}
-	if (!inside)
+	if (!locate(a, i, idx))
 	{
 		atomicOr(a.err, DEV_ERR_AGENT_OUTSIDE);
-		a.foff[i] = kNoAgent;
+		a.vox[i] = kNoAgent;
 		return;
 	}
-	const uint32_t off = (uint32_t)((idx[2] * a.n[1] + idx[1]) * a.pitch + idx[0]);
-	a.foff[i] = off;
-	a.owner[off] = kNoAgent;
+	const uint32_t v = (uint32_t)(idx[0] + a.n[0] * (idx[1] + a.n[1] * idx[2]));
+	a.vox[i] = v;
+	a.foff[i] = (uint32_t)((idx[2] * a.n[1] + idx[1]) * a.pitch + idx[0] * a.S);
+	a.owner[v] = kNoAgent;
 	T* num = static_cast<T*>(a.num);
 	T* den = static_cast<T*>(a.den);
 	T* fac = static_cast<T*>(a.fac);
@@ -114,7 +118,7 @@ __global__ void cells_locate_kernel(CellArgs a)
 __global__ void cells_ballot_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-	const uint32_t key = i < a.A ? a.foff[i] : kNoAgent;
+	const uint32_t key = i < a.A ? a.vox[i] : kNoAgent;
 	const uint32_t group = __match_any_sync(0xffffffffu, key);
 	if (key == kNoAgent)
 		return;
@@ -132,7 +136,7 @@ template <typename T>
 __global__ void cells_reduce_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-	const uint32_t key = i < a.A ? a.foff[i] : kNoAgent;
+	const uint32_t key = i < a.A ? a.vox[i] : kNoAgent;
 	bool conflict = false;
 	if (key != kNoAgent)
 	{
@@ -157,41 +161,52 @@ __global__ void cells_reduce_kernel(CellArgs a)
 		atomicOr(a.flags, 1u);
 }
 
-// compute_result (cell_solver.cpp:187-227)
+constexpr int kSubBatch = 8; // substrates whose loads are issued together
+
+// compute_result (cell_solver.cpp:187-227).  All loads of a batch of substrates are
+// issued before any store, so an agent's independent memory accesses overlap.
 template <typename T>
 __global__ void cells_apply_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	if (i >= a.A)
 		return;
-	const uint32_t key = a.foff[i];
+	const uint32_t key = a.vox[i];
 	if (key == kNoAgent)
 		return;
-	const bool conflict = *(volatile uint32_t*)a.flags != 0;
-	const T* rnum = static_cast<const T*>(a.rnum);
-	const T* rden = static_cast<const T*>(a.rden);
-	const T* rfac = static_cast<const T*>(a.rfac);
-	T* field = static_cast<T*>(a.field);
-	if (a.internalized && !conflict)
-	{
-		for (uint64_t s = 0; s < a.S; s++)
-		{
-			const uint64_t k = i * a.S + s;
-			T* D = field + s * a.plane + key;
-			const T prev = *D;
-			const T next = (prev + rnum[k]) / rden[k] + rfac[k];
-			*D = next;
-			a.internal[k] += a.Vv * ((double)prev - (double)next);
-		}
+	const uint32_t off = a.foff[i];
+	const bool fused = a.internalized && *(volatile uint32_t*)a.flags == 0;
+	if (!fused && a.owner[key] != (uint32_t)i)
 		return;
-	}
-	if (a.owner[key] != (uint32_t)i)
-		return;
-	for (uint64_t s = 0; s < a.S; s++)
+	T* __restrict__ D = static_cast<T*>(a.field) + off;
+	const T* __restrict__ rn = static_cast<const T*>(a.rnum) + i * a.S;
+	const T* __restrict__ rd = static_cast<const T*>(a.rden) + i * a.S;
+	const T* __restrict__ rf = static_cast<const T*>(a.rfac) + i * a.S;
+	double* __restrict__ I = a.internal + i * a.S;
+	for (uint32_t s0 = 0; s0 < a.S; s0 += kSubBatch)
 	{
-		const uint64_t k = i * a.S + s;
-		T* D = field + s * a.plane + key;
-		*D = (*D + rnum[k]) / rden[k] + rfac[k];
+		T dv[kSubBatch], n_[kSubBatch], d_[kSubBatch], f_[kSubBatch];
+		double iv[kSubBatch];
+#pragma unroll
+		for (int q = 0; q < kSubBatch; q++)
+			if (s0 + q < a.S)
+			{
+				dv[q] = D[s0 + q];
+				n_[q] = rn[s0 + q];
+				d_[q] = rd[s0 + q];
+				f_[q] = rf[s0 + q];
+				if (fused)
+					iv[q] = I[s0 + q];
+			}
+#pragma unroll
+		for (int q = 0; q < kSubBatch; q++)
+			if (s0 + q < a.S)
+			{
+				const T next = (dv[q] + n_[q]) / d_[q] + f_[q];
+				D[s0 + q] = next;
+				if (fused)
+					I[s0 + q] = iv[q] + a.Vv * ((double)dv[q] - (double)next);
+			}
 	}
 }
 
@@ -204,18 +219,31 @@ __global__ void cells_internalize_kernel(CellArgs a)
 		return;
 	if (*(volatile uint32_t*)a.flags == 0)
 		return;
-	const uint32_t key = a.foff[i];
-	if (key == kNoAgent)
+	if (a.vox[i] == kNoAgent)
 		return;
-	const T* num = static_cast<const T*>(a.num);
-	const T* den = static_cast<const T*>(a.den);
-	const T* fac = static_cast<const T*>(a.fac);
-	const T* field = static_cast<const T*>(a.field);
-	for (uint64_t s = 0; s < a.S; s++)
+	const T* __restrict__ D = static_cast<const T*>(a.field) + a.foff[i];
+	const T* __restrict__ nu = static_cast<const T*>(a.num) + i * a.S;
+	const T* __restrict__ de = static_cast<const T*>(a.den) + i * a.S;
+	const T* __restrict__ fa = static_cast<const T*>(a.fac) + i * a.S;
+	double* __restrict__ I = a.internal + i * a.S;
+	for (uint32_t s0 = 0; s0 < a.S; s0 += kSubBatch)
 	{
-		const uint64_t k = i * a.S + s;
-		const double D = (double)field[s * a.plane + key];
-		a.internal[k] -= a.Vv * ((double)num[k] - D * (double)den[k] + (double)fac[k]);
+		T dv[kSubBatch], n_[kSubBatch], d_[kSubBatch], f_[kSubBatch];
+		double iv[kSubBatch];
+#pragma unroll
+		for (int q = 0; q < kSubBatch; q++)
+			if (s0 + q < a.S)
+			{
+				dv[q] = D[s0 + q];
+				n_[q] = nu[s0 + q];
+				d_[q] = de[s0 + q];
+				f_[q] = fa[s0 + q];
+				iv[q] = I[s0 + q];
+			}
+#pragma unroll
+		for (int q = 0; q < kSubBatch; q++)
+			if (s0 + q < a.S)
+				I[s0 + q] = iv[q] - a.Vv * ((double)n_[q] - (double)dv[q] * (double)d_[q] + (double)f_[q]);
 	}
 }
 
@@ -226,22 +254,15 @@ __global__ void cells_release_kernel(CellArgs a, uint64_t agent)
 	const uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	if (s >= a.S)
 		return;
-	uint64_t idx[3] = { 0, 0, 0 };
-	for (int d = 0; d < a.dims; d++)
+	uint64_t idx[3];
+	if (!locate(a, agent, idx))
 	{
-		const double q = (a.pos[agent * a.dims + d] - a.bbmin[d]) / a.voxel[d];
-		if (!(q >= 0.0) || q >= (double)a.n[d])
-		{
-			atomicOr(a.err, DEV_ERR_AGENT_OUTSIDE);
-			return;
-		}
-		idx[d] = (uint64_t)q;
+		atomicOr(a.err, DEV_ERR_AGENT_OUTSIDE);
+		return;
 	}
-	const uint64_t off = (idx[2] * a.n[1] + idx[1]) * a.pitch + idx[0];
-	T* field = static_cast<T*>(a.field);
+	T* D = static_cast<T*>(a.field) + (idx[2] * a.n[1] + idx[1]) * a.pitch + idx[0] * a.S + s;
 	const uint64_t k = agent * a.S + s;
-	const double add = a.internal[k] * a.frac[k] / a.Vv;
-	field[s * a.plane + off] = (T)((double)field[s * a.plane + off] + add);
+	*D = (T)((double)*D + a.internal[k] * a.frac[k] / a.Vv);
 	a.internal[k] = 0.0;
 }
 
@@ -258,7 +279,6 @@ CellArgs make_args(Context* c)
 		a.voxel[d] = (double)c->voxel[d];
 	}
 	a.pitch = c->pitch;
-	a.plane = c->plane;
 	a.Vv = (double)(c->voxel[0] * c->voxel[1] * c->voxel[2]);
 	a.dt = c->dt;
 	a.pos = static_cast<const double*>(c->a_pos.ptr);
@@ -270,6 +290,7 @@ CellArgs make_args(Context* c)
 	a.frac = static_cast<const double*>(c->a_frac.ptr);
 	a.active = static_cast<const uint8_t*>(c->a_active.ptr);
 	a.internal = static_cast<double*>(c->a_internal.ptr);
+	a.vox = static_cast<uint32_t*>(c->a_vox.ptr);
 	a.foff = static_cast<uint32_t*>(c->a_foff.ptr);
 	a.num = c->a_num.ptr;
 	a.den = c->a_den.ptr;
@@ -300,8 +321,8 @@ static int run_cells(Context* c, bool recompute)
 	cudaEvent_t ev;
 	if (recompute)
 	{
-		PCG_CUDA_TRY(cudaMemsetAsync(c->counts.ptr, 0, c->plane * sizeof(uint32_t), c->stream));
-		launch_begin(c, K_CELLS_LOCATE, A * (8.0 * c->dims + 1 + 5 * S * 8 + 4 + 6 * S * w + 4), &ev);
+		PCG_CUDA_TRY(cudaMemsetAsync(c->counts.ptr, 0, c->V * sizeof(uint32_t), c->stream));
+		launch_begin(c, K_CELLS_LOCATE, A * (8.0 * c->dims + 1 + 5 * S * 8 + 8 + 6 * S * w + 4), &ev);
 		cells_locate_kernel<T><<<grid, block, 0, c->stream>>>(a);
 		launch_end(c, K_CELLS_LOCATE, ev);
 		PCG_CUDA_TRY(cudaGetLastError());
@@ -314,13 +335,15 @@ static int run_cells(Context* c, bool recompute)
 		launch_end(c, K_CELLS_REDUCE, ev);
 		PCG_CUDA_TRY(cudaGetLastError());
 	}
-	launch_begin(c, K_CELLS_APPLY, A * (4 + 4 + 3 * S * w + 2 * S * w + (c->compute_internalized ? 16 * S : 0)), &ev);
+	// per active agent: voxel index, offset, reduced terms, density read+write
+	launch_begin(c, K_CELLS_APPLY, A * (8 + 3 * S * w + 2 * S * w + (c->compute_internalized ? 16 * S : 0)), &ev);
 	cells_apply_kernel<T><<<grid, block, 0, c->stream>>>(a);
 	launch_end(c, K_CELLS_APPLY, ev);
 	PCG_CUDA_TRY(cudaGetLastError());
 	if (c->compute_internalized)
 	{
-		launch_begin(c, K_CELLS_INTERNALIZE, A * 4, &ev);
+		// after a conflict: own terms, density read, internalized read+write
+		launch_begin(c, K_CELLS_INTERNALIZE, A * (8 + 3 * S * w + S * w + 16 * S), &ev);
 		cells_internalize_kernel<T><<<grid, block, 0, c->stream>>>(a);
 		launch_end(c, K_CELLS_INTERNALIZE, ev);
 		PCG_CUDA_TRY(cudaGetLastError());

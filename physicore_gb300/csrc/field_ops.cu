@@ -3,7 +3,7 @@
 // Dirichlet (openmp_solver/src/dirichlet_solver.cpp:22-93): the reference writes
 // the x-min, x-max, y-min, y-max, z-min, z-max faces one after another (a later
 // face wins on shared edges) and then the interior voxels.  Here one launch covers
-// all six faces: a thread owns one (substrate, face voxel) and applies the face
+// all six faces: a thread owns one (face voxel, substrate) and applies the face
 // with the highest precedence whose condition holds, so edges resolve exactly as
 // the sequential order does; a second launch writes the interior list.
 //
@@ -21,9 +21,9 @@ struct FaceArgs
 	const void* values; // real [6*S]: face f = axis*2 + side
 	const uint8_t* conds;
 	uint32_t face_mask; // bit f set when face f exists
-	uint64_t S, nx, ny, nz, pitch, plane;
+	uint64_t S, nx, ny, nz, pitch;
 	uint64_t cnt_x, cnt_y, cnt_z; // voxels on each pair of faces
-	uint64_t total;               // per substrate
+	uint64_t total;               // face voxels (all pairs)
 };
 
 template <typename T>
@@ -34,8 +34,8 @@ __global__ void dirichlet_faces_kernel(FaceArgs a)
 	for (uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; idx < a.total * a.S;
 		 idx += (uint64_t)gridDim.x * blockDim.x)
 	{
-		const uint64_t s = idx / a.total;
-		uint64_t k = idx % a.total;
+		const uint64_t s = idx % a.S;
+		uint64_t k = idx / a.S;
 		uint64_t x, y, z;
 		if (k < a.cnt_x)
 		{ // x faces: k -> (side, y, z)
@@ -71,7 +71,7 @@ __global__ void dirichlet_faces_kernel(FaceArgs a)
 				continue;
 			if (a.conds[fi * a.S + s])
 			{
-				f[s * a.plane + (z * a.ny + y) * a.pitch + x] = vals[fi * a.S + s];
+				f[(z * a.ny + y) * a.pitch + x * a.S + s] = vals[fi * a.S + s];
 				break;
 			}
 		}
@@ -80,67 +80,70 @@ __global__ void dirichlet_faces_kernel(FaceArgs a)
 
 template <typename T>
 __global__ void dirichlet_interior_kernel(T* field, const uint64_t* offsets, const T* values, const uint8_t* conds,
-										  uint64_t K, uint64_t S, uint64_t plane)
+										  uint64_t K, uint64_t S)
 {
 	for (uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; idx < K * S;
 		 idx += (uint64_t)gridDim.x * blockDim.x)
 	{
-		const uint64_t k = idx / S, s = idx % S;
 		if (conds[idx])
-			field[s * plane + offsets[k]] = values[idx];
+			field[offsets[idx / S] + idx % S] = values[idx];
 	}
 }
 
-// One CTA row-block: blockDim.x threads walk x of `rows_per_block` rows.
+// A warp per row; each lane walks the row's (x,s) run with its substrate index
+// advanced incrementally.
 template <typename T, bool PER_VOXEL>
-__global__ void bulk_kernel(T* field, const T* supply, const T* uptake, const T* target, uint64_t nx,
-							uint64_t pitch, uint64_t rows_per_s, uint64_t S, T dt)
+__global__ void bulk_kernel(T* field, const T* supply, const T* uptake, const T* target, uint64_t row_len,
+							uint64_t pitch, uint64_t rows, uint32_t S, T dt)
 {
-	const uint64_t total_rows = rows_per_s * S;
-	for (uint64_t r = blockIdx.x * (uint64_t)blockDim.y + threadIdx.y; r < total_rows;
-		 r += (uint64_t)gridDim.x * blockDim.y)
+	const int lane = threadIdx.x & 31;
+	const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+	const uint32_t s_step = 32 % S;
+	for (uint64_t r = warp; r < rows; r += nwarps)
 	{
-		const uint64_t s = r / rows_per_s;
 		T* row = field + r * pitch;
-		T Sr = T(0), U = T(0), Tt = T(0);
-		if (!PER_VOXEL)
+		uint32_t s = (uint32_t)lane % S;
+		for (uint64_t k = lane; k < row_len; k += 32)
 		{
-			Sr = supply[s];
-			U = uptake[s];
-			Tt = target[s];
-		}
-		for (uint64_t x = threadIdx.x; x < nx; x += blockDim.x)
-		{
+			T Sr, U, Tt;
 			if (PER_VOXEL)
 			{
-				const uint64_t o = r * pitch + x;
+				const uint64_t o = r * pitch + k;
 				Sr = supply[o];
 				U = uptake[o];
 				Tt = target[o];
 			}
-			row[x] = (row[x] + dt * Sr * Tt) / (T(1) + dt * (U + Sr));
+			else
+			{
+				Sr = supply[s];
+				U = uptake[s];
+				Tt = target[s];
+			}
+			row[k] = (row[k] + dt * Sr * Tt) / (T(1) + dt * (U + Sr));
+			s += s_step;
+			if (s >= S)
+				s -= S;
 		}
 	}
 }
 
-// FP64 mass per substrate: each warp accumulates rows with compensated FP32/FP64
-// sums, then one double atomic per warp.
+// FP64 mass per substrate: a warp per row, one substrate at a time.
 template <typename T>
-__global__ void mass_kernel(const T* field, double* out, uint64_t nx, uint64_t pitch, uint64_t rows_per_s,
-							uint64_t S)
+__global__ void mass_kernel(const T* field, double* out, uint64_t nx, uint64_t pitch, uint64_t rows, uint32_t S)
 {
-	const uint64_t total_rows = rows_per_s * S;
 	const int lane = threadIdx.x & 31;
 	const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
 	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-	// a warp handles a contiguous run of rows of a single substrate at a time
-	for (uint64_t r = warp; r < total_rows; r += nwarps)
+	for (uint32_t s = 0; s < S; s++)
 	{
-		const uint64_t s = r / rows_per_s;
 		double acc = 0.0;
-		const T* row = field + r * pitch;
-		for (uint64_t x = lane; x < nx; x += 32)
-			acc += (double)row[x];
+		for (uint64_t r = warp; r < rows; r += nwarps)
+		{
+			const T* row = field + r * pitch + s;
+			for (uint64_t x = lane; x < nx; x += 32)
+				acc += (double)row[x * S];
+		}
 		for (int o = 16; o > 0; o >>= 1)
 			acc += __shfl_xor_sync(0xffffffffu, acc, o);
 		if (lane == 0)
@@ -149,23 +152,22 @@ __global__ void mass_kernel(const T* field, double* out, uint64_t nx, uint64_t p
 }
 
 template <typename T>
-__global__ void fill_kernel(T* field, const T* init, uint64_t nx, uint64_t pitch, uint64_t rows_per_s, uint64_t S)
+__global__ void fill_kernel(T* field, const T* init, uint64_t row_len, uint64_t pitch, uint64_t rows, uint32_t S)
 {
-	const uint64_t total = rows_per_s * S * pitch;
+	const uint64_t total = rows * pitch;
 	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
 		 i += (uint64_t)gridDim.x * blockDim.x)
 	{
-		const uint64_t x = i % pitch;
-		const uint64_t s = i / (pitch * rows_per_s);
-		field[i] = x < nx ? init[s] : T(0);
+		const uint64_t k = i % pitch;
+		field[i] = k < row_len ? init[k % S] : T(0);
 	}
 }
 
-// device field -> dense host-order buffer; OUT element type, planar or interleaved
+// device field -> dense host-order buffer of element type OUT; planar or interleaved
 template <typename T, typename OUT, bool INTERLEAVED>
-__global__ void pack_kernel(const T* field, OUT* dst, uint64_t nx, uint64_t pitch, uint64_t rows_per_s, uint64_t S)
+__global__ void pack_kernel(const T* field, OUT* dst, uint64_t nx, uint64_t pitch, uint64_t rows, uint64_t S)
 {
-	const uint64_t V = nx * rows_per_s;
+	const uint64_t V = nx * rows;
 	const uint64_t total = V * S;
 	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
 		 i += (uint64_t)gridDim.x * blockDim.x)
@@ -181,15 +183,14 @@ __global__ void pack_kernel(const T* field, OUT* dst, uint64_t nx, uint64_t pitc
 			s = i / V;
 			v = i % V;
 		}
-		const uint64_t x = v % nx, r = v / nx;
-		dst[i] = (OUT)field[s * rows_per_s * pitch + r * pitch + x];
+		dst[i] = (OUT)field[(v / nx) * pitch + (v % nx) * S + s];
 	}
 }
 
 template <typename T, typename IN, bool INTERLEAVED>
-__global__ void unpack_kernel(T* field, const IN* src, uint64_t nx, uint64_t pitch, uint64_t rows_per_s, uint64_t S)
+__global__ void unpack_kernel(T* field, const IN* src, uint64_t nx, uint64_t pitch, uint64_t rows, uint64_t S)
 {
-	const uint64_t V = nx * rows_per_s;
+	const uint64_t V = nx * rows;
 	const uint64_t total = V * S;
 	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
 		 i += (uint64_t)gridDim.x * blockDim.x)
@@ -205,15 +206,14 @@ __global__ void unpack_kernel(T* field, const IN* src, uint64_t nx, uint64_t pit
 			s = i / V;
 			v = i % V;
 		}
-		const uint64_t x = v % nx, r = v / nx;
-		field[s * rows_per_s * pitch + r * pitch + x] = (T)src[i];
+		field[(v / nx) * pitch + (v % nx) * S + s] = (T)src[i];
 	}
 }
 
-unsigned grid_for(uint64_t work, unsigned block)
+unsigned grid_for(const Context* c, uint64_t work, unsigned block)
 {
 	uint64_t g = (work + block - 1) / block;
-	const uint64_t cap = 152ull * 16;
+	const uint64_t cap = (uint64_t)(c->sm_count > 0 ? c->sm_count : 152) * 16;
 	if (g > cap)
 		g = cap;
 	return (unsigned)(g ? g : 1);
@@ -225,7 +225,6 @@ template <typename T>
 static int run_dirichlet(Context* c)
 {
 	const uint64_t nx = c->n[0], ny = c->n[1], nz = c->n[2];
-	FaceArgs a {};
 	uint32_t mask = 0;
 	for (int axis = 0; axis < c->dims; axis++)
 		for (int side = 0; side < 2; side++)
@@ -233,6 +232,7 @@ static int run_dirichlet(Context* c)
 				mask |= 1u << (axis * 2 + side);
 	if (mask)
 	{
+		FaceArgs a {};
 		a.field = c->field.ptr;
 		a.values = c->face_values.ptr;
 		a.conds = static_cast<const uint8_t*>(c->face_conds.ptr);
@@ -240,14 +240,13 @@ static int run_dirichlet(Context* c)
 		a.S = c->S;
 		a.nx = nx, a.ny = ny, a.nz = nz;
 		a.pitch = c->pitch;
-		a.plane = c->plane;
 		a.cnt_x = (mask & 0x3) ? 2 * ny * nz : 0;
 		a.cnt_y = (mask & 0xc) ? 2 * nx * nz : 0;
 		a.cnt_z = (mask & 0x30) ? 2 * nx * ny : 0;
 		a.total = a.cnt_x + a.cnt_y + a.cnt_z;
 		cudaEvent_t ev;
 		launch_begin(c, K_DIRICHLET_FACES, (double)(a.total * c->S * sizeof(T)), &ev);
-		dirichlet_faces_kernel<T><<<grid_for(a.total * c->S, 256), 256, 0, c->stream>>>(a);
+		dirichlet_faces_kernel<T><<<grid_for(c, a.total * c->S, 256), 256, 0, c->stream>>>(a);
 		launch_end(c, K_DIRICHLET_FACES, ev);
 		PCG_CUDA_TRY(cudaGetLastError());
 	}
@@ -255,10 +254,9 @@ static int run_dirichlet(Context* c)
 	{
 		cudaEvent_t ev;
 		launch_begin(c, K_DIRICHLET_INTERIOR, (double)(c->K * (8 + c->S * (2 * sizeof(T) + 1))), &ev);
-		dirichlet_interior_kernel<T><<<grid_for(c->K * c->S, 256), 256, 0, c->stream>>>(
+		dirichlet_interior_kernel<T><<<grid_for(c, c->K * c->S, 256), 256, 0, c->stream>>>(
 			static_cast<T*>(c->field.ptr), static_cast<const uint64_t*>(c->dir_offsets.ptr),
-			static_cast<const T*>(c->dir_values.ptr), static_cast<const uint8_t*>(c->dir_conds.ptr), c->K, c->S,
-			c->plane);
+			static_cast<const T*>(c->dir_values.ptr), static_cast<const uint8_t*>(c->dir_conds.ptr), c->K, c->S);
 		launch_end(c, K_DIRICHLET_INTERIOR, ev);
 		PCG_CUDA_TRY(cudaGetLastError());
 	}
@@ -272,10 +270,8 @@ static int run_bulk(Context* c)
 {
 	if (c->bulk_mode == PCG_BULK_NONE)
 		return PCG_OK;
-	const uint64_t rows = c->n[1] * c->n[2];
-	dim3 block(64, 4);
-	const unsigned grid = grid_for(rows * c->S, 4);
 	const bool pv = c->bulk_mode == PCG_BULK_PER_VOXEL;
+	const unsigned grid = grid_for(c, c->rows * 32, 256);
 	cudaEvent_t ev;
 	const double bytes = (double)(c->V * c->S * sizeof(T)) * (pv ? 5.0 : 2.0);
 	launch_begin(c, K_BULK, bytes, &ev);
@@ -283,11 +279,11 @@ static int run_bulk(Context* c)
 	const T* up = static_cast<const T*>(c->bulk[1].ptr);
 	const T* tp = static_cast<const T*>(c->bulk[2].ptr);
 	if (pv)
-		bulk_kernel<T, true><<<grid, block, 0, c->stream>>>(static_cast<T*>(c->field.ptr), sp, up, tp, c->n[0],
-															c->pitch, rows, c->S, (T)c->dt);
+		bulk_kernel<T, true><<<grid, 256, 0, c->stream>>>(static_cast<T*>(c->field.ptr), sp, up, tp, c->row_len,
+														  c->pitch, c->rows, (uint32_t)c->S, (T)c->dt);
 	else
-		bulk_kernel<T, false><<<grid, block, 0, c->stream>>>(static_cast<T*>(c->field.ptr), sp, up, tp, c->n[0],
-															 c->pitch, rows, c->S, (T)c->dt);
+		bulk_kernel<T, false><<<grid, 256, 0, c->stream>>>(static_cast<T*>(c->field.ptr), sp, up, tp, c->row_len,
+														   c->pitch, c->rows, (uint32_t)c->S, (T)c->dt);
 	launch_end(c, K_BULK, ev);
 	PCG_CUDA_TRY(cudaGetLastError());
 	return PCG_OK;
@@ -299,11 +295,11 @@ template <typename T>
 static int run_mass(Context* c, double* out)
 {
 	PCG_CUDA_TRY(cudaMemsetAsync(out, 0, c->S * sizeof(double), c->stream));
-	const uint64_t rows = c->n[1] * c->n[2];
 	cudaEvent_t ev;
 	launch_begin(c, K_MASS, (double)(c->V * c->S * sizeof(T)), &ev);
-	mass_kernel<T><<<grid_for(rows * c->S * 32, 256), 256, 0, c->stream>>>(static_cast<const T*>(c->field.ptr), out,
-																			c->n[0], c->pitch, rows, c->S);
+	mass_kernel<T><<<grid_for(c, c->rows * 32, 256), 256, 0, c->stream>>>(static_cast<const T*>(c->field.ptr), out,
+																		   c->n[0], c->pitch, c->rows,
+																		   (uint32_t)c->S);
 	launch_end(c, K_MASS, ev);
 	PCG_CUDA_TRY(cudaGetLastError());
 	return PCG_OK;
@@ -314,16 +310,16 @@ int launch_mass(Context* c, double* out) { return c->wsize == 4 ? run_mass<float
 template <typename T>
 static int run_fill(Context* c)
 {
-	// initial conditions as T on the device, staged through the mass buffer (S doubles >= S T's)
+	// initial conditions as T, staged through the mass buffer (S doubles >= S T's)
 	std::vector<T> h(c->S);
 	for (uint64_t s = 0; s < c->S; s++)
 		h[s] = (T)c->init[s];
 	PCG_CUDA_TRY(cudaMemcpyAsync(c->mass.ptr, h.data(), c->S * sizeof(T), cudaMemcpyHostToDevice, c->stream));
-	const uint64_t rows = c->n[1] * c->n[2];
 	cudaEvent_t ev;
-	launch_begin(c, K_LAYOUT, (double)(c->plane * c->S * sizeof(T)), &ev);
-	fill_kernel<T><<<grid_for(rows * c->S * c->pitch, 256), 256, 0, c->stream>>>(
-		static_cast<T*>(c->field.ptr), static_cast<const T*>(c->mass.ptr), c->n[0], c->pitch, rows, c->S);
+	launch_begin(c, K_LAYOUT, (double)(c->rows * c->pitch * sizeof(T)), &ev);
+	fill_kernel<T><<<grid_for(c, c->rows * c->pitch, 256), 256, 0, c->stream>>>(
+		static_cast<T*>(c->field.ptr), static_cast<const T*>(c->mass.ptr), c->row_len, c->pitch, c->rows,
+		(uint32_t)c->S);
 	launch_end(c, K_LAYOUT, ev);
 	PCG_CUDA_TRY(cudaGetLastError());
 	return PCG_OK;
@@ -334,16 +330,15 @@ int launch_fill_initial(Context* c) { return c->wsize == 4 ? run_fill<float>(c) 
 template <typename T, typename H>
 static int run_pack(Context* c, void* dst, int layout)
 {
-	const uint64_t rows = c->n[1] * c->n[2];
 	const uint64_t total = c->V * c->S;
 	cudaEvent_t ev;
 	launch_begin(c, K_LAYOUT, (double)(total * (sizeof(T) + sizeof(H))), &ev);
 	if (layout == PCG_LAYOUT_INTERLEAVED)
-		pack_kernel<T, H, true><<<grid_for(total, 256), 256, 0, c->stream>>>(
-			static_cast<const T*>(c->field.ptr), static_cast<H*>(dst), c->n[0], c->pitch, rows, c->S);
+		pack_kernel<T, H, true><<<grid_for(c, total, 256), 256, 0, c->stream>>>(
+			static_cast<const T*>(c->field.ptr), static_cast<H*>(dst), c->n[0], c->pitch, c->rows, c->S);
 	else
-		pack_kernel<T, H, false><<<grid_for(total, 256), 256, 0, c->stream>>>(
-			static_cast<const T*>(c->field.ptr), static_cast<H*>(dst), c->n[0], c->pitch, rows, c->S);
+		pack_kernel<T, H, false><<<grid_for(c, total, 256), 256, 0, c->stream>>>(
+			static_cast<const T*>(c->field.ptr), static_cast<H*>(dst), c->n[0], c->pitch, c->rows, c->S);
 	launch_end(c, K_LAYOUT, ev);
 	PCG_CUDA_TRY(cudaGetLastError());
 	return PCG_OK;
@@ -352,16 +347,15 @@ static int run_pack(Context* c, void* dst, int layout)
 template <typename T, typename H>
 static int run_unpack(Context* c, const void* src, int layout)
 {
-	const uint64_t rows = c->n[1] * c->n[2];
 	const uint64_t total = c->V * c->S;
 	cudaEvent_t ev;
 	launch_begin(c, K_LAYOUT, (double)(total * (sizeof(T) + sizeof(H))), &ev);
 	if (layout == PCG_LAYOUT_INTERLEAVED)
-		unpack_kernel<T, H, true><<<grid_for(total, 256), 256, 0, c->stream>>>(
-			static_cast<T*>(c->field.ptr), static_cast<const H*>(src), c->n[0], c->pitch, rows, c->S);
+		unpack_kernel<T, H, true><<<grid_for(c, total, 256), 256, 0, c->stream>>>(
+			static_cast<T*>(c->field.ptr), static_cast<const H*>(src), c->n[0], c->pitch, c->rows, c->S);
 	else
-		unpack_kernel<T, H, false><<<grid_for(total, 256), 256, 0, c->stream>>>(
-			static_cast<T*>(c->field.ptr), static_cast<const H*>(src), c->n[0], c->pitch, rows, c->S);
+		unpack_kernel<T, H, false><<<grid_for(c, total, 256), 256, 0, c->stream>>>(
+			static_cast<T*>(c->field.ptr), static_cast<const H*>(src), c->n[0], c->pitch, c->rows, c->S);
 	launch_end(c, K_LAYOUT, ev);
 	PCG_CUDA_TRY(cudaGetLastError());
 	return PCG_OK;

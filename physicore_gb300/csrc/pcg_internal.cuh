@@ -1,12 +1,15 @@
 // pcg_internal.cuh -- shared definitions of the GB300 BioFVM backend.
 //
-// Device data layout (chosen for the sweeps, not copied from the reference):
-//   field[s][z][y][x], each x-row padded to `pitch` elements so that every row
-//   starts on a 32-byte sector boundary.  Element (s,x,y,z) lives at
-//   ((s*nz + z)*ny + y)*pitch + x.  The reference keeps substrates interleaved
-//   (s fastest, diffusion_solver.h:64-83); host transfers convert between the two.
+// Device field layout: the reference's interleaved order (s fastest, then x, y, z;
+// openmp_solver/src/diffusion_solver.h:64-83) with every x-row padded to `pitch`
+// elements, pitch*sizeof(T) a multiple of 32 bytes so rows start on DRAM sectors.
+// Element (s,x,y,z) lives at (z*ny + y)*pitch + x*S + s.  Keeping a voxel's
+// substrates adjacent makes every agent touch one sector per voxel (S*4 <= 32 B for
+// S <= 8 in FP32); the y/z sweeps tile the merged (x,s) run of a row, and the x
+// sweep walks whole rows with S independent recurrences per thread.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -64,44 +67,42 @@ const char* kernel_name(int id);
 
 // ------------------------------------------------------------------ launch geometry
 
-constexpr int kSweepLanes = 32;        // lines per y/z tile (one warp)
-constexpr int kSweepXRows = 32;        // rows per x tile (one warp)
+constexpr int kLanes = 32;           // lines per y/z tile, rows per x tile (one warp per CTA)
+constexpr int kStages = 2;           // shared-memory ring depth of the persistent sweeps
 constexpr uint64_t kMaxSmemBytes = 227 * 1024;
+constexpr uint64_t kCoefSmemLimit = 64 * 1024; // larger coefficient tables stay in global memory
 
-// ------------------------------------------------------------------ argument blocks
+__host__ __device__ constexpr uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
+__host__ __device__ constexpr int gcd_i(int a, int b) { return b == 0 ? a : gcd_i(b, a % b); }
+// Elements per x-sweep vector group: the smallest multiple of both S and a 16-byte chunk.
+__host__ __device__ constexpr int group_elems(int S, int vn) { return S <= 8 ? S / gcd_i(S, vn) * vn : vn; }
 
-// One Thomas sweep along y or z over a set of tiles.  A tile is `lanes`
-// consecutive x positions of every line of one (s, outer) pair.
-struct SweepYZArgs
-{
-	void* field;
-	const void* coef;     // per substrate: B[n], E[n] (E[0] = 0, E[i] = e_{i-1}), padded to coef_pitch
-	const void* coef_c;   // c[s]
-	uint64_t coef_pitch;  // elements between the B tables of consecutive substrates (E follows B)
-	uint64_t n;           // line length
-	uint64_t nx;
-	uint64_t line_stride; // elements between consecutive points of a line
-	uint64_t outer_count; // z (y sweep) or y (z sweep)
-	uint64_t outer_stride;
-	uint64_t plane;       // elements per substrate
-	uint64_t xblocks;
-	uint64_t tiles;
-	uint32_t* err;
-};
+// ------------------------------------------------------------------ argument block
 
-// One Thomas sweep along x.  A tile is up to `rows` consecutive rows of one substrate.
-struct SweepXArgs
+// A Thomas sweep over one axis.  The coefficient table of the axis is
+// [B | E | C]: B[i*S+s] = b'_i, E[i*S+s] = e_{i-1} (E = 0 for i = 0), each
+// padded to coef_len elements, then C[s] = c padded to a 16-byte multiple.
+struct SweepArgs
 {
 	void* field;
 	const void* coef;
-	const void* coef_c;
-	uint64_t coef_pitch;
-	uint64_t n;           // nx
+	uint64_t coef_len;    // elements of one padded B or E table
+	uint64_t coef_elems;  // elements of the whole [B | E | C] table
+	uint32_t S;
+	uint32_t n;           // line length
+	uint64_t row_len;     // nx*S: elements of one row
 	uint64_t pitch;       // row pitch of the field (elements)
-	uint64_t rows;        // rows per substrate (ny*nz)
-	uint64_t rblocks;     // tiles per substrate
 	uint64_t tiles;
-	uint64_t smem_pitch;  // shared-memory row pitch (elements)
+	// y/z sweeps: a tile is 32 consecutive (x,s) elements of all n points of a line set
+	uint64_t line_stride; // elements between consecutive points of a line
+	uint64_t outer_stride;
+	uint64_t xblocks;
+	uint32_t box_rows;    // line points per TMA box (<= 256)
+	uint32_t boxes;       // boxes per tile (boxes * box_rows >= n)
+	// x sweep: a tile is rows_per_tile whole rows
+	uint64_t rows;        // ny*nz
+	uint64_t smem_pitch;  // shared-memory row pitch (elements); in 16-byte chunks == threads per row (mod 8)
+	uint32_t rows_per_tile;
 	uint32_t* err;
 };
 
@@ -130,6 +131,7 @@ struct Context
 	int device = 0;
 	int precision = PCG_FP32;
 	size_t wsize = 4; // bytes per field element
+	int sm_count = 0;
 	cudaStream_t own_stream = nullptr;
 	cudaStream_t stream = nullptr;
 
@@ -146,8 +148,9 @@ struct Context
 	std::vector<double> D, decay, init;
 
 	// derived layout
-	uint64_t pitch = 0; // row pitch (elements)
-	uint64_t plane = 0; // elements per substrate = nz*ny*pitch
+	uint64_t row_len = 0; // nx*S
+	uint64_t pitch = 0;   // row pitch (elements)
+	uint64_t rows = 0;    // ny*nz
 	uint64_t V = 0;
 
 	// device state
@@ -155,8 +158,13 @@ struct Context
 	bool recompute_cells = true;
 	DeviceBuffer field;
 	DeviceBuffer coef[3];
-	DeviceBuffer coef_c[3];
-	uint64_t coef_pitch[3] = { 0, 0, 0 };
+	// TMA tensor maps of the field for the y and z sweeps: the field as a 3-D tensor
+	// (x*S+s, y, z) with 32 x (box_rows) boxes along the swept axis
+	CUtensorMap tmap[3];
+	uint32_t tmap_box_rows[3] = { 0, 0, 0 };
+	uint32_t tmap_boxes[3] = { 0, 0, 0 };
+	uint64_t coef_len[3] = { 0, 0, 0 };
+	uint64_t coef_elems[3] = { 0, 0, 0 };
 	DeviceBuffer err;      // uint32 device error word
 	DeviceBuffer flags;    // uint32 [4]: [0] ballot conflict
 	DeviceBuffer mass;     // double [S]
@@ -167,7 +175,7 @@ struct Context
 	std::vector<uint64_t> h_dir_voxels;
 	std::vector<double> h_dir_values;
 	std::vector<uint8_t> h_dir_conds;
-	DeviceBuffer dir_offsets; // uint64 [K] element offset inside a substrate plane
+	DeviceBuffer dir_offsets; // uint64 [K] field offset of the node's first substrate
 	DeviceBuffer dir_values;  // real [K*S]
 	DeviceBuffer dir_conds;   // uint8 [K*S]
 	bool face_on[3][2] = { { false, false }, { false, false }, { false, false } };
@@ -175,24 +183,23 @@ struct Context
 	std::vector<uint8_t> h_face_conds[3][2];
 	DeviceBuffer face_values; // real [6*S]
 	DeviceBuffer face_conds;  // uint8 [6*S]
-	bool dirichlet_dirty = true;
 
 	// bulk
 	int bulk_mode = PCG_BULK_NONE;
 	std::vector<double> h_bulk[3];
-	DeviceBuffer bulk[3]; // real tables: supply, uptake, target (S or S*plane)
-	bool bulk_dirty = true;
+	DeviceBuffer bulk[3]; // real tables: supply, uptake, target ([S] or field-shaped)
 
 	// agents
 	uint64_t A = 0;
 	bool compute_internalized = false;
 	DeviceBuffer a_pos, a_sec, a_sat, a_upt, a_net, a_vol, a_active, a_internal, a_frac;
 	// cell scratch
-	DeviceBuffer a_foff;                  // uint32 [A]: offset of the agent's voxel inside a plane
+	DeviceBuffer a_vox;                   // uint32 [A]: linear voxel index (x + nx*(y + ny*z)), or ~0
+	DeviceBuffer a_foff;                  // uint32 [A]: field offset of the voxel's first substrate
 	DeviceBuffer a_num, a_den, a_fac;     // real [A*S]
 	DeviceBuffer a_rnum, a_rden, a_rfac;  // real [A*S]
-	DeviceBuffer owner;                   // uint32 [plane]: winning agent per voxel
-	DeviceBuffer counts;                  // uint32 [plane]: active agents per voxel
+	DeviceBuffer owner;                   // uint32 [V]: winning agent per voxel
+	DeviceBuffer counts;                  // uint32 [V]: active agents per voxel
 
 	// measurement
 	bool timing = false;
@@ -226,9 +233,13 @@ int launch_to_host_layout(Context* c, void* dst, int layout, int dtype);
 int launch_from_host_layout(Context* c, const void* src, int layout, int dtype);
 int launch_fill_initial(Context* c);
 
-uint64_t sweep_yz_smem_bytes(const Context* c, int axis);
-uint64_t sweep_x_smem_bytes(const Context* c);
-uint64_t sweep_x_smem_pitch(const Context* c);
+// geometry helpers shared by the launchers and the feasibility checks
+uint64_t coef_table_len(uint64_t n, uint64_t S, size_t wsize);
+uint64_t coef_row_pitch(uint64_t n);
+uint64_t sweep_x_smem_pitch(uint64_t row_len, uint64_t S, size_t wsize);
+uint64_t x_threads_per_row(uint64_t S, size_t wsize);
+uint64_t sweep_smem_bytes(const Context* c, int axis);
+int prepare_sweep_maps(Context* c);
 
 } // namespace pcg
 
@@ -269,7 +280,7 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
 				 : "memory");
 }
 
-// Returns true when the phase with parity `phase` completed within the limit.
+// Returns true when the phase with parity `phase` completed within the time limit.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase)
 {
 	const uint32_t addr = smem_addr(bar);
@@ -309,8 +320,32 @@ __device__ __forceinline__ void bulk_s2g(void* dst, const void* src, uint32_t by
 				 : "memory");
 }
 
+// TMA tile load of a 3-D box at coordinates (c0, c1, c2) into shared memory,
+// completing on `bar`; c0 * sizeof(element) must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
+											uint64_t* bar)
+{
+	asm volatile(
+		"cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+		"[%5];" ::"r"(smem_addr(dst)),
+		"l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar))
+		: "memory");
+}
+
+// TMA tile store of a 3-D box (elements outside the tensor are not written).
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, int c0, int c1, int c2, const void* src)
+{
+	asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(map),
+				 "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(src))
+				 : "memory");
+}
+
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 
+// Waits until this thread's bulk groups have finished reading shared memory.
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// Waits until this thread's bulk groups have completed.
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // Makes generic-proxy shared-memory writes visible to the async (bulk copy) proxy.
@@ -318,6 +353,9 @@ __device__ __forceinline__ void fence_proxy_async_smem()
 {
 	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
+
+__device__ __forceinline__ float fmadd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmadd(double a, double b, double c) { return __fma_rn(a, b, c); }
 
 } // namespace pcg::dev
 #endif

@@ -1,30 +1,43 @@
 // sweeps.cu -- ADI/LOD Thomas sweeps along x, y and z on sm_103a.
 //
 // Arithmetic per line follows the reference (openmp_solver/src/diffusion_solver.cpp:
-// 116-202 for x, 390-794 for y/z; the coefficients of diffusion_solver.cpp:29-86):
+// 116-202 for x, 390-794 for y/z; coefficients of diffusion_solver.cpp:29-86):
 //   forward   d_i  = d_i + e_{i-1} d_{i-1}            i = 1..n-1
 //             d_{n-1} = d_{n-1} b'_{n-1}
 //   backward  d_i  = (d_i + c d_{i+1}) b'_i            i = n-2..0
+// with each line using the coefficients of its own substrate.  Both passes start
+// from a zero carry: e_{-1} = 0 makes the first forward step d_0 = d_0, and c*0 = 0
+// makes the first backward step d_{n-1} b'_{n-1}, so every step has one form.
 //
 // GB300 mapping (our own design):
-//  * y/z sweeps: a tile is 32 consecutive x positions of all n points of the
-//    lines of one (substrate, outer) pair.  Its n rows of 128 B (FP32) are pulled
-//    into shared memory by TMA bulk copies (cp.async.bulk) completing on an
-//    mbarrier; lane t then solves line t out of shared memory (column t of an
-//    [n][32] tile: bank-conflict free), and the tile goes back by bulk copies.
-//  * x sweep: lines run along the contiguous axis, so a tile is 32 whole rows;
-//    each row is one bulk copy into a shared-memory row whose pitch is 16 B
-//    modulo 128 B, and lane r walks row r with 16-byte vector accesses (8 lanes
-//    of a quarter-warp hit 8 distinct 16-byte bank groups).
-//  * The per-substrate coefficient tables (b', e padded to 16 B) travel with the
-//    tile in the same bulk transaction; every lane reads them as broadcasts.
-//  * Every wait is bounded; a timeout sets a device error bit and the CTA exits
-//    after its own copies have drained.
+//  * A line must stay on chip between its forward and backward pass, so shared
+//    memory bounds how many lines an SM can hold (~160 lines of 320 FP32 points).
+//    Every byte of it therefore holds line data: tiles are single-stage, the
+//    coefficient tables are read through L1 (__ldg, 16-byte vectors), and tile
+//    sizes are chosen so that several CTAs share an SM and all four schedulers
+//    have warps to issue.
+//  * Persistent CTAs (one warp) walk their tiles: a TMA bulk-copy load completes on
+//    an mbarrier, the warp solves the tile in place, and a TMA bulk store writes it
+//    back; the next load is issued as soon as the store has read shared memory.
+//  * Solvers run in blocks of P steps without per-step predicates; the next block's
+//    points and coefficients are requested before the current block's dependent
+//    chain, so load latency overlaps the chain.
+//  * y/z: a tile is 32 consecutive (x,s) elements of a row at every point of the
+//    lines; lane t solves column t of the [n][32] tile (bank-conflict free) with
+//    the coefficient row of its substrate ([s][j] table).
+//  * x: a tile is R whole rows; a row is walked as a stream of 16-byte chunks,
+//    element k belonging to substrate k % S, with one carry per substrate.  When a
+//    voxel's substrates fill whole chunks, TPR threads share a row, one chunk slot
+//    each; rows are TPR (mod 8) chunks apart so quarter-warps hit distinct banks.
+//  * Every wait is bounded; a timeout sets a device error bit instead of trapping.
 #include "pcg_internal.cuh"
 
 namespace pcg {
 
 namespace {
+
+constexpr int kBlock = 8;      // recurrence steps per pipelined block (y/z, one point per step)
+constexpr int kChunkBlock = 4; // 16-byte chunks per pipelined block (x, several points per chunk)
 
 template <typename T>
 struct Vec16;
@@ -41,316 +54,776 @@ struct Vec16<double>
 	static constexpr int N = 2;
 };
 
+template <typename V, typename T>
+__device__ __forceinline__ T vget(const V& v, int u)
+{
+	return reinterpret_cast<const T*>(&v)[u];
+}
+template <typename V, typename T>
+__device__ __forceinline__ void vset(V& v, int u, T x)
+{
+	reinterpret_cast<T*>(&v)[u] = x;
+}
+
+template <typename V>
+__device__ __forceinline__ V ldg_vec(const V* p)
+{
+	return __ldg(p);
+}
+
+// ------------------------------------------------------------------ y / z
+
+// One line at col[j*kLanes], j < n; eE/eB are the line's substrate rows of the
+// [s][j] coefficient table (16-byte aligned, padded to a multiple of kBlock).
 template <typename T>
-__device__ __forceinline__ T vget(const typename Vec16<T>::type& v, int u);
-template <>
-__device__ __forceinline__ float vget<float>(const float4& v, int u)
+__device__ __forceinline__ void solve_column(T* __restrict__ col, uint32_t n, const T* __restrict__ eB,
+											 const T* __restrict__ eE, T c)
 {
-	return u == 0 ? v.x : u == 1 ? v.y : u == 2 ? v.z : v.w;
-}
-template <>
-__device__ __forceinline__ double vget<double>(const double2& v, int u)
-{
-	return u == 0 ? v.x : v.y;
-}
-template <typename T>
-__device__ __forceinline__ void vset(typename Vec16<T>::type& v, int u, T x);
-template <>
-__device__ __forceinline__ void vset<float>(float4& v, int u, float x)
-{
-	if (u == 0)
-		v.x = x;
-	else if (u == 1)
-		v.y = x;
-	else if (u == 2)
-		v.z = x;
-	else
-		v.w = x;
-}
-template <>
-__device__ __forceinline__ void vset<double>(double2& v, int u, double x)
-{
-	if (u == 0)
-		v.x = x;
-	else
-		v.y = x;
+	using V = typename Vec16<T>::type;
+	constexpr int P = kBlock, VN = Vec16<T>::N, NV = P / VN;
+	const uint32_t nb = n / P;
+	T d = T(0);
+	// ---- forward
+	{
+		T x[P], xn[P];
+		V e[NV], en[NV];
+		if (nb)
+		{
+#pragma unroll
+			for (int q = 0; q < P; q++)
+				x[q] = col[q * kLanes];
+#pragma unroll
+			for (int v = 0; v < NV; v++)
+				e[v] = ldg_vec(reinterpret_cast<const V*>(eE) + v);
+		}
+		for (uint32_t b = 0; b < nb; b++)
+		{
+			T* blk = col + (uint64_t)b * P * kLanes;
+			if (b + 1 < nb)
+			{
+#pragma unroll
+				for (int q = 0; q < P; q++)
+					xn[q] = blk[(P + q) * kLanes];
+#pragma unroll
+				for (int v = 0; v < NV; v++)
+					en[v] = ldg_vec(reinterpret_cast<const V*>(eE + (b + 1) * P) + v);
+			}
+#pragma unroll
+			for (int q = 0; q < P; q++)
+			{
+				d = dev::fmadd(vget<V, T>(e[q / VN], q % VN), d, x[q]);
+				blk[q * kLanes] = d;
+			}
+#pragma unroll
+			for (int q = 0; q < P; q++)
+				x[q] = xn[q];
+#pragma unroll
+			for (int v = 0; v < NV; v++)
+				e[v] = en[v];
+		}
+		for (uint32_t j = nb * P; j < n; j++)
+		{
+			d = dev::fmadd(__ldg(eE + j), d, col[(uint64_t)j * kLanes]);
+			col[(uint64_t)j * kLanes] = d;
+		}
+	}
+	// ---- backward (top partial block first, then aligned full blocks downwards)
+	d = T(0);
+	for (int j = (int)n - 1; j >= (int)(nb * P); j--)
+	{
+		d = dev::fmadd(c, d, col[(uint64_t)j * kLanes]) * __ldg(eB + j);
+		col[(uint64_t)j * kLanes] = d;
+	}
+	{
+		T x[P], xn[P];
+		V bb[NV], bn[NV];
+		if (nb)
+		{
+			const T* blk = col + (uint64_t)(nb - 1) * P * kLanes;
+#pragma unroll
+			for (int q = 0; q < P; q++)
+				x[q] = blk[q * kLanes];
+#pragma unroll
+			for (int v = 0; v < NV; v++)
+				bb[v] = ldg_vec(reinterpret_cast<const V*>(eB + (nb - 1) * P) + v);
+		}
+		for (int b = (int)nb - 1; b >= 0; b--)
+		{
+			T* blk = col + (uint64_t)b * P * kLanes;
+			if (b > 0)
+			{
+#pragma unroll
+				for (int q = 0; q < P; q++)
+					xn[q] = blk[(q - P) * kLanes];
+#pragma unroll
+				for (int v = 0; v < NV; v++)
+					bn[v] = ldg_vec(reinterpret_cast<const V*>(eB + (b - 1) * P) + v);
+			}
+#pragma unroll
+			for (int q = P - 1; q >= 0; q--)
+			{
+				d = dev::fmadd(c, d, x[q]) * vget<V, T>(bb[q / VN], q % VN);
+				blk[q * kLanes] = d;
+			}
+#pragma unroll
+			for (int q = 0; q < P; q++)
+				x[q] = xn[q];
+#pragma unroll
+			for (int v = 0; v < NV; v++)
+				bb[v] = bn[v];
+		}
+	}
 }
 
-__host__ __device__ inline uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
-
-__device__ __forceinline__ float fmadd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-__device__ __forceinline__ double fmadd(double a, double b, double c) { return __fma_rn(a, b, c); }
-
-// -------------------------------------------------------------------- y / z
-
-template <typename T>
-__global__ void __launch_bounds__(kSweepLanes) sweep_yz_kernel(SweepYZArgs a)
+// One TMA tensor box per box_rows points moves a whole [n][32] tile: the field is
+// described to the TMA unit as a 3-D tensor (x*S+s, y, z), and a tile is the box
+// (32, box_rows, 1) at (x0, j0, z) for the y sweep or (32, 1, box_rows) at
+// (x0, y, j0) for the z sweep.  Elements beyond the row (x*S+s >= nx*S) or the line
+// are zero-filled on load and not written on store.
+template <typename T, int AXIS>
+__global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __grid_constant__ CUtensorMap tmap)
 {
 	extern __shared__ __align__(128) unsigned char smem[];
 	uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
-	const uint64_t npad = a.coef_pitch / 2;
-	T* sB = reinterpret_cast<T*>(smem + 16);
-	T* sE = sB + npad;
-	T* tile = sB + a.coef_pitch;
-
-	const uint64_t t = blockIdx.x;
-	if (t >= a.tiles)
-		return;
-	const uint64_t xb = t % a.xblocks;
-	const uint64_t rest = t / a.xblocks;
-	const uint64_t o = rest % a.outer_count;
-	const uint64_t s = rest / a.outer_count;
-	const uint64_t x0 = xb * kSweepLanes;
-	const uint64_t valid = a.nx - x0 < (uint64_t)kSweepLanes ? a.nx - x0 : (uint64_t)kSweepLanes;
-	const uint32_t row_bytes = (uint32_t)round_up(valid * sizeof(T), 16);
-	const uint32_t coef_bytes = (uint32_t)(a.coef_pitch * sizeof(T));
-	const uint32_t n = (uint32_t)a.n;
-
-	T* gbase = static_cast<T*>(a.field) + s * a.plane + o * a.outer_stride + x0;
-	const T* gcoef = static_cast<const T*>(a.coef) + s * a.coef_pitch;
+	T* tile = reinterpret_cast<T*>(smem + 128);
 	const int lane = threadIdx.x;
-
+	const uint32_t n = a.n, S = a.S;
+	const uint32_t box_elems = a.box_rows * kLanes;
+	const T* cB = static_cast<const T*>(a.coef);
+	const T* cE = cB + a.coef_len;
+	const T* cC = cE + a.coef_len;
+	const uint64_t cp = a.coef_len / S; // per-substrate row pitch of the [s][j] tables
 	if (lane == 0)
 	{
 		dev::mbar_init(bar, 1);
 		dev::fence_mbar_init();
 	}
 	__syncwarp();
-	if (lane == 0)
-		dev::mbar_arrive_expect_tx(bar, coef_bytes + n * row_bytes);
-	__syncwarp();
-	if (lane == 0)
-		dev::bulk_g2s(sB, gcoef, coef_bytes, bar);
-	for (uint32_t j = lane; j < n; j += kSweepLanes)
-		dev::bulk_g2s(tile + (uint64_t)j * kSweepLanes, gbase + j * a.line_stride, row_bytes, bar);
 
-	if (!dev::mbar_wait(bar, 0))
+	uint32_t phase = 0;
+	for (uint64_t t = blockIdx.x; t < a.tiles; t += gridDim.x, phase ^= 1)
 	{
+		const int x0 = (int)((t % a.xblocks) * kLanes);
+		const int o = (int)(t / a.xblocks);
 		if (lane == 0)
-			atomicOr(a.err, DEV_ERR_WAIT_TIMEOUT);
-		return;
-	}
-
-	if ((uint64_t)lane < valid)
-	{
-		const T c = static_cast<const T*>(a.coef_c)[s];
-		T* col = tile + lane;
-		T d = col[0];
-#pragma unroll 8
-		for (uint32_t j = 1; j < n; j++)
 		{
-			d = fmadd(sE[j], d, col[(uint64_t)j * kSweepLanes]);
-			col[(uint64_t)j * kSweepLanes] = d;
+			dev::mbar_arrive_expect_tx(bar, a.boxes * box_elems * (uint32_t)sizeof(T));
+			for (uint32_t b = 0; b < a.boxes; b++)
+			{
+				const int j0 = (int)(b * a.box_rows);
+				if (AXIS == 1)
+					dev::tma_load_3d(tile + b * box_elems, &tmap, x0, j0, o, bar);
+				else
+					dev::tma_load_3d(tile + b * box_elems, &tmap, x0, o, j0, bar);
+			}
 		}
-		d = d * sB[n - 1];
-		col[(uint64_t)(n - 1) * kSweepLanes] = d;
-#pragma unroll 8
-		for (int j = (int)n - 2; j >= 0; j--)
+		if (!dev::mbar_wait(bar, phase))
 		{
-			d = fmadd(c, d, col[(uint64_t)j * kSweepLanes]) * sB[j];
-			col[(uint64_t)j * kSweepLanes] = d;
+			if (lane == 0)
+				atomicOr(a.err, DEV_ERR_WAIT_TIMEOUT);
+			return;
 		}
+		if ((uint64_t)(x0 + lane) < a.row_len)
+		{
+			const uint32_t s = (uint32_t)((x0 + lane) % S);
+			solve_column<T>(tile + lane, n, cB + s * cp, cE + s * cp, cC[s]);
+		}
+		dev::fence_proxy_async_smem();
+		__syncwarp();
+		if (lane == 0)
+		{
+			for (uint32_t b = 0; b < a.boxes; b++)
+			{
+				const int j0 = (int)(b * a.box_rows);
+				if (AXIS == 1)
+					dev::tma_store_3d(&tmap, x0, j0, o, tile + b * box_elems);
+				else
+					dev::tma_store_3d(&tmap, x0, o, j0, tile + b * box_elems);
+			}
+			dev::bulk_commit();
+			dev::bulk_wait_read(); // the tile buffer is free once the store has read it
+		}
+		__syncwarp();
 	}
-	dev::fence_proxy_async_smem();
-	__syncwarp();
-	for (uint32_t j = lane; j < n; j += kSweepLanes)
-		dev::bulk_s2g(gbase + j * a.line_stride, tile + (uint64_t)j * kSweepLanes, row_bytes);
-	dev::bulk_commit();
-	dev::bulk_wait_all();
+	if (lane == 0)
+		dev::bulk_wait_all();
 }
 
-// -------------------------------------------------------------------- x
+// ------------------------------------------------------------------ x
 
-template <typename T>
-__global__ void __launch_bounds__(kSweepXRows) sweep_x_kernel(SweepXArgs a)
+// S*sizeof(T) a multiple of 16 bytes: thread h of a row's TPR threads owns chunk
+// slot h of every x position (VN substrates, VN independent recurrences).
+template <typename T, int TPR>
+__device__ __forceinline__ void solve_row_chunks(T* row, const T* __restrict__ cB, const T* __restrict__ cE,
+												 const T* __restrict__ cC, uint32_t n, int h)
+{
+	using V = typename Vec16<T>::type;
+	constexpr int VN = Vec16<T>::N, P = kChunkBlock;
+	V* __restrict__ vrow = reinterpret_cast<V*>(row) + h;
+	const V* vE = reinterpret_cast<const V*>(cE) + h;
+	const V* vB = reinterpret_cast<const V*>(cB) + h;
+	const uint32_t nb = n / P;
+	T d[VN], c[VN];
+#pragma unroll
+	for (int u = 0; u < VN; u++)
+	{
+		d[u] = T(0);
+		c[u] = __ldg(cC + h * VN + u);
+	}
+	auto step_fwd = [&](V& v, const V& e) {
+#pragma unroll
+		for (int u = 0; u < VN; u++)
+		{
+			d[u] = dev::fmadd(vget<V, T>(e, u), d[u], vget<V, T>(v, u));
+			vset<V, T>(v, u, d[u]);
+		}
+	};
+	auto step_bwd = [&](V& v, const V& b) {
+#pragma unroll
+		for (int u = 0; u < VN; u++)
+		{
+			d[u] = dev::fmadd(c[u], d[u], vget<V, T>(v, u)) * vget<V, T>(b, u);
+			vset<V, T>(v, u, d[u]);
+		}
+	};
+	{
+		V x[P], xn[P], e[P], en[P];
+		if (nb)
+#pragma unroll
+			for (int q = 0; q < P; q++)
+			{
+				x[q] = vrow[q * TPR];
+				e[q] = ldg_vec(vE + q * TPR);
+			}
+		for (uint32_t b = 0; b < nb; b++)
+		{
+			const uint32_t i0 = b * P;
+			if (b + 1 < nb)
+#pragma unroll
+				for (int q = 0; q < P; q++)
+				{
+					xn[q] = vrow[(i0 + P + q) * TPR];
+					en[q] = ldg_vec(vE + (i0 + P + q) * TPR);
+				}
+#pragma unroll
+			for (int q = 0; q < P; q++)
+			{
+				step_fwd(x[q], e[q]);
+				vrow[(i0 + q) * TPR] = x[q];
+			}
+#pragma unroll
+			for (int q = 0; q < P; q++)
+			{
+				x[q] = xn[q];
+				e[q] = en[q];
+			}
+		}
+		for (uint32_t i = nb * P; i < n; i++)
+		{
+			V v = vrow[i * TPR];
+			step_fwd(v, ldg_vec(vE + i * TPR));
+			vrow[i * TPR] = v;
+		}
+	}
+#pragma unroll
+	for (int u = 0; u < VN; u++)
+		d[u] = T(0);
+	for (int i = (int)n - 1; i >= (int)(nb * P); i--)
+	{
+		V v = vrow[i * TPR];
+		step_bwd(v, ldg_vec(vB + i * TPR));
+		vrow[i * TPR] = v;
+	}
+	{
+		V x[P], xn[P], bb[P], bn[P];
+		if (nb)
+#pragma unroll
+			for (int q = 0; q < P; q++)
+			{
+				x[q] = vrow[((nb - 1) * P + q) * TPR];
+				bb[q] = ldg_vec(vB + ((nb - 1) * P + q) * TPR);
+			}
+		for (int b = (int)nb - 1; b >= 0; b--)
+		{
+			const uint32_t i0 = (uint32_t)b * P;
+			if (b > 0)
+#pragma unroll
+				for (int q = 0; q < P; q++)
+				{
+					xn[q] = vrow[(i0 - P + q) * TPR];
+					bn[q] = ldg_vec(vB + (i0 - P + q) * TPR);
+				}
+#pragma unroll
+			for (int q = P - 1; q >= 0; q--)
+			{
+				step_bwd(x[q], bb[q]);
+				vrow[(i0 + q) * TPR] = x[q];
+			}
+#pragma unroll
+			for (int q = 0; q < P; q++)
+			{
+				x[q] = xn[q];
+				bb[q] = bn[q];
+			}
+		}
+	}
+}
+
+// ST substrates (1..8) not filling whole chunks: the row is a stream of chunks,
+// element k of substrate k % ST.  Blocks of NB chunks hold whole groups of
+// lcm(ST, VN) elements, so each element's substrate is a compile-time index.
+template <typename T, int ST>
+__device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, const T* __restrict__ cE,
+											  const T* __restrict__ cC, uint32_t n)
 {
 	using V = typename Vec16<T>::type;
 	constexpr int VN = Vec16<T>::N;
+	constexpr int GE = group_elems(ST, VN);
+	constexpr int U = GE / VN;
+	constexpr int NB = U * ((kChunkBlock + U - 1) / U); // chunks per block
+	const uint32_t total = n * ST;
+	const uint32_t nchunks = (total + GE - 1) / GE * U; // whole groups (tail elements predicated)
+	V* __restrict__ vrow = reinterpret_cast<V*>(row);
+	const V* vE = reinterpret_cast<const V*>(cE);
+	const V* vB = reinterpret_cast<const V*>(cB);
+	T d[ST], c[ST];
+#pragma unroll
+	for (int s = 0; s < ST; s++)
+	{
+		d[s] = T(0);
+		c[s] = __ldg(cC + s);
+	}
+	// In a block or group starting at chunk k0 (k0*VN a multiple of ST), element
+	// k0*VN + q*VN + u has substrate (q*VN + u) % ST.
+	auto fwd_chunk = [&](V& v, const V& e, int q, uint32_t k) {
+#pragma unroll
+		for (int u = 0; u < VN; u++)
+		{
+			const int s = (q * VN + u) % ST;
+			if (k * VN + u < total)
+			{
+				d[s] = dev::fmadd(vget<V, T>(e, u), d[s], vget<V, T>(v, u));
+				vset<V, T>(v, u, d[s]);
+			}
+		}
+	};
+	auto bwd_chunk = [&](V& v, const V& b, int q, uint32_t k) {
+#pragma unroll
+		for (int u = VN - 1; u >= 0; u--)
+		{
+			const int s = (q * VN + u) % ST;
+			if (k * VN + u < total)
+			{
+				d[s] = dev::fmadd(c[s], d[s], vget<V, T>(v, u)) * vget<V, T>(b, u);
+				vset<V, T>(v, u, d[s]);
+			}
+		}
+	};
+	const uint32_t nb = nchunks / NB;
+	{
+		V x[NB], xn[NB], e[NB], en[NB];
+		if (nb)
+#pragma unroll
+			for (int q = 0; q < NB; q++)
+			{
+				x[q] = vrow[q];
+				e[q] = ldg_vec(vE + q);
+			}
+		for (uint32_t b = 0; b < nb; b++)
+		{
+			const uint32_t k0 = b * NB;
+			if (b + 1 < nb)
+#pragma unroll
+				for (int q = 0; q < NB; q++)
+				{
+					xn[q] = vrow[k0 + NB + q];
+					en[q] = ldg_vec(vE + k0 + NB + q);
+				}
+#pragma unroll
+			for (int q = 0; q < NB; q++)
+			{
+				fwd_chunk(x[q], e[q], q, k0 + q);
+				vrow[k0 + q] = x[q];
+			}
+#pragma unroll
+			for (int q = 0; q < NB; q++)
+			{
+				x[q] = xn[q];
+				e[q] = en[q];
+			}
+		}
+		// remaining whole groups (fewer than NB chunks)
+		for (uint32_t k0 = nb * NB; k0 < nchunks; k0 += U)
+		{
+#pragma unroll
+			for (int q = 0; q < U; q++)
+			{
+				V v = vrow[k0 + q];
+				fwd_chunk(v, ldg_vec(vE + k0 + q), q, k0 + q);
+				vrow[k0 + q] = v;
+			}
+		}
+	}
+#pragma unroll
+	for (int s = 0; s < ST; s++)
+		d[s] = T(0);
+	for (int k0 = (int)nchunks - U; k0 >= (int)(nb * NB); k0 -= U)
+	{
+#pragma unroll
+		for (int q = U - 1; q >= 0; q--)
+		{
+			V v = vrow[k0 + q];
+			bwd_chunk(v, ldg_vec(vB + k0 + q), q, (uint32_t)(k0 + q));
+			vrow[k0 + q] = v;
+		}
+	}
+	{
+		V x[NB], xn[NB], bb[NB], bn[NB];
+		if (nb)
+#pragma unroll
+			for (int q = 0; q < NB; q++)
+			{
+				x[q] = vrow[(nb - 1) * NB + q];
+				bb[q] = ldg_vec(vB + (nb - 1) * NB + q);
+			}
+		for (int b = (int)nb - 1; b >= 0; b--)
+		{
+			const uint32_t k0 = (uint32_t)b * NB;
+			if (b > 0)
+#pragma unroll
+				for (int q = 0; q < NB; q++)
+				{
+					xn[q] = vrow[k0 - NB + q];
+					bn[q] = ldg_vec(vB + k0 - NB + q);
+				}
+#pragma unroll
+			for (int q = NB - 1; q >= 0; q--)
+			{
+				bwd_chunk(x[q], bb[q], q, k0 + q);
+				vrow[k0 + q] = x[q];
+			}
+#pragma unroll
+			for (int q = 0; q < NB; q++)
+			{
+				x[q] = xn[q];
+				bb[q] = bn[q];
+			}
+		}
+	}
+}
+
+// Any S: one recurrence at a time, scalar shared-memory accesses.
+template <typename T>
+__device__ __forceinline__ void solve_row_generic(T* row, const T* cB, const T* cE, const T* cC, uint32_t n,
+												  uint32_t S)
+{
+	for (uint32_t s = 0; s < S; s++)
+	{
+		T d = T(0);
+		for (uint32_t i = 0; i < n; i++)
+		{
+			d = dev::fmadd(__ldg(cE + i * S + s), d, row[i * S + s]);
+			row[i * S + s] = d;
+		}
+		const T c = __ldg(cC + s);
+		d = T(0);
+		for (int i = (int)n - 1; i >= 0; i--)
+		{
+			d = dev::fmadd(c, d, row[i * S + s]) * __ldg(cB + i * S + s);
+			row[i * S + s] = d;
+		}
+	}
+}
+
+template <typename T, int ST>
+constexpr int x_tpr()
+{
+	return (ST > 0 && ST <= 8 && (ST * (int)sizeof(T)) % 16 == 0) ? ST * (int)sizeof(T) / 16 : 1;
+}
+
+// A tile is rows_per_tile consecutive rows; the CTA has rows_per_tile * TPR threads (<= 32).
+template <typename T, int ST>
+__global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
+{
+	constexpr int TPR = x_tpr<T, ST>();
 	extern __shared__ __align__(128) unsigned char smem[];
 	uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
-	const uint64_t npad = a.coef_pitch / 2;
-	T* sB = reinterpret_cast<T*>(smem + 16);
-	T* sE = sB + npad;
-	T* rows = sB + a.coef_pitch;
-
-	const uint64_t t = blockIdx.x;
-	if (t >= a.tiles)
-		return;
-	const uint64_t rb = t % a.rblocks;
-	const uint64_t s = t / a.rblocks;
-	const uint64_t r0 = rb * kSweepXRows;
-	const uint64_t nrows = a.rows - r0 < (uint64_t)kSweepXRows ? a.rows - r0 : (uint64_t)kSweepXRows;
-	const uint32_t n = (uint32_t)a.n;
-	const uint32_t row_bytes = (uint32_t)(npad * sizeof(T));
-	const uint32_t coef_bytes = (uint32_t)(a.coef_pitch * sizeof(T));
-	const uint64_t plane = a.rows * a.pitch;
-
-	T* gbase = static_cast<T*>(a.field) + s * plane + r0 * a.pitch;
-	const T* gcoef = static_cast<const T*>(a.coef) + s * a.coef_pitch;
-	const int lane = threadIdx.x;
-
-	if (lane == 0)
+	T* tile = reinterpret_cast<T*>(smem + 16);
+	const int tid = threadIdx.x;
+	const uint32_t R = a.rows_per_tile;
+	const int r_local = tid / TPR, h = tid % TPR;
+	const uint32_t n = a.n;
+	const uint32_t row_bytes = (uint32_t)round_up(a.row_len * sizeof(T), 16);
+	const T* cB = static_cast<const T*>(a.coef);
+	const T* cE = cB + a.coef_len;
+	const T* cC = cE + a.coef_len;
+	if (tid == 0)
 	{
 		dev::mbar_init(bar, 1);
 		dev::fence_mbar_init();
 	}
-	__syncwarp();
-	if (lane == 0)
-		dev::mbar_arrive_expect_tx(bar, coef_bytes + (uint32_t)nrows * row_bytes);
-	__syncwarp();
-	if (lane == 0)
-		dev::bulk_g2s(sB, gcoef, coef_bytes, bar);
-	if ((uint64_t)lane < nrows)
-		dev::bulk_g2s(rows + lane * a.smem_pitch, gbase + lane * a.pitch, row_bytes, bar);
+	__syncthreads();
 
-	if (!dev::mbar_wait(bar, 0))
+	uint32_t phase = 0;
+	for (uint64_t t = blockIdx.x; t < a.tiles; t += gridDim.x, phase ^= 1)
 	{
-		if (lane == 0)
-			atomicOr(a.err, DEV_ERR_WAIT_TIMEOUT);
-		return;
-	}
-
-	if ((uint64_t)lane < nrows)
-	{
-		const T c = static_cast<const T*>(a.coef_c)[s];
-		V* row = reinterpret_cast<V*>(rows + lane * a.smem_pitch);
-		const V* vE = reinterpret_cast<const V*>(sE);
-		const V* vB = reinterpret_cast<const V*>(sB);
-		const uint32_t nv = (n + VN - 1) / VN;
-		T d = T(0);
-		// forward elimination; E[0] = 0 makes the first point pass through unchanged
-		for (uint32_t k = 0; k < nv; k++)
+		const uint64_t r0 = t * R;
+		const uint32_t nrows = (uint32_t)(a.rows - r0 < (uint64_t)R ? a.rows - r0 : (uint64_t)R);
+		T* g = static_cast<T*>(a.field) + r0 * a.pitch;
+		if (tid == 0)
+			dev::mbar_arrive_expect_tx(bar, nrows * row_bytes);
+		__syncthreads();
+		if ((uint32_t)tid < nrows)
+			dev::bulk_g2s(tile + tid * a.smem_pitch, g + tid * a.pitch, row_bytes, bar);
+		if (!dev::mbar_wait(bar, phase))
 		{
-			V v = row[k];
-			const V e = vE[k];
-#pragma unroll
-			for (int u = 0; u < VN; u++)
-			{
-				if (k * VN + u < n)
-				{
-					d = fmadd(vget<T>(e, u), d, vget<T>(v, u));
-					vset<T>(v, u, d);
-				}
-			}
-			row[k] = v;
+			if (tid == 0)
+				atomicOr(a.err, DEV_ERR_WAIT_TIMEOUT);
+			return;
 		}
-		// back substitution
-		for (int k = (int)nv - 1; k >= 0; k--)
+		if ((uint32_t)r_local < nrows)
 		{
-			V v = row[k];
-			const V b = vB[k];
-#pragma unroll
-			for (int u = VN - 1; u >= 0; u--)
-			{
-				const uint32_t i = (uint32_t)k * VN + u;
-				if (i == n - 1)
-				{
-					d = vget<T>(v, u) * vget<T>(b, u);
-					vset<T>(v, u, d);
-				}
-				else if (i < n - 1)
-				{
-					d = fmadd(c, d, vget<T>(v, u)) * vget<T>(b, u);
-					vset<T>(v, u, d);
-				}
-			}
-			row[k] = v;
+			T* row = tile + r_local * a.smem_pitch;
+			if constexpr (ST == 0)
+				solve_row_generic<T>(row, cB, cE, cC, n, a.S);
+			else if constexpr ((ST * (int)sizeof(T)) % 16 == 0)
+				solve_row_chunks<T, TPR>(row, cB, cE, cC, n, h);
+			else
+				solve_row_vec<T, ST>(row, cB, cE, cC, n);
 		}
+		dev::fence_proxy_async_smem();
+		__syncthreads();
+		if ((uint32_t)tid < nrows)
+			dev::bulk_s2g(g + tid * a.pitch, tile + tid * a.smem_pitch, row_bytes);
+		dev::bulk_commit();
+		dev::bulk_wait_read();
+		__syncthreads();
 	}
-	dev::fence_proxy_async_smem();
-	__syncwarp();
-	if ((uint64_t)lane < nrows)
-		dev::bulk_s2g(gbase + lane * a.pitch, rows + lane * a.smem_pitch, row_bytes);
-	dev::bulk_commit();
 	dev::bulk_wait_all();
+}
+
+void box_geometry(uint64_t n, uint32_t& box_rows, uint32_t& boxes);
+
+struct Plan
+{
+	uint64_t smem;
+	int threads;
+	uint64_t rows_per_tile;
+};
+
+template <typename T>
+Plan plan(const Context* c, int axis)
+{
+	Plan p {};
+	if (axis == 0)
+	{
+		const uint64_t row_stage = sweep_x_smem_pitch(c->row_len, c->S, sizeof(T)) * sizeof(T);
+		const uint64_t tpr = x_threads_per_row(c->S, sizeof(T));
+		// aim for >= 4 CTAs per SM so that every scheduler has a warp
+		uint64_t rows = (kMaxSmemBytes / 4) / row_stage;
+		const uint64_t cap = kLanes / tpr;
+		rows = rows < 1 ? 1 : (rows > cap ? cap : rows);
+		p.rows_per_tile = rows;
+		p.smem = 16 + rows * row_stage;
+		p.threads = (int)(rows * tpr);
+		return p;
+	}
+	uint32_t box_rows, boxes;
+	box_geometry(c->n[axis], box_rows, boxes);
+	p.smem = 128 + (uint64_t)boxes * box_rows * kLanes * sizeof(T);
+	p.threads = kLanes;
+	return p;
+}
+
+template <typename KernelT>
+int launch_persistent(Context* c, KernelT kernel, const SweepArgs& a, const Plan& p, int kid, double bytes)
+{
+	PCG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem));
+	int per_sm = 0;
+	PCG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, p.threads, p.smem));
+	if (per_sm < 1)
+		return fail(PCG_ERR_UNSUPPORTED, "sweep tile does not fit in shared memory");
+	uint64_t grid = (uint64_t)per_sm * (uint64_t)c->sm_count;
+	if (grid > a.tiles)
+		grid = a.tiles;
+	cudaEvent_t ev;
+	launch_begin(c, kid, bytes, &ev);
+	kernel<<<(unsigned)grid, p.threads, p.smem, c->stream>>>(a);
+	launch_end(c, kid, ev);
+	PCG_CUDA_TRY(cudaGetLastError());
+	return PCG_OK;
+}
+
+SweepArgs base_args(const Context* c, int axis)
+{
+	SweepArgs a {};
+	a.field = c->field.ptr;
+	a.coef = c->coef[axis].ptr;
+	a.coef_len = c->coef_len[axis];
+	a.coef_elems = c->coef_elems[axis];
+	a.S = (uint32_t)c->S;
+	a.n = (uint32_t)c->n[axis];
+	a.row_len = c->row_len;
+	a.pitch = c->pitch;
+	a.rows = c->rows;
+	a.err = static_cast<uint32_t*>(c->err.ptr);
+	return a;
+}
+
+template <typename T>
+int run_sweep_x(Context* c)
+{
+	SweepArgs a = base_args(c, 0);
+	a.smem_pitch = sweep_x_smem_pitch(c->row_len, c->S, sizeof(T));
+	const Plan p = plan<T>(c, 0);
+	if (p.smem > kMaxSmemBytes)
+		return fail(PCG_ERR_UNSUPPORTED, "x rows too long for the shared-memory x sweep");
+	a.rows_per_tile = (uint32_t)p.rows_per_tile;
+	a.tiles = (c->rows + p.rows_per_tile - 1) / p.rows_per_tile;
+	const double bytes = 2.0 * (double)(c->V * c->S) * (double)sizeof(T);
+	switch (c->S)
+	{
+	case 1: return launch_persistent(c, sweep_x_kernel<T, 1>, a, p, K_SWEEP_X, bytes);
+	case 2: return launch_persistent(c, sweep_x_kernel<T, 2>, a, p, K_SWEEP_X, bytes);
+	case 3: return launch_persistent(c, sweep_x_kernel<T, 3>, a, p, K_SWEEP_X, bytes);
+	case 4: return launch_persistent(c, sweep_x_kernel<T, 4>, a, p, K_SWEEP_X, bytes);
+	case 5: return launch_persistent(c, sweep_x_kernel<T, 5>, a, p, K_SWEEP_X, bytes);
+	case 6: return launch_persistent(c, sweep_x_kernel<T, 6>, a, p, K_SWEEP_X, bytes);
+	case 7: return launch_persistent(c, sweep_x_kernel<T, 7>, a, p, K_SWEEP_X, bytes);
+	case 8: return launch_persistent(c, sweep_x_kernel<T, 8>, a, p, K_SWEEP_X, bytes);
+	default: return launch_persistent(c, sweep_x_kernel<T, 0>, a, p, K_SWEEP_X, bytes);
+	}
+}
+
+template <typename T>
+int run_sweep_yz(Context* c, int axis)
+{
+	SweepArgs a = base_args(c, axis);
+	if (axis == 1)
+	{
+		a.line_stride = c->pitch;
+		a.outer_stride = c->n[1] * c->pitch;
+		a.tiles = c->n[2];
+	}
+	else
+	{
+		a.line_stride = c->n[1] * c->pitch;
+		a.outer_stride = c->pitch;
+		a.tiles = c->n[1];
+	}
+	a.xblocks = (c->row_len + kLanes - 1) / kLanes;
+	a.tiles *= a.xblocks;
+	a.box_rows = c->tmap_box_rows[axis];
+	a.boxes = c->tmap_boxes[axis];
+	const Plan p = plan<T>(c, axis);
+	if (p.smem > kMaxSmemBytes)
+		return fail(PCG_ERR_UNSUPPORTED, "lines too long for the shared-memory y/z sweep");
+	if (a.box_rows == 0)
+		return fail(PCG_ERR_INVALID, "tensor maps of the field were not prepared");
+	const int kid = axis == 1 ? K_SWEEP_Y : K_SWEEP_Z;
+	const double bytes = 2.0 * (double)(c->V * c->S) * (double)sizeof(T);
+	auto kernel = axis == 1 ? sweep_yz_kernel<T, 1> : sweep_yz_kernel<T, 2>;
+	PCG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem));
+	int per_sm = 0;
+	PCG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, p.threads, p.smem));
+	if (per_sm < 1)
+		return fail(PCG_ERR_UNSUPPORTED, "sweep tile does not fit in shared memory");
+	uint64_t grid = (uint64_t)per_sm * (uint64_t)c->sm_count;
+	if (grid > a.tiles)
+		grid = a.tiles;
+	cudaEvent_t ev;
+	launch_begin(c, kid, bytes, &ev);
+	kernel<<<(unsigned)grid, p.threads, p.smem, c->stream>>>(a, c->tmap[axis]);
+	launch_end(c, kid, ev);
+	PCG_CUDA_TRY(cudaGetLastError());
+	return PCG_OK;
+}
+
+// Points per TMA box along a swept axis of length n (boxes are at most 256 long).
+void box_geometry(uint64_t n, uint32_t& box_rows, uint32_t& boxes)
+{
+	boxes = (uint32_t)((n + 255) / 256);
+	box_rows = (uint32_t)((n + boxes - 1) / boxes);
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+								   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+								   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+	static EncodeTiledFn fn = nullptr;
+	if (!fn)
+	{
+		void* p = nullptr;
+		cudaDriverEntryPointQueryResult q {};
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+				cudaSuccess &&
+			q == cudaDriverEntryPointSuccess)
+			fn = reinterpret_cast<EncodeTiledFn>(p);
+	}
+	return fn;
 }
 
 } // namespace
 
 // -------------------------------------------------------------------- host side
 
-uint64_t sweep_x_smem_pitch(const Context* c)
+uint64_t coef_table_len(uint64_t n, uint64_t S, size_t wsize)
 {
-	const uint64_t chunk = 16 / c->wsize; // elements per 16-byte chunk
-	uint64_t chunks = round_up(c->n[0], chunk) / chunk;
-	chunks += (1 + 8 - chunks % 8) % 8; // chunks per row == 1 (mod 8): conflict-free 16-byte lanes
-	return chunks * chunk;
+	const int vn = (int)(16 / wsize);
+	return round_up(n * S, (uint64_t)group_elems((int)S, vn));
 }
 
-uint64_t sweep_x_smem_bytes(const Context* c)
+uint64_t coef_row_pitch(uint64_t n) { return round_up(n, kBlock); }
+
+uint64_t x_threads_per_row(uint64_t S, size_t wsize)
 {
-	return 16 + c->coef_pitch[0] * c->wsize + (uint64_t)kSweepXRows * sweep_x_smem_pitch(c) * c->wsize;
+	return (S <= 8 && (S * wsize) % 16 == 0) ? S * wsize / 16 : 1;
 }
 
-uint64_t sweep_yz_smem_bytes(const Context* c, int axis)
+uint64_t sweep_x_smem_pitch(uint64_t row_len, uint64_t S, size_t wsize)
 {
-	return 16 + c->coef_pitch[axis] * c->wsize + c->n[axis] * (uint64_t)kSweepLanes * c->wsize;
+	const uint64_t vn = 16 / wsize;
+	const uint64_t ge = (uint64_t)group_elems((int)S, (int)vn);
+	const uint64_t tpr = x_threads_per_row(S, wsize);
+	uint64_t chunks = round_up(row_len, ge) / vn;
+	// rows tpr (mod 8) chunks apart: the 8 lanes of a quarter-warp (8/tpr rows x tpr
+	// chunk slots) read 8 distinct 16-byte bank groups
+	const uint64_t want = tpr % 8;
+	chunks += (want + 8 - chunks % 8) % 8;
+	return chunks * vn;
 }
 
-template <typename T>
-static int run_sweep_x(Context* c)
+// Encodes the TMA tensor maps of the y and z sweeps for the current field buffer.
+int prepare_sweep_maps(Context* c)
 {
-	SweepXArgs a {};
-	a.field = c->field.ptr;
-	a.coef = c->coef[0].ptr;
-	a.coef_c = c->coef_c[0].ptr;
-	a.coef_pitch = c->coef_pitch[0];
-	a.n = c->n[0];
-	a.pitch = c->pitch;
-	a.rows = c->n[1] * c->n[2];
-	a.rblocks = (a.rows + kSweepXRows - 1) / kSweepXRows;
-	a.tiles = a.rblocks * c->S;
-	a.smem_pitch = sweep_x_smem_pitch(c);
-	a.err = static_cast<uint32_t*>(c->err.ptr);
-	const uint64_t smem = sweep_x_smem_bytes(c);
-	if (smem > kMaxSmemBytes)
-		return fail(PCG_ERR_UNSUPPORTED, "x extent too long for the shared-memory x sweep");
-	PCG_CUDA_TRY(cudaFuncSetAttribute(sweep_x_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-	cudaEvent_t ev;
-	launch_begin(c, K_SWEEP_X, 2.0 * (double)(c->V * c->S) * (double)sizeof(T), &ev);
-	sweep_x_kernel<T><<<(unsigned)a.tiles, kSweepXRows, smem, c->stream>>>(a);
-	launch_end(c, K_SWEEP_X, ev);
-	PCG_CUDA_TRY(cudaGetLastError());
+	EncodeTiledFn enc = encode_fn();
+	if (!enc)
+		return fail(PCG_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+	const cuuint64_t dims[3] = { c->row_len, c->n[1], c->n[2] };
+	const cuuint64_t strides[2] = { c->pitch * c->wsize, c->n[1] * c->pitch * c->wsize };
+	const cuuint32_t estr[3] = { 1, 1, 1 };
+	const CUtensorMapDataType dt = c->wsize == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+	for (int axis = 1; axis < c->dims; axis++)
+	{
+		uint32_t box_rows, boxes;
+		box_geometry(c->n[axis], box_rows, boxes);
+		const cuuint32_t box[3] = { (cuuint32_t)kLanes, axis == 1 ? box_rows : 1u, axis == 2 ? box_rows : 1u };
+		CUresult r = enc(&c->tmap[axis], dt, 3, c->field.ptr, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+						 CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+						 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+		if (r != CUDA_SUCCESS)
+			return fail(PCG_ERR_CUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r));
+		c->tmap_box_rows[axis] = box_rows;
+		c->tmap_boxes[axis] = boxes;
+	}
 	return PCG_OK;
 }
 
-template <typename T>
-static int run_sweep_yz(Context* c, int axis)
+uint64_t sweep_smem_bytes(const Context* c, int axis)
 {
-	SweepYZArgs a {};
-	a.field = c->field.ptr;
-	a.coef = c->coef[axis].ptr;
-	a.coef_c = c->coef_c[axis].ptr;
-	a.coef_pitch = c->coef_pitch[axis];
-	a.n = c->n[axis];
-	a.nx = c->n[0];
-	a.plane = c->plane;
-	if (axis == 1)
-	{
-		a.line_stride = c->pitch;
-		a.outer_count = c->n[2];
-		a.outer_stride = c->n[1] * c->pitch;
-	}
-	else
-	{
-		a.line_stride = c->n[1] * c->pitch;
-		a.outer_count = c->n[1];
-		a.outer_stride = c->pitch;
-	}
-	a.xblocks = (c->n[0] + kSweepLanes - 1) / kSweepLanes;
-	a.tiles = a.xblocks * a.outer_count * c->S;
-	a.err = static_cast<uint32_t*>(c->err.ptr);
-	const uint64_t smem = sweep_yz_smem_bytes(c, axis);
-	if (smem > kMaxSmemBytes)
-		return fail(PCG_ERR_UNSUPPORTED, "line too long for the shared-memory y/z sweep");
-	PCG_CUDA_TRY(cudaFuncSetAttribute(sweep_yz_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-	const int kid = axis == 1 ? K_SWEEP_Y : K_SWEEP_Z;
-	cudaEvent_t ev;
-	launch_begin(c, kid, 2.0 * (double)(c->V * c->S) * (double)sizeof(T), &ev);
-	sweep_yz_kernel<T><<<(unsigned)a.tiles, kSweepLanes, smem, c->stream>>>(a);
-	launch_end(c, kid, ev);
-	PCG_CUDA_TRY(cudaGetLastError());
-	return PCG_OK;
+	return c->wsize == 4 ? plan<float>(c, axis).smem : plan<double>(c, axis).smem;
 }
 
 int launch_sweep_x(Context* c) { return c->wsize == 4 ? run_sweep_x<float>(c) : run_sweep_x<double>(c); }
