@@ -345,6 +345,12 @@ __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.comm
 // Waits until this thread's bulk groups have finished reading shared memory.
 __device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 
+// Same, except for the most recently committed group.
+__device__ __forceinline__ void bulk_wait_read_allbut1()
+{
+	asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+}
+
 // Waits until this thread's bulk groups have completed.
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 

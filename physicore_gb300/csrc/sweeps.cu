@@ -73,178 +73,241 @@ __device__ __forceinline__ V ldg_vec(const V* p)
 
 // ------------------------------------------------------------------ y / z
 
-// One line at col[j*kLanes], j < n; eE/eB are the line's substrate rows of the
-// [s][j] coefficient table (16-byte aligned, padded to a multiple of kBlock).
-template <typename T>
-__device__ __forceinline__ void solve_column(T* __restrict__ col, uint32_t n, const T* __restrict__ eB,
-											 const T* __restrict__ eE, T c)
-{
-	using V = typename Vec16<T>::type;
-	constexpr int P = kBlock, VN = Vec16<T>::N, NV = P / VN;
-	const uint32_t nb = n / P;
-	T d = T(0);
-	// ---- forward
-	{
-		T x[P], xn[P];
-		V e[NV], en[NV];
-		if (nb)
-		{
-#pragma unroll
-			for (int q = 0; q < P; q++)
-				x[q] = col[q * kLanes];
-#pragma unroll
-			for (int v = 0; v < NV; v++)
-				e[v] = ldg_vec(reinterpret_cast<const V*>(eE) + v);
-		}
-		for (uint32_t b = 0; b < nb; b++)
-		{
-			T* blk = col + (uint64_t)b * P * kLanes;
-			if (b + 1 < nb)
-			{
-#pragma unroll
-				for (int q = 0; q < P; q++)
-					xn[q] = blk[(P + q) * kLanes];
-#pragma unroll
-				for (int v = 0; v < NV; v++)
-					en[v] = ldg_vec(reinterpret_cast<const V*>(eE + (b + 1) * P) + v);
-			}
-#pragma unroll
-			for (int q = 0; q < P; q++)
-			{
-				d = dev::fmadd(vget<V, T>(e[q / VN], q % VN), d, x[q]);
-				blk[q * kLanes] = d;
-			}
-#pragma unroll
-			for (int q = 0; q < P; q++)
-				x[q] = xn[q];
-#pragma unroll
-			for (int v = 0; v < NV; v++)
-				e[v] = en[v];
-		}
-		for (uint32_t j = nb * P; j < n; j++)
-		{
-			d = dev::fmadd(__ldg(eE + j), d, col[(uint64_t)j * kLanes]);
-			col[(uint64_t)j * kLanes] = d;
-		}
-	}
-	// ---- backward (top partial block first, then aligned full blocks downwards)
-	d = T(0);
-	for (int j = (int)n - 1; j >= (int)(nb * P); j--)
-	{
-		d = dev::fmadd(c, d, col[(uint64_t)j * kLanes]) * __ldg(eB + j);
-		col[(uint64_t)j * kLanes] = d;
-	}
-	{
-		T x[P], xn[P];
-		V bb[NV], bn[NV];
-		if (nb)
-		{
-			const T* blk = col + (uint64_t)(nb - 1) * P * kLanes;
-#pragma unroll
-			for (int q = 0; q < P; q++)
-				x[q] = blk[q * kLanes];
-#pragma unroll
-			for (int v = 0; v < NV; v++)
-				bb[v] = ldg_vec(reinterpret_cast<const V*>(eB + (nb - 1) * P) + v);
-		}
-		for (int b = (int)nb - 1; b >= 0; b--)
-		{
-			T* blk = col + (uint64_t)b * P * kLanes;
-			if (b > 0)
-			{
-#pragma unroll
-				for (int q = 0; q < P; q++)
-					xn[q] = blk[(q - P) * kLanes];
-#pragma unroll
-				for (int v = 0; v < NV; v++)
-					bn[v] = ldg_vec(reinterpret_cast<const V*>(eB + (b - 1) * P) + v);
-			}
-#pragma unroll
-			for (int q = P - 1; q >= 0; q--)
-			{
-				d = dev::fmadd(c, d, x[q]) * vget<V, T>(bb[q / VN], q % VN);
-				blk[q * kLanes] = d;
-			}
-#pragma unroll
-			for (int q = 0; q < P; q++)
-				x[q] = xn[q];
-#pragma unroll
-			for (int v = 0; v < NV; v++)
-				bb[v] = bn[v];
-		}
-	}
-}
-
-// One TMA tensor box per box_rows points moves a whole [n][32] tile: the field is
-// described to the TMA unit as a 3-D tensor (x*S+s, y, z), and a tile is the box
-// (32, box_rows, 1) at (x0, j0, z) for the y sweep or (32, 1, box_rows) at
-// (x0, y, j0) for the z sweep.  Elements beyond the row (x*S+s >= nx*S) or the line
-// are zero-filled on load and not written on store.
+// The y/z sweep as a "zipper" pipeline over one shared-memory buffer per CTA.
+//
+// A tile (32 consecutive (x,s) elements at all n points of the lines of one outer
+// index) is split into nc chunks of R points; each chunk moves as one TMA tensor
+// box (32, R) of the field described as the 3-D tensor (x*S+s, y, z).  Chunk c of
+// the CTA's k-th tile sits in slot c when k is even and in slot nc-1-c when k is
+// odd.  Back substitution finishes chunks from the top (c = nc-1 first); each
+// finished chunk is stored, and its slot immediately receives chunk nc-1-c of the
+// next tile -- exactly the chunk order in which that tile's forward elimination
+// will want them.  Loads, stores and both passes therefore overlap inside one
+// buffer, so all shared memory holds line data.  Each slot has an mbarrier that
+// completes once per tile.
 template <typename T, int AXIS>
 __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __grid_constant__ CUtensorMap tmap)
 {
+	using V = typename Vec16<T>::type;
+	constexpr int P = kBlock, VN = Vec16<T>::N, NV = P / VN;
 	extern __shared__ __align__(128) unsigned char smem[];
-	uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
-	T* tile = reinterpret_cast<T*>(smem + 128);
-	const int lane = threadIdx.x;
 	const uint32_t n = a.n, S = a.S;
-	const uint32_t box_elems = a.box_rows * kLanes;
+	const uint32_t R = a.box_rows; // points per chunk, a multiple of P
+	const uint32_t nc = a.boxes;   // chunks per line
+	const uint32_t chunk_elems = R * kLanes;
+	const uint32_t chunk_bytes = chunk_elems * (uint32_t)sizeof(T);
+	uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+	T* base = reinterpret_cast<T*>(smem + round_up(nc * 8, 128));
+	const int lane = threadIdx.x;
 	const T* cB = static_cast<const T*>(a.coef);
 	const T* cE = cB + a.coef_len;
 	const T* cC = cE + a.coef_len;
 	const uint64_t cp = a.coef_len / S; // per-substrate row pitch of the [s][j] tables
+	const uint32_t nb = n / P;          // full blocks; blocks never straddle chunks
+
 	if (lane == 0)
 	{
-		dev::mbar_init(bar, 1);
+		for (uint32_t c = 0; c < nc; c++)
+			dev::mbar_init(&full[c], 1);
 		dev::fence_mbar_init();
 	}
 	__syncwarp();
 
-	uint32_t phase = 0;
-	for (uint64_t t = blockIdx.x; t < a.tiles; t += gridDim.x, phase ^= 1)
+	auto coords = [&](uint64_t t, int& x0, int& o) {
+		x0 = (int)((t % a.xblocks) * kLanes);
+		o = (int)(t / a.xblocks);
+	};
+	auto load_chunk = [&](uint64_t t, uint32_t c, uint32_t slot) { // lane 0
+		int x0, o;
+		coords(t, x0, o);
+		dev::mbar_arrive_expect_tx(&full[slot], chunk_bytes);
+		if (AXIS == 1)
+			dev::tma_load_3d(base + slot * chunk_elems, &tmap, x0, (int)(c * R), o, &full[slot]);
+		else
+			dev::tma_load_3d(base + slot * chunk_elems, &tmap, x0, o, (int)(c * R), &full[slot]);
+	};
+	auto store_chunk = [&](uint64_t t, uint32_t c, uint32_t slot) { // lane 0
+		int x0, o;
+		coords(t, x0, o);
+		if (AXIS == 1)
+			dev::tma_store_3d(&tmap, x0, (int)(c * R), o, base + slot * chunk_elems);
+		else
+			dev::tma_store_3d(&tmap, x0, o, (int)(c * R), base + slot * chunk_elems);
+		dev::bulk_commit();
+	};
+
+	uint64_t t = blockIdx.x;
+	if (t < a.tiles && lane == 0)
+		for (uint32_t c = 0; c < nc; c++)
+			load_chunk(t, c, c);
+	const uint32_t BPC = R / P;           // blocks per chunk
+	const uint32_t tail = n - nb * P;     // rows after the last full block (all in the last chunk)
+	const uint32_t blk_elems = P * kLanes;
+	bool ok = true;
+	for (uint32_t k = 0; t < a.tiles && ok; t += gridDim.x, k++)
 	{
-		const int x0 = (int)((t % a.xblocks) * kLanes);
-		const int o = (int)(t / a.xblocks);
-		if (lane == 0)
+		const bool rev = (k & 1) != 0;
+		const uint32_t par = k & 1;
+		const uint64_t tn = t + gridDim.x;
+		const bool has_next = tn < a.tiles;
+		int x0, o;
+		coords(t, x0, o);
+		const uint32_t s = (uint64_t)(x0 + lane) < a.row_len ? (uint32_t)((x0 + lane) % S) : 0;
+		const T* __restrict__ eB = cB + s * cp;
+		const T* __restrict__ eE = cE + s * cp;
+		const T cc = cC[s];
+		// this lane's column of chunk ch (lanes past the row hold zero-filled, never-stored columns)
+		auto chunk_ptr = [&](uint32_t ch) { return base + (rev ? nc - 1 - ch : ch) * chunk_elems + lane; };
+		auto wait_chunk = [&](uint32_t ch) { return dev::mbar_wait(&full[rev ? nc - 1 - ch : ch], par); };
+
+		// ---- forward elimination, block by block; a block never straddles chunks
+		T d = T(0);
+		ok = wait_chunk(0);
+		T* pcur = chunk_ptr(0);
+		uint32_t ch = 0, bin = 0; // chunk and block-in-chunk of pcur
 		{
-			dev::mbar_arrive_expect_tx(bar, a.boxes * box_elems * (uint32_t)sizeof(T));
-			for (uint32_t b = 0; b < a.boxes; b++)
+			T x[P], xn[P];
+			V e[NV], en[NV];
+			const V* ve = reinterpret_cast<const V*>(eE);
+			if (nb)
 			{
-				const int j0 = (int)(b * a.box_rows);
-				if (AXIS == 1)
-					dev::tma_load_3d(tile + b * box_elems, &tmap, x0, j0, o, bar);
-				else
-					dev::tma_load_3d(tile + b * box_elems, &tmap, x0, o, j0, bar);
+#pragma unroll
+				for (int q = 0; q < P; q++)
+					x[q] = pcur[q * kLanes];
+#pragma unroll
+				for (int v = 0; v < NV; v++)
+					e[v] = __ldg(ve + v);
+			}
+			for (uint32_t b = 0; b < nb; b++)
+			{
+				T* pnext = pcur + blk_elems;
+				if (++bin == BPC)
+				{
+					bin = 0;
+					if (++ch < nc)
+					{
+						ok = ok && wait_chunk(ch);
+						pnext = chunk_ptr(ch);
+					}
+				}
+				if (b + 1 < nb)
+				{
+#pragma unroll
+					for (int q = 0; q < P; q++)
+						xn[q] = pnext[q * kLanes];
+#pragma unroll
+					for (int v = 0; v < NV; v++)
+						en[v] = __ldg(ve + (b + 1) * NV + v);
+				}
+#pragma unroll
+				for (int q = 0; q < P; q++)
+				{
+					d = dev::fmadd(vget<V, T>(e[q / VN], q % VN), d, x[q]);
+					pcur[q * kLanes] = d;
+				}
+				pcur = pnext;
+#pragma unroll
+				for (int q = 0; q < P; q++)
+					x[q] = xn[q];
+#pragma unroll
+				for (int v = 0; v < NV; v++)
+					e[v] = en[v];
+			}
+			// pcur now addresses row nb*P (the tail, inside the last chunk)
+			for (uint32_t j = 0; j < tail; j++)
+			{
+				d = dev::fmadd(__ldg(eE + nb * P + j), d, pcur[j * kLanes]);
+				pcur[j * kLanes] = d;
 			}
 		}
-		if (!dev::mbar_wait(bar, phase))
-		{
+		if (!ok)
+			break;
+
+		// ---- back substitution; finished chunks are stored and their slots refilled
+		int pending = -1; // finished chunk whose slot awaits the next tile's load
+		auto finish_chunk = [&](uint32_t fch) {
+			dev::fence_proxy_async_smem();
+			__syncwarp();
 			if (lane == 0)
-				atomicOr(a.err, DEV_ERR_WAIT_TIMEOUT);
-			return;
-		}
-		if ((uint64_t)(x0 + lane) < a.row_len)
-		{
-			const uint32_t s = (uint32_t)((x0 + lane) % S);
-			solve_column<T>(tile + lane, n, cB + s * cp, cE + s * cp, cC[s]);
-		}
-		dev::fence_proxy_async_smem();
-		__syncwarp();
-		if (lane == 0)
-		{
-			for (uint32_t b = 0; b < a.boxes; b++)
 			{
-				const int j0 = (int)(b * a.box_rows);
-				if (AXIS == 1)
-					dev::tma_store_3d(&tmap, x0, j0, o, tile + b * box_elems);
-				else
-					dev::tma_store_3d(&tmap, x0, o, j0, tile + b * box_elems);
+				store_chunk(t, fch, rev ? nc - 1 - fch : fch);
+				if (has_next && pending >= 0)
+				{
+					dev::bulk_wait_read_allbut1(); // the previous chunk's store has read its slot
+					const uint32_t pc = (uint32_t)pending;
+					load_chunk(tn, nc - 1 - pc, rev ? nc - 1 - pc : pc);
+				}
 			}
-			dev::bulk_commit();
-			dev::bulk_wait_read(); // the tile buffer is free once the store has read it
+			pending = (int)fch;
+			__syncwarp();
+		};
+		d = T(0);
+		for (int j = (int)tail - 1; j >= 0; j--)
+		{
+			d = dev::fmadd(cc, d, pcur[j * kLanes]) * __ldg(eB + nb * P + j);
+			pcur[j * kLanes] = d;
+		}
+		if (tail && nb % BPC == 0)
+			finish_chunk(nb / BPC); // the last chunk holds tail rows only
+		if (nb)
+		{
+			ch = (nb - 1) / BPC;
+			bin = (nb - 1) % BPC;
+			pcur = chunk_ptr(ch) + bin * blk_elems;
+			T x[P], xn[P];
+			V bb[NV], bn[NV];
+			const V* vb = reinterpret_cast<const V*>(eB);
+#pragma unroll
+			for (int q = 0; q < P; q++)
+				x[q] = pcur[q * kLanes];
+#pragma unroll
+			for (int v = 0; v < NV; v++)
+				bb[v] = __ldg(vb + (nb - 1) * NV + v);
+			for (int b = (int)nb - 1; b >= 0; b--)
+			{
+				T* pnext = bin ? pcur - blk_elems : (ch ? chunk_ptr(ch - 1) + (BPC - 1) * blk_elems : pcur);
+				if (b > 0)
+				{
+#pragma unroll
+					for (int q = 0; q < P; q++)
+						xn[q] = pnext[q * kLanes];
+#pragma unroll
+					for (int v = 0; v < NV; v++)
+						bn[v] = __ldg(vb + (b - 1) * NV + v);
+				}
+#pragma unroll
+				for (int q = P - 1; q >= 0; q--)
+				{
+					d = dev::fmadd(cc, d, x[q]) * vget<V, T>(bb[q / VN], q % VN);
+					pcur[q * kLanes] = d;
+				}
+				if (bin == 0)
+				{
+					finish_chunk(ch);
+					bin = BPC - 1;
+					ch--;
+				}
+				else
+					bin--;
+				pcur = pnext;
+#pragma unroll
+				for (int q = 0; q < P; q++)
+					x[q] = xn[q];
+#pragma unroll
+				for (int v = 0; v < NV; v++)
+					bb[v] = bn[v];
+			}
+		}
+		if (lane == 0 && has_next && pending >= 0)
+		{
+			dev::bulk_wait_read();
+			const uint32_t pc = (uint32_t)pending;
+			load_chunk(tn, nc - 1 - pc, rev ? nc - 1 - pc : pc);
 		}
 		__syncwarp();
 	}
+	if (!ok && lane == 0)
+		atomicOr(a.err, DEV_ERR_WAIT_TIMEOUT);
 	if (lane == 0)
 		dev::bulk_wait_all();
 }
@@ -630,7 +693,7 @@ Plan plan(const Context* c, int axis)
 	}
 	uint32_t box_rows, boxes;
 	box_geometry(c->n[axis], box_rows, boxes);
-	p.smem = 128 + (uint64_t)boxes * box_rows * kLanes * sizeof(T);
+	p.smem = round_up((uint64_t)boxes * 8, 128) + (uint64_t)boxes * box_rows * kLanes * sizeof(T);
 	p.threads = kLanes;
 	return p;
 }
@@ -739,11 +802,31 @@ int run_sweep_yz(Context* c, int axis)
 	return PCG_OK;
 }
 
-// Points per TMA box along a swept axis of length n (boxes are at most 256 long).
+// Chunk geometry of the y/z zipper: R points per chunk (a multiple of the solver
+// block, at most 256, the TMA box limit).  The first size in order of preference
+// (about 32 points: enough chunks to pipeline, few TMA operations) that pads the
+// line by at most 1/8 wins; otherwise the size with the fewest padded points.
 void box_geometry(uint64_t n, uint32_t& box_rows, uint32_t& boxes)
 {
-	boxes = (uint32_t)((n + 255) / 256);
-	box_rows = (uint32_t)((n + boxes - 1) / boxes);
+	static const uint32_t pref[] = { 32, 40, 48, 24, 56, 64, 16, 72, 80, 96, 112, 128, 8, 160, 192, 256 };
+	uint64_t best = ~0ull;
+	for (uint32_t R : pref)
+	{
+		const uint64_t nc = (n + R - 1) / R;
+		const uint64_t rows = nc * R;
+		if ((rows - n) * 8 <= n)
+		{
+			box_rows = R;
+			boxes = (uint32_t)nc;
+			return;
+		}
+		if (rows < best)
+		{
+			best = rows;
+			box_rows = R;
+			boxes = (uint32_t)nc;
+		}
+	}
 }
 
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
