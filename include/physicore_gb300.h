@@ -183,6 +183,34 @@ int pcg_reset_kernel_stats(pcg_context* ctx);
 /* Kernels launched by this context since creation or the last reset. */
 int pcg_get_launch_count(pcg_context* ctx, uint64_t* launches);
 
+/* ---- allocation-free cell step ------------------------------------------- */
+
+/* No counterpart in the reference.  For callers that cannot let a library
+ * allocate device memory -- frameworks that serve all GPU memory from their own
+ * pool or arena, and loops that must avoid the device synchronisation of
+ * cudaMalloc/cudaFree -- this runs one cell secretion/uptake pass (ballot rebuilt,
+ * then the density and internalized updates; cell_solver.cpp:246-272 with
+ * recompute) on buffers the caller owns, and allocates nothing.
+ *
+ *  - field: FP32 device field in the interleaved layout with row pitch `pitch`
+ *    elements (>= grid_shape[0] * substrates), rows ordered by y then z.
+ *  - All agent arrays are device pointers, laid out as in pcg_set_agents;
+ *    internalized is updated in place when compute_internalized is non-zero.
+ *  - Work is queued on `stream` (NULL: the default stream), and the call then
+ *    synchronises that stream to report device faults (PCG_ERR_DEVICE).
+ *  - Scratch comes from one fixed 16 MiB array in device memory that every GPU
+ *    loading this library holds until the process exits; a problem that needs
+ *    more (about 8 bytes per voxel plus 8 + 24*substrates bytes per agent) is
+ *    rejected with PCG_ERR_UNSUPPORTED.  The first call on a device looks up the
+ *    array's device address, so make that first call before any stream capture.
+ *  - All calls share the array: calls that overlap on the GPU (other streams,
+ *    other host threads) race with each other and must be serialised. */
+int pcg_cells_noalloc(float* field, uint64_t pitch, int dims, const int64_t bbox_min[3],
+					  const uint64_t voxel_shape[3], const uint64_t grid_shape[3], uint64_t substrates, double dt,
+					  uint64_t agents, const double* positions, const double* secretion, const double* saturation,
+					  const double* uptake, const double* net_export, const double* volumes, const uint8_t* is_active,
+					  double* internalized, int compute_internalized, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -356,6 +356,62 @@ int launch_cells(Context* c, bool recompute)
 	return c->wsize == 4 ? run_cells<float>(c, recompute) : run_cells<double>(c, recompute);
 }
 
+// The same kernels over caller-owned buffers: the counts are cleared here, the
+// conflict flag, ballot slots and reduced terms by the locate kernel.
+int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream)
+{
+	if (b.A == 0)
+		return PCG_OK;
+	CellArgs a {};
+	a.dims = b.dims;
+	a.A = b.A;
+	a.S = b.S;
+	for (int d = 0; d < 3; d++)
+	{
+		a.n[d] = b.n[d];
+		a.bbmin[d] = (double)b.bbmin[d];
+		a.voxel[d] = (double)b.voxel[d];
+	}
+	a.pitch = b.pitch;
+	a.Vv = (double)(b.voxel[0] * b.voxel[1] * b.voxel[2]);
+	a.dt = b.dt;
+	a.pos = b.pos;
+	a.sec = b.sec;
+	a.sat = b.sat;
+	a.upt = b.upt;
+	a.net = b.net;
+	a.vol = b.vol;
+	a.frac = nullptr;
+	a.active = b.active;
+	a.internal = b.internal;
+	a.vox = b.vox;
+	a.foff = b.foff;
+	a.num = b.num;
+	a.den = b.den;
+	a.fac = b.fac;
+	a.rnum = b.rnum;
+	a.rden = b.rden;
+	a.rfac = b.rfac;
+	a.owner = b.owner;
+	a.counts = b.counts;
+	a.flags = b.flags;
+	a.err = b.err;
+	a.field = b.field;
+	a.internalized = b.internalized;
+	const uint64_t V = b.n[0] * b.n[1] * b.n[2];
+	const unsigned block = 256;
+	const unsigned grid = (unsigned)((b.A + block - 1) / block);
+	PCG_CUDA_TRY(cudaMemsetAsync(b.counts, 0, V * sizeof(uint32_t), stream));
+	cells_locate_kernel<float><<<grid, block, 0, stream>>>(a);
+	cells_ballot_kernel<<<grid, block, 0, stream>>>(a);
+	cells_reduce_kernel<float><<<grid, block, 0, stream>>>(a);
+	cells_apply_kernel<float><<<grid, block, 0, stream>>>(a);
+	if (b.internalized)
+		cells_internalize_kernel<float><<<grid, block, 0, stream>>>(a);
+	PCG_CUDA_TRY(cudaGetLastError());
+	return PCG_OK;
+}
+
 template <typename T>
 static int run_release(Context* c, uint64_t agent)
 {

@@ -233,6 +233,29 @@ int launch_to_host_layout(Context* c, void* dst, int layout, int dtype);
 int launch_from_host_layout(Context* c, const void* src, int layout, int dtype);
 int launch_fill_initial(Context* c);
 
+// One FP32 cell secretion/uptake pass (ballot rebuilt) over caller-owned device
+// buffers, with the scratch arrays supplied by the caller as well; used by the
+// allocation-free entry point.
+struct CellStepBuffers
+{
+	int dims;
+	uint64_t A, S;
+	uint64_t n[3];
+	int64_t bbmin[3];
+	uint64_t voxel[3];
+	uint64_t pitch; // field row pitch (elements)
+	double dt;
+	const double *pos, *sec, *sat, *upt, *net, *vol;
+	const uint8_t* active;
+	double* internal;
+	int internalized;
+	float* field;
+	// scratch: vox/foff [A], owner/counts [V], flags/err [4] each, terms [A*S] each
+	uint32_t *vox, *foff, *owner, *counts, *flags, *err;
+	float *num, *den, *fac, *rnum, *rden, *rfac;
+};
+int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream);
+
 // geometry helpers shared by the launchers and the feasibility checks
 uint64_t coef_table_len(uint64_t n, uint64_t S, size_t wsize);
 uint64_t coef_row_pitch(uint64_t n);
