@@ -169,8 +169,8 @@ int pcg_synchronize(pcg_context* ctx);
 /* ---- device-resident access (benchmarks, zero-copy integration) -------- */
 
 /* Device pointer of the field, its element size and row pitch (elements).
- * Device layout: planar, row-padded: element (s,x,y,z) is at
- * ptr[((s*nz + z)*ny + y)*pitch + x]. */
+ * Device layout: the reference's interleaved order with padded rows: element
+ * (s,x,y,z) is at ptr[(z*ny + y)*pitch + x*S + s]. */
 int pcg_get_field_device(pcg_context* ctx, void** ptr, uint64_t* elem_bytes, uint64_t* pitch);
 
 /* ---- measurement -------------------------------------------------------- */
@@ -182,6 +182,51 @@ int pcg_get_kernel_stats(pcg_context* ctx, pcg_kernel_stat* stats, uint64_t cap,
 int pcg_reset_kernel_stats(pcg_context* ctx);
 /* Kernels launched by this context since creation or the last reset. */
 int pcg_get_launch_count(pcg_context* ctx, uint64_t* launches);
+
+/* ---- batches of independent domains -------------------------------------- */
+
+/* No counterpart in the reference, which steps one microenvironment per solver
+ * (openmp_solver.cpp:23-40).  A batch steps many initialised contexts of one
+ * precision on one device together: every phase of a step is one launch over all
+ * domains (one persistent launch per sweep axis, tiles handed out dynamically),
+ * and the step is replayed from a CUDA graph.  Each domain's arithmetic and
+ * phase order are those of pcg_solve on that context, whose buffers the batch
+ * uses in place: results are read back with the per-context calls.
+ *  - The contexts stay owned by the caller and must outlive the batch; setters
+ *    that change a context's sizes or tables are picked up at the next
+ *    pcg_batch_solve (descriptors rebuilt, graph re-captured).
+ *  - Work is queued on the batch's stream, ordered after each context's stream
+ *    on entry and before it on return, so per-context calls see the results. */
+typedef struct pcg_batch pcg_batch;
+
+int pcg_batch_create(pcg_batch** out, pcg_context* const* contexts, uint64_t count);
+int pcg_batch_destroy(pcg_batch* batch);
+/* `iterations` steps of every domain (solver::solve; a context whose positional
+ * data are marked for recomputation rebuilds its ballot on each of them). */
+int pcg_batch_solve(pcg_batch* batch, uint64_t iterations);
+int pcg_batch_synchronize(pcg_batch* batch);
+int pcg_batch_get_stream(pcg_batch* batch, void** stream);
+/* Replays the step from a CUDA graph (default 1) or launches it directly. */
+int pcg_batch_set_graph(pcg_batch* batch, int enable);
+/* Times candidate line mappings and tile shapes of each sweep axis for each size
+ * bucket (line length, substrates) present in the batch and keeps the fastest;
+ * results are cached for the process.  Field contents are restored afterwards. */
+int pcg_batch_autotune(pcg_batch* batch);
+/* Overrides the autotuner for one sweep axis of every domain (tests, experiments):
+ * mapping PCG_MAP_ROW (a thread owns a row) or PCG_MAP_SUBSTRATE (a thread owns
+ * one substrate of a row; x only), rows = rows per x tile or points per y/z chunk
+ * (0: the default); clamped per domain to what fits.  mapping < 0 removes it. */
+#define PCG_MAP_ROW 0
+#define PCG_MAP_SUBSTRATE 1
+int pcg_batch_force_config(pcg_batch* batch, int axis, int mapping, uint32_t rows);
+/* Writes a JSON description of the per-bucket choices (NUL-terminated, at most
+ * cap bytes); *needed receives the full length including the NUL. */
+int pcg_batch_describe(pcg_batch* batch, char* text, uint64_t cap, uint64_t* needed);
+int pcg_batch_set_kernel_timing(pcg_batch* batch, int enable);
+int pcg_batch_get_kernel_stats(pcg_batch* batch, pcg_kernel_stat* stats, uint64_t cap, uint64_t* count);
+int pcg_batch_reset_kernel_stats(pcg_batch* batch);
+/* Kernels launched by this batch (graph replays count their kernels). */
+int pcg_batch_get_launch_count(pcg_batch* batch, uint64_t* launches);
 
 /* ---- allocation-free cell step ------------------------------------------- */
 

@@ -22,6 +22,7 @@ DTYPE_F64, DTYPE_F32 = 0, 1
 PHASE_DIFFUSION, PHASE_DIRICHLET, PHASE_BULK, PHASE_CELLS = 1, 2, 4, 8
 PHASE_ALL = 15
 BULK_NONE, BULK_UNIFORM, BULK_PER_VOXEL = 0, 1, 2
+MAP_ROW, MAP_SUBSTRATE = 0, 1
 
 ERRORS = {1: "invalid", 2: "cuda", 3: "nomem", 4: "device", 5: "unsupported"}
 
@@ -71,6 +72,19 @@ SIGNATURES = {
     "pcg_get_kernel_stats": [_P, _P, _u64, _P],
     "pcg_reset_kernel_stats": [_P],
     "pcg_get_launch_count": [_P, _P],
+    "pcg_batch_create": [_P, _P, _u64],
+    "pcg_batch_destroy": [_P],
+    "pcg_batch_solve": [_P, _u64],
+    "pcg_batch_synchronize": [_P],
+    "pcg_batch_get_stream": [_P, _P],
+    "pcg_batch_set_graph": [_P, _i32],
+    "pcg_batch_autotune": [_P],
+    "pcg_batch_force_config": [_P, _i32, _i32, _u32],
+    "pcg_batch_describe": [_P, _P, _u64, _P],
+    "pcg_batch_set_kernel_timing": [_P, _i32],
+    "pcg_batch_get_kernel_stats": [_P, _P, _u64, _P],
+    "pcg_batch_reset_kernel_stats": [_P],
+    "pcg_batch_get_launch_count": [_P, _P],
 }
 
 _lib = None
@@ -303,4 +317,80 @@ class Solver:
     def launch_count(self):
         v = ctypes.c_uint64()
         self._check(self._L.pcg_get_launch_count(self._h, ctypes.byref(v)))
+        return v.value
+
+
+class Batch:
+    """Many Solver contexts (one device, one precision) stepped together: every
+    phase is one launch over all domains and the step replays from a CUDA graph.
+    Results are read back through each Solver."""
+
+    def __init__(self, solvers):
+        self._L = load_library()
+        self.solvers = list(solvers)  # the contexts must outlive the batch
+        arr = (ctypes.c_void_p * len(self.solvers))(*[s.handle.value for s in self.solvers])
+        h = ctypes.c_void_p()
+        self._check(self._L.pcg_batch_create(ctypes.byref(h), arr, len(self.solvers)))
+        self._h = h
+
+    def _check(self, rc):
+        if rc != 0:
+            raise PcgError(rc, self._L.pcg_last_error().decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.pcg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, iterations=1):
+        self._check(self._L.pcg_batch_solve(self._h, iterations))
+
+    def synchronize(self):
+        self._check(self._L.pcg_batch_synchronize(self._h))
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        self._check(self._L.pcg_batch_get_stream(self._h, ctypes.byref(s)))
+        return s.value
+
+    def set_graph(self, enable):
+        self._check(self._L.pcg_batch_set_graph(self._h, int(bool(enable))))
+
+    def autotune(self):
+        self._check(self._L.pcg_batch_autotune(self._h))
+
+    def force_config(self, axis, mapping, rows=0):
+        """mapping: MAP_ROW / MAP_SUBSTRATE (x only); -1 returns the axis to the tuner."""
+        self._check(self._L.pcg_batch_force_config(self._h, axis, mapping, rows))
+
+    def describe(self):
+        import json
+        need = ctypes.c_uint64()
+        self._check(self._L.pcg_batch_describe(self._h, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value)
+        self._check(self._L.pcg_batch_describe(self._h, buf, need.value, ctypes.byref(need)))
+        return json.loads(buf.value.decode())
+
+    def set_kernel_timing(self, enable):
+        self._check(self._L.pcg_batch_set_kernel_timing(self._h, int(bool(enable))))
+
+    def kernel_stats(self):
+        arr = (KernelStat * 32)()
+        cnt = ctypes.c_uint64()
+        self._check(self._L.pcg_batch_get_kernel_stats(self._h, arr, 32, ctypes.byref(cnt)))
+        return {arr[i].name.decode(): {"launches": arr[i].launches, "ms": arr[i].total_ms,
+                                       "bytes": arr[i].algorithmic_bytes} for i in range(min(cnt.value, 32))}
+
+    def reset_kernel_stats(self):
+        self._check(self._L.pcg_batch_reset_kernel_stats(self._h))
+
+    def launch_count(self):
+        v = ctypes.c_uint64()
+        self._check(self._L.pcg_batch_get_launch_count(self._h, ctypes.byref(v)))
         return v.value

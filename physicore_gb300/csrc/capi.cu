@@ -31,7 +31,7 @@ const char* kernel_name(int id)
 	static const char* names[K_COUNT] = { "sweep_x",	  "sweep_y",		"sweep_z",	   "dirichlet_faces",
 										  "dirichlet_interior", "bulk", "cells_locate", "cells_ballot",
 										  "cells_reduce", "cells_apply", "cells_internalize", "cells_release",
-										  "mass",		  "layout" };
+										  "mass",		  "layout", "cells_clear" };
 	return (id >= 0 && id < K_COUNT) ? names[id] : "?";
 }
 
@@ -113,23 +113,21 @@ void collect_timings(Context* c)
 
 // ------------------------------------------------------------------ helpers
 
-struct DeviceGuard
-{
-	int prev = -1;
-	explicit DeviceGuard(int dev)
-	{
-		cudaGetDevice(&prev);
-		if (prev != dev)
-			cudaSetDevice(dev);
-	}
-	~DeviceGuard()
-	{
-		if (prev >= 0)
-			cudaSetDevice(prev);
-	}
-};
-
 // Reads and clears the device error word after synchronising the stream.
+std::string device_error_text(uint32_t word)
+{
+	std::string msg = "device fault:";
+	if (word & DEV_ERR_AGENT_OUTSIDE)
+		msg += " an active agent lies outside the mesh;";
+	if (word & DEV_ERR_WAIT_TIMEOUT)
+		msg += " a bounded shared-memory wait timed out;";
+	if (word & DEV_ERR_DIRICHLET_INDEX)
+		msg += " a Dirichlet voxel lies outside the mesh;";
+	if (word & DEV_ERR_BAD_TILE)
+		msg += " a batched tile descriptor was invalid;";
+	return msg;
+}
+
 static int check_device(Context* c)
 {
 	cudaError_t e = cudaStreamSynchronize(c->stream);
@@ -141,16 +139,7 @@ static int check_device(Context* c)
 	if (word)
 	{
 		PCG_CUDA_TRY(cudaMemset(c->err.ptr, 0, sizeof(uint32_t)));
-		std::string msg = "device fault:";
-		if (word & DEV_ERR_AGENT_OUTSIDE)
-			msg += " an active agent lies outside the mesh;";
-		if (word & DEV_ERR_WAIT_TIMEOUT)
-			msg += " a bounded shared-memory wait timed out;";
-		if (word & DEV_ERR_DIRICHLET_INDEX)
-			msg += " a Dirichlet voxel lies outside the mesh;";
-		if (word & DEV_ERR_BAD_TILE)
-			msg += " a batched tile descriptor was invalid;";
-		return fail(PCG_ERR_DEVICE, msg);
+		return fail(PCG_ERR_DEVICE, device_error_text(word));
 	}
 	return PCG_OK;
 }
@@ -376,8 +365,12 @@ static int do_initialize(Context* c)
 			return fail(PCG_ERR_UNSUPPORTED, "a line of axis " + std::to_string(axis) +
 												 " exceeds the shared-memory sweep limit");
 	c->initialized = true;
+	c->generation++;
 	return check_device(c);
 }
+
+int initialize_context(Context* c) { return do_initialize(c); }
+int check_context(Context* c) { return check_device(c); }
 
 static int alloc_agents(Context* c, uint64_t A)
 {
@@ -414,8 +407,6 @@ static int alloc_agents(Context* c, uint64_t A)
 using pcg::Context;
 using pcg::fail;
 
-struct pcg_context : Context
-{};
 
 #define CTX_CHECK(ctx)                                                                                       \
 	do                                                                                                       \
@@ -512,6 +503,7 @@ int pcg_get_stream(pcg_context* c, void** stream)
 int pcg_set_mesh(pcg_context* c, int dims, const int64_t bbmin[3], const int64_t bbmax[3], const uint64_t voxel[3])
 {
 	CTX_CHECK(c);
+	c->generation++;
 	if (c->initialized)
 		return fail(PCG_ERR_INVALID, "the mesh cannot change after initialize");
 	if (dims < 1 || dims > 3)
@@ -553,6 +545,7 @@ int pcg_set_substrates(pcg_context* c, uint64_t S, double dt, const double* D, c
 					   const double* initial)
 {
 	CTX_CHECK(c);
+	c->generation++;
 	if (c->initialized)
 		return fail(PCG_ERR_INVALID, "substrates cannot change after initialize");
 	if (S == 0 || !D || !decay || !initial)
@@ -569,6 +562,7 @@ int pcg_set_dirichlet_interior(pcg_context* c, uint64_t K, const uint64_t* voxel
 							   const uint8_t* conditions)
 {
 	CTX_CHECK(c);
+	c->generation++;
 	if (!c->mesh_set || c->S == 0)
 		return fail(PCG_ERR_INVALID, "mesh and substrates must be set before Dirichlet nodes");
 	if (K && (!voxels || !values || !conditions))
@@ -590,6 +584,7 @@ int pcg_set_dirichlet_interior(pcg_context* c, uint64_t K, const uint64_t* voxel
 int pcg_set_dirichlet_boundary(pcg_context* c, int axis, int side, const double* values, const uint8_t* conditions)
 {
 	CTX_CHECK(c);
+	c->generation++;
 	if (axis < 0 || axis > 2 || side < 0 || side > 1)
 		return fail(PCG_ERR_INVALID, "axis must be 0..2 and side 0 (min) or 1 (max)");
 	if (c->S == 0)
@@ -611,6 +606,7 @@ int pcg_set_dirichlet_boundary(pcg_context* c, int axis, int side, const double*
 int pcg_set_bulk(pcg_context* c, int mode, const double* supply, const double* uptake, const double* target)
 {
 	CTX_CHECK(c);
+	c->generation++;
 	if (mode != PCG_BULK_NONE && mode != PCG_BULK_UNIFORM && mode != PCG_BULK_PER_VOXEL)
 		return fail(PCG_ERR_INVALID, "unknown bulk mode");
 	if (mode != PCG_BULK_NONE && (!supply || !uptake || !target))
@@ -639,6 +635,7 @@ int pcg_set_agents(pcg_context* c, uint64_t A, const double* positions, const do
 				   int compute_internalized)
 {
 	CTX_CHECK(c);
+	c->generation++;
 	if (!c->mesh_set || c->S == 0)
 		return fail(PCG_ERR_INVALID, "mesh and substrates must be set before agents");
 	if (A >= 0xffffffffull)

@@ -25,226 +25,56 @@
 //    fused or two-pass branch.  A voxel's substrates are adjacent in the field, so
 //    each agent touches one 32-byte sector of densities (S <= 8, FP32).
 //  Internalized substrates are kept in FP64 in both builds.
-#include "pcg_internal.cuh"
+#include "cells_device.cuh"
 
 namespace pcg {
 
 namespace {
 
-constexpr uint32_t kNoAgent = 0xffffffffu;
+using namespace cellsdev;
 
-struct CellArgs
-{
-	int dims;
-	uint64_t A, S;
-	uint64_t n[3];
-	double bbmin[3];
-	double voxel[3];
-	uint64_t pitch;
-	double Vv, dt;
-	const double *pos, *sec, *sat, *upt, *net, *vol, *frac;
-	const uint8_t* active;
-	double* internal;
-	uint32_t* vox;
-	uint32_t* foff;
-	void *num, *den, *fac, *rnum, *rden, *rfac;
-	uint32_t* owner;
-	uint32_t* counts;
-	uint32_t* flags; // [0] conflict
-	uint32_t* err;
-	void* field;
-	int internalized;
-};
-
-// cartesian_mesh::voxel_position (mesh.cpp:37-61); false when outside the grid.
-__device__ __forceinline__ bool locate(const CellArgs& a, uint64_t i, uint64_t idx[3])
-{
-	idx[0] = idx[1] = idx[2] = 0;
-	for (int d = 0; d < a.dims; d++)
-	{
-		const double q = (a.pos[i * a.dims + d] - a.bbmin[d]) / a.voxel[d];
-		if (!(q >= 0.0) || q >= (double)a.n[d])
-			return false;
-		idx[d] = (uint64_t)q;
-	}
-	return true;
-}
-
-// compute_intermediates + clear_ballots (cell_solver.cpp:22-77)
 template <typename T>
 __global__ void cells_locate_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	if (i == 0)
 		a.flags[0] = 0;
-	if (i >= a.A)
-		return;
-	uint64_t idx[3];
-	if (!a.active[i])
-	{
-		a.vox[i] = kNoAgent;
-		return;
-	}
-	if (!locate(a, i, idx))
-	{
-		atomicOr(a.err, DEV_ERR_AGENT_OUTSIDE);
-		a.vox[i] = kNoAgent;
-		return;
-	}
-	const uint32_t v = (uint32_t)(idx[0] + a.n[0] * (idx[1] + a.n[1] * idx[2]));
-	a.vox[i] = v;
-	a.foff[i] = (uint32_t)((idx[2] * a.n[1] + idx[1]) * a.pitch + idx[0] * a.S);
-	a.owner[v] = kNoAgent;
-	T* num = static_cast<T*>(a.num);
-	T* den = static_cast<T*>(a.den);
-	T* fac = static_cast<T*>(a.fac);
-	T* rnum = static_cast<T*>(a.rnum);
-	T* rden = static_cast<T*>(a.rden);
-	T* rfac = static_cast<T*>(a.rfac);
-	const double vol = a.vol[i];
-	for (uint64_t s = 0; s < a.S; s++)
-	{
-		const uint64_t k = i * a.S + s;
-		num[k] = (T)(a.sec[k] * a.sat[k] * a.dt * vol / a.Vv);
-		den[k] = (T)((a.upt[k] + a.sec[k]) * a.dt * vol / a.Vv);
-		fac[k] = (T)(a.net[k] * a.dt / a.Vv);
-		rnum[k] = T(0);
-		rden[k] = T(0);
-		rfac[k] = T(0);
-	}
+	if (i < a.A)
+		agent_locate<T>(a, i);
 }
 
-// ballot (cell_solver.cpp:79-101 with a canonical winner)
 __global__ void cells_ballot_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	const uint32_t key = i < a.A ? a.vox[i] : kNoAgent;
-	const uint32_t group = __match_any_sync(0xffffffffu, key);
-	if (key == kNoAgent)
-		return;
-	const int lane = threadIdx.x & 31;
-	if (lane == __ffs(group) - 1)
-	{
-		// lanes of a warp hold consecutive agent indices, so the leader is the group minimum
-		atomicMin(a.owner + key, (uint32_t)i);
-		atomicAdd(a.counts + key, (uint32_t)__popc(group));
-	}
+	// lanes of a warp hold consecutive agent indices, so a group's leader is its minimum
+	warp_ballot(&a, i, key, key);
 }
 
-// sums into the winner's row (cell_solver.cpp:102-127)
 template <typename T>
 __global__ void cells_reduce_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	const uint32_t key = i < a.A ? a.vox[i] : kNoAgent;
-	bool conflict = false;
-	if (key != kNoAgent)
-	{
-		const uint32_t w = a.owner[key];
-		conflict = w != (uint32_t)i;
-		const T* num = static_cast<const T*>(a.num);
-		const T* den = static_cast<const T*>(a.den);
-		const T* fac = static_cast<const T*>(a.fac);
-		T* rnum = static_cast<T*>(a.rnum);
-		T* rden = static_cast<T*>(a.rden);
-		T* rfac = static_cast<T*>(a.rfac);
-		for (uint64_t s = 0; s < a.S; s++)
-		{
-			const uint64_t k = i * a.S + s;
-			const uint64_t kw = (uint64_t)w * a.S + s;
-			atomicAdd(rnum + kw, num[k]);
-			atomicAdd(rden + kw, conflict ? den[k] : den[k] + T(1));
-			atomicAdd(rfac + kw, fac[k]);
-		}
-	}
+	const bool conflict = key != kNoAgent && agent_reduce<T>(a, i, key);
 	if (__any_sync(0xffffffffu, conflict) && (threadIdx.x & 31) == 0)
 		atomicOr(a.flags, 1u);
 }
 
-constexpr int kSubBatch = 8; // substrates whose loads are issued together
-
-// compute_result (cell_solver.cpp:187-227).  All loads of a batch of substrates are
-// issued before any store, so an agent's independent memory accesses overlap.
 template <typename T>
 __global__ void cells_apply_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-	if (i >= a.A)
-		return;
-	const uint32_t key = a.vox[i];
-	if (key == kNoAgent)
-		return;
-	const uint32_t off = a.foff[i];
-	const bool fused = a.internalized && *(volatile uint32_t*)a.flags == 0;
-	if (!fused && a.owner[key] != (uint32_t)i)
-		return;
-	T* __restrict__ D = static_cast<T*>(a.field) + off;
-	const T* __restrict__ rn = static_cast<const T*>(a.rnum) + i * a.S;
-	const T* __restrict__ rd = static_cast<const T*>(a.rden) + i * a.S;
-	const T* __restrict__ rf = static_cast<const T*>(a.rfac) + i * a.S;
-	double* __restrict__ I = a.internal + i * a.S;
-	for (uint32_t s0 = 0; s0 < a.S; s0 += kSubBatch)
-	{
-		T dv[kSubBatch], n_[kSubBatch], d_[kSubBatch], f_[kSubBatch];
-		double iv[kSubBatch];
-#pragma unroll
-		for (int q = 0; q < kSubBatch; q++)
-			if (s0 + q < a.S)
-			{
-				dv[q] = D[s0 + q];
-				n_[q] = rn[s0 + q];
-				d_[q] = rd[s0 + q];
-				f_[q] = rf[s0 + q];
-				if (fused)
-					iv[q] = I[s0 + q];
-			}
-#pragma unroll
-		for (int q = 0; q < kSubBatch; q++)
-			if (s0 + q < a.S)
-			{
-				const T next = (dv[q] + n_[q]) / d_[q] + f_[q];
-				D[s0 + q] = next;
-				if (fused)
-					I[s0 + q] = iv[q] + a.Vv * ((double)dv[q] - (double)next);
-			}
-	}
+	if (i < a.A)
+		agent_apply<T>(a, i);
 }
 
-// compute_internalized after a conflict (cell_solver.cpp:229-243)
 template <typename T>
 __global__ void cells_internalize_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-	if (i >= a.A)
-		return;
-	if (*(volatile uint32_t*)a.flags == 0)
-		return;
-	if (a.vox[i] == kNoAgent)
-		return;
-	const T* __restrict__ D = static_cast<const T*>(a.field) + a.foff[i];
-	const T* __restrict__ nu = static_cast<const T*>(a.num) + i * a.S;
-	const T* __restrict__ de = static_cast<const T*>(a.den) + i * a.S;
-	const T* __restrict__ fa = static_cast<const T*>(a.fac) + i * a.S;
-	double* __restrict__ I = a.internal + i * a.S;
-	for (uint32_t s0 = 0; s0 < a.S; s0 += kSubBatch)
-	{
-		T dv[kSubBatch], n_[kSubBatch], d_[kSubBatch], f_[kSubBatch];
-		double iv[kSubBatch];
-#pragma unroll
-		for (int q = 0; q < kSubBatch; q++)
-			if (s0 + q < a.S)
-			{
-				dv[q] = D[s0 + q];
-				n_[q] = nu[s0 + q];
-				d_[q] = de[s0 + q];
-				f_[q] = fa[s0 + q];
-				iv[q] = I[s0 + q];
-			}
-#pragma unroll
-		for (int q = 0; q < kSubBatch; q++)
-			if (s0 + q < a.S)
-				I[s0 + q] = iv[q] - a.Vv * ((double)n_[q] - (double)dv[q] * (double)d_[q] + (double)f_[q]);
-	}
+	if (i < a.A)
+		agent_internalize<T>(a, i);
 }
 
 // release_internal (cell_solver.cpp:274-289) for one agent
@@ -266,7 +96,11 @@ __global__ void cells_release_kernel(CellArgs a, uint64_t agent)
 	a.internal[k] = 0.0;
 }
 
-CellArgs make_args(Context* c)
+} // namespace
+
+namespace cellsdev {
+
+CellArgs make_cell_args(const Context* c)
 {
 	CellArgs a {};
 	a.dims = c->dims;
@@ -307,14 +141,14 @@ CellArgs make_args(Context* c)
 	return a;
 }
 
-} // namespace
+} // namespace cellsdev
 
 template <typename T>
 static int run_cells(Context* c, bool recompute)
 {
 	if (c->A == 0)
 		return PCG_OK;
-	CellArgs a = make_args(c);
+	CellArgs a = make_cell_args(c);
 	const unsigned block = 256;
 	const unsigned grid = (unsigned)((c->A + block - 1) / block);
 	const double S = (double)c->S, A = (double)c->A, w = (double)sizeof(T);
@@ -415,7 +249,7 @@ int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream)
 template <typename T>
 static int run_release(Context* c, uint64_t agent)
 {
-	CellArgs a = make_args(c);
+	CellArgs a = make_cell_args(c);
 	cudaEvent_t ev;
 	launch_begin(c, K_CELLS_RELEASE, (double)(c->S * 32), &ev);
 	cells_release_kernel<T><<<(unsigned)((c->S + 63) / 64), 64, 0, c->stream>>>(a, agent);

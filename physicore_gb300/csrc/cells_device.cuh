@@ -1,0 +1,216 @@
+// cells_device.cuh -- per-agent device code of the cell secretion/uptake step,
+// shared by the single-domain kernels (cells.cu) and the batched ones (batch.cu).
+//
+// Arithmetic follows openmp_solver/src/cell_solver.cpp:
+//   intermediates (51-77)   num = S*T*dt*Vc/Vv, den = (U+S)*dt*Vc/Vv, fac = N*dt/Vv
+//   ballot        (79-129)  one winner per voxel collects sum(num), 1+sum(den), sum(fac)
+//   result       (131-244)  D' = (D + sum num)/(1 + sum den) + sum fac by the winner;
+//                           internalized: fused I += Vv (D - D') when no voxel holds two
+//                           agents, otherwise I -= Vv (num - D' den + fac) per agent
+//   release      (274-289)  D += I F / Vv, I = 0
+#pragma once
+
+#include "pcg_internal.cuh"
+
+namespace pcg {
+namespace cellsdev {
+
+constexpr uint32_t kNoAgent = 0xffffffffu;
+constexpr int kSubBatch = 8; // substrates whose loads are issued together
+
+struct CellArgs
+{
+	int dims;
+	uint64_t A, S;
+	uint64_t n[3];
+	double bbmin[3];
+	double voxel[3];
+	uint64_t pitch;
+	double Vv, dt;
+	const double *pos, *sec, *sat, *upt, *net, *vol, *frac;
+	const uint8_t* active;
+	double* internal;
+	uint32_t* vox;
+	uint32_t* foff;
+	void *num, *den, *fac, *rnum, *rden, *rfac;
+	uint32_t* owner;
+	uint32_t* counts;
+	uint32_t* flags; // [0] conflict
+	uint32_t* err;
+	void* field;
+	int internalized;
+};
+
+// Cell arguments of a context's own buffers (cells.cu).
+CellArgs make_cell_args(const Context* c);
+
+// cartesian_mesh::voxel_position (mesh.cpp:37-61) in FP64; false when outside the grid.
+__device__ __forceinline__ bool locate(const CellArgs& a, uint64_t i, uint64_t idx[3])
+{
+	idx[0] = idx[1] = idx[2] = 0;
+	for (int d = 0; d < a.dims; d++)
+	{
+		const double q = (a.pos[i * a.dims + d] - a.bbmin[d]) / a.voxel[d];
+		if (!(q >= 0.0) || q >= (double)a.n[d])
+			return false;
+		idx[d] = (uint64_t)q;
+	}
+	return true;
+}
+
+// compute_intermediates + clear_ballots (cell_solver.cpp:22-77) for agent i < A.
+template <typename T>
+__device__ __forceinline__ void agent_locate(const CellArgs& a, uint64_t i)
+{
+	uint64_t idx[3];
+	if (!a.active[i])
+	{
+		a.vox[i] = kNoAgent;
+		return;
+	}
+	if (!locate(a, i, idx))
+	{
+		atomicOr(a.err, DEV_ERR_AGENT_OUTSIDE);
+		a.vox[i] = kNoAgent;
+		return;
+	}
+	const uint32_t v = (uint32_t)(idx[0] + a.n[0] * (idx[1] + a.n[1] * idx[2]));
+	a.vox[i] = v;
+	a.foff[i] = (uint32_t)((idx[2] * a.n[1] + idx[1]) * a.pitch + idx[0] * a.S);
+	a.owner[v] = kNoAgent;
+	T* num = static_cast<T*>(a.num);
+	T* den = static_cast<T*>(a.den);
+	T* fac = static_cast<T*>(a.fac);
+	T* rnum = static_cast<T*>(a.rnum);
+	T* rden = static_cast<T*>(a.rden);
+	T* rfac = static_cast<T*>(a.rfac);
+	const double vol = a.vol[i];
+	for (uint64_t s = 0; s < a.S; s++)
+	{
+		const uint64_t k = i * a.S + s;
+		num[k] = (T)(a.sec[k] * a.sat[k] * a.dt * vol / a.Vv);
+		den[k] = (T)((a.upt[k] + a.sec[k]) * a.dt * vol / a.Vv);
+		fac[k] = (T)(a.net[k] * a.dt / a.Vv);
+		rnum[k] = T(0);
+		rden[k] = T(0);
+		rfac[k] = T(0);
+	}
+}
+
+// Ballot of one warp (cell_solver.cpp:79-101 with a canonical winner).  `key`
+// must be unique per voxel across everything the warp holds (kNoAgent for none);
+// the lanes of a warp hold ascending agent indices of one domain per group.
+__device__ __forceinline__ void warp_ballot(const CellArgs* a, uint64_t i, uint32_t v, uint32_t key)
+{
+	const uint32_t group = __match_any_sync(0xffffffffu, key);
+	if (key == kNoAgent)
+		return;
+	if ((threadIdx.x & 31) == __ffs(group) - 1)
+	{
+		atomicMin(a->owner + v, (uint32_t)i); // the leader holds the group's lowest index
+		atomicAdd(a->counts + v, (uint32_t)__popc(group));
+	}
+}
+
+// Sums into the winner's row (cell_solver.cpp:102-127); returns true when agent i
+// is not its voxel's winner (a ballot conflict).
+template <typename T>
+__device__ __forceinline__ bool agent_reduce(const CellArgs& a, uint64_t i, uint32_t v)
+{
+	const uint32_t w = a.owner[v];
+	const bool conflict = w != (uint32_t)i;
+	const T* num = static_cast<const T*>(a.num);
+	const T* den = static_cast<const T*>(a.den);
+	const T* fac = static_cast<const T*>(a.fac);
+	T* rnum = static_cast<T*>(a.rnum);
+	T* rden = static_cast<T*>(a.rden);
+	T* rfac = static_cast<T*>(a.rfac);
+	for (uint64_t s = 0; s < a.S; s++)
+	{
+		const uint64_t k = i * a.S + s;
+		const uint64_t kw = (uint64_t)w * a.S + s;
+		atomicAdd(rnum + kw, num[k]);
+		atomicAdd(rden + kw, conflict ? den[k] : den[k] + T(1));
+		atomicAdd(rfac + kw, fac[k]);
+	}
+	return conflict;
+}
+
+// compute_result (cell_solver.cpp:187-227) for agent i.  All loads of a batch of
+// substrates are issued before any store, so an agent's accesses overlap.
+template <typename T>
+__device__ __forceinline__ void agent_apply(const CellArgs& a, uint64_t i)
+{
+	const uint32_t key = a.vox[i];
+	if (key == kNoAgent)
+		return;
+	const uint32_t off = a.foff[i];
+	const bool fused = a.internalized && *(volatile uint32_t*)a.flags == 0;
+	if (!fused && a.owner[key] != (uint32_t)i)
+		return;
+	T* __restrict__ D = static_cast<T*>(a.field) + off;
+	const T* __restrict__ rn = static_cast<const T*>(a.rnum) + i * a.S;
+	const T* __restrict__ rd = static_cast<const T*>(a.rden) + i * a.S;
+	const T* __restrict__ rf = static_cast<const T*>(a.rfac) + i * a.S;
+	double* __restrict__ I = a.internal + i * a.S;
+	for (uint32_t s0 = 0; s0 < a.S; s0 += kSubBatch)
+	{
+		T dv[kSubBatch], n_[kSubBatch], d_[kSubBatch], f_[kSubBatch];
+		double iv[kSubBatch];
+#pragma unroll
+		for (int q = 0; q < kSubBatch; q++)
+			if (s0 + q < a.S)
+			{
+				dv[q] = D[s0 + q];
+				n_[q] = rn[s0 + q];
+				d_[q] = rd[s0 + q];
+				f_[q] = rf[s0 + q];
+				if (fused)
+					iv[q] = I[s0 + q];
+			}
+#pragma unroll
+		for (int q = 0; q < kSubBatch; q++)
+			if (s0 + q < a.S)
+			{
+				const T next = (dv[q] + n_[q]) / d_[q] + f_[q];
+				D[s0 + q] = next;
+				if (fused)
+					I[s0 + q] = iv[q] + a.Vv * ((double)dv[q] - (double)next);
+			}
+	}
+}
+
+// compute_internalized after a conflict (cell_solver.cpp:229-243) for agent i.
+template <typename T>
+__device__ __forceinline__ void agent_internalize(const CellArgs& a, uint64_t i)
+{
+	if (*(volatile uint32_t*)a.flags == 0 || a.vox[i] == kNoAgent)
+		return;
+	const T* __restrict__ D = static_cast<const T*>(a.field) + a.foff[i];
+	const T* __restrict__ nu = static_cast<const T*>(a.num) + i * a.S;
+	const T* __restrict__ de = static_cast<const T*>(a.den) + i * a.S;
+	const T* __restrict__ fa = static_cast<const T*>(a.fac) + i * a.S;
+	double* __restrict__ I = a.internal + i * a.S;
+	for (uint32_t s0 = 0; s0 < a.S; s0 += kSubBatch)
+	{
+		T dv[kSubBatch], n_[kSubBatch], d_[kSubBatch], f_[kSubBatch];
+		double iv[kSubBatch];
+#pragma unroll
+		for (int q = 0; q < kSubBatch; q++)
+			if (s0 + q < a.S)
+			{
+				dv[q] = D[s0 + q];
+				n_[q] = nu[s0 + q];
+				d_[q] = de[s0 + q];
+				f_[q] = fa[s0 + q];
+				iv[q] = I[s0 + q];
+			}
+#pragma unroll
+		for (int q = 0; q < kSubBatch; q++)
+			if (s0 + q < a.S)
+				I[s0 + q] = iv[q] - a.Vv * ((double)n_[q] - (double)dv[q] * (double)d_[q] + (double)f_[q]);
+	}
+}
+
+} // namespace cellsdev
+} // namespace pcg

@@ -1,0 +1,139 @@
+// field_device.cuh -- per-item device code of the Dirichlet and bulk phases,
+// shared by the single-domain kernels (field_ops.cu) and the batched ones (batch.cu).
+//
+// Dirichlet (openmp_solver/src/dirichlet_solver.cpp:22-93): the reference writes
+// the x-min, x-max, y-min, y-max, z-min, z-max faces one after another (a later
+// face wins on shared edges) and then the interior voxels.  A face item is one
+// (face voxel, substrate); it applies the face of highest precedence whose
+// condition holds, so edges resolve exactly as the sequential order does.
+//
+// Bulk (openmp_solver/src/bulk_solver.cpp:12-49): D = (D + dt*S*T)/(1 + dt*(U+S)).
+#pragma once
+
+#include "pcg_internal.cuh"
+
+namespace pcg {
+
+struct FaceArgs
+{
+	void* field;
+	const void* values; // real [6*S]: face f = axis*2 + side
+	const uint8_t* conds;
+	uint32_t face_mask; // bit f set when face f exists
+	uint64_t S, nx, ny, nz, pitch;
+	uint64_t cnt_x, cnt_y, cnt_z; // voxels on each pair of faces
+	uint64_t total;               // face voxels (all pairs)
+};
+
+// Fills the face geometry of a mesh from its per-face presence.
+inline FaceArgs make_face_args(const Context* c)
+{
+	FaceArgs a {};
+	uint32_t mask = 0;
+	for (int axis = 0; axis < c->dims; axis++)
+		for (int side = 0; side < 2; side++)
+			if (c->face_on[axis][side])
+				mask |= 1u << (axis * 2 + side);
+	const uint64_t nx = c->n[0], ny = c->n[1], nz = c->n[2];
+	a.field = c->field.ptr;
+	a.values = c->face_values.ptr;
+	a.conds = static_cast<const uint8_t*>(c->face_conds.ptr);
+	a.face_mask = mask;
+	a.S = c->S;
+	a.nx = nx, a.ny = ny, a.nz = nz;
+	a.pitch = c->pitch;
+	a.cnt_x = (mask & 0x3) ? 2 * ny * nz : 0;
+	a.cnt_y = (mask & 0xc) ? 2 * nx * nz : 0;
+	a.cnt_z = (mask & 0x30) ? 2 * nx * ny : 0;
+	a.total = a.cnt_x + a.cnt_y + a.cnt_z;
+	return a;
+}
+
+#ifdef __CUDACC__
+namespace fielddev {
+
+// Face item idx < total*S.
+template <typename T>
+__device__ __forceinline__ void face_item(const FaceArgs& a, uint64_t idx)
+{
+	const T* vals = static_cast<const T*>(a.values);
+	T* f = static_cast<T*>(a.field);
+	const uint64_t s = idx % a.S;
+	uint64_t k = idx / a.S;
+	uint64_t x, y, z;
+	if (k < a.cnt_x)
+	{ // x faces: k -> (side, y, z)
+		const uint64_t per = a.ny * a.nz;
+		x = (k / per) ? a.nx - 1 : 0;
+		y = (k % per) % a.ny;
+		z = (k % per) / a.ny;
+	}
+	else if ((k -= a.cnt_x) < a.cnt_y)
+	{
+		const uint64_t per = a.nx * a.nz;
+		y = (k / per) ? a.ny - 1 : 0;
+		x = (k % per) % a.nx;
+		z = (k % per) / a.nx;
+	}
+	else
+	{
+		k -= a.cnt_y;
+		const uint64_t per = a.nx * a.ny;
+		z = (k / per) ? a.nz - 1 : 0;
+		x = (k % per) % a.nx;
+		y = (k % per) / a.nx;
+	}
+	// precedence: the reference applies faces 0..5 in order, so scan 5..0
+	const uint64_t coord[3] = { x, y, z };
+	const uint64_t last[3] = { a.nx - 1, a.ny - 1, a.nz - 1 };
+	for (int fi = 5; fi >= 0; fi--)
+	{
+		if (!(a.face_mask & (1u << fi)))
+			continue;
+		const int axis = fi >> 1, side = fi & 1;
+		if (coord[axis] != (side ? last[axis] : 0))
+			continue;
+		if (a.conds[fi * a.S + s])
+		{
+			f[(z * a.ny + y) * a.pitch + x * a.S + s] = vals[fi * a.S + s];
+			break;
+		}
+	}
+}
+
+// One row of the bulk update by the 32 lanes of a warp; a lane walks the row's
+// (x,s) run with its substrate index advanced incrementally.
+template <typename T, bool PER_VOXEL>
+__device__ __forceinline__ void bulk_row(T* field, const T* supply, const T* uptake, const T* target,
+										 uint64_t row_len, uint64_t pitch, uint64_t r, uint32_t S, T dt, int lane)
+{
+	const uint32_t s_step = 32 % S;
+	T* row = field + r * pitch;
+	uint32_t s = (uint32_t)lane % S;
+	for (uint64_t k = lane; k < row_len; k += 32)
+	{
+		T Sr, U, Tt;
+		if (PER_VOXEL)
+		{
+			const uint64_t o = r * pitch + k;
+			Sr = supply[o];
+			U = uptake[o];
+			Tt = target[o];
+		}
+		else
+		{
+			Sr = supply[s];
+			U = uptake[s];
+			Tt = target[s];
+		}
+		row[k] = (row[k] + dt * Sr * Tt) / (T(1) + dt * (U + Sr));
+		s += s_step;
+		if (s >= S)
+			s -= S;
+	}
+}
+
+} // namespace fielddev
+#endif
+
+} // namespace pcg

@@ -1,81 +1,20 @@
 // field_ops.cu -- Dirichlet, bulk source/sink, mass and layout kernels.
 //
-// Dirichlet (openmp_solver/src/dirichlet_solver.cpp:22-93): the reference writes
-// the x-min, x-max, y-min, y-max, z-min, z-max faces one after another (a later
-// face wins on shared edges) and then the interior voxels.  Here one launch covers
-// all six faces: a thread owns one (face voxel, substrate) and applies the face
-// with the highest precedence whose condition holds, so edges resolve exactly as
-// the sequential order does; a second launch writes the interior list.
-//
-// Bulk (openmp_solver/src/bulk_solver.cpp:12-49): D = (D + dt*S*T)/(1 + dt*(U+S))
-// with S, U, T read from device tables instead of three virtual calls per element.
-#include "pcg_internal.cuh"
+// Dirichlet faces and interior (openmp_solver/src/dirichlet_solver.cpp:22-93) and
+// bulk (openmp_solver/src/bulk_solver.cpp:12-49): per-item bodies live in
+// field_device.cuh; one launch covers all six faces, a second the interior list.
+#include "field_device.cuh"
 
 namespace pcg {
 
 namespace {
 
-struct FaceArgs
-{
-	void* field;
-	const void* values; // real [6*S]: face f = axis*2 + side
-	const uint8_t* conds;
-	uint32_t face_mask; // bit f set when face f exists
-	uint64_t S, nx, ny, nz, pitch;
-	uint64_t cnt_x, cnt_y, cnt_z; // voxels on each pair of faces
-	uint64_t total;               // face voxels (all pairs)
-};
-
 template <typename T>
 __global__ void dirichlet_faces_kernel(FaceArgs a)
 {
-	const T* vals = static_cast<const T*>(a.values);
-	T* f = static_cast<T*>(a.field);
 	for (uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; idx < a.total * a.S;
 		 idx += (uint64_t)gridDim.x * blockDim.x)
-	{
-		const uint64_t s = idx % a.S;
-		uint64_t k = idx / a.S;
-		uint64_t x, y, z;
-		if (k < a.cnt_x)
-		{ // x faces: k -> (side, y, z)
-			const uint64_t per = a.ny * a.nz;
-			x = (k / per) ? a.nx - 1 : 0;
-			y = (k % per) % a.ny;
-			z = (k % per) / a.ny;
-		}
-		else if ((k -= a.cnt_x) < a.cnt_y)
-		{
-			const uint64_t per = a.nx * a.nz;
-			y = (k / per) ? a.ny - 1 : 0;
-			x = (k % per) % a.nx;
-			z = (k % per) / a.nx;
-		}
-		else
-		{
-			k -= a.cnt_y;
-			const uint64_t per = a.nx * a.ny;
-			z = (k / per) ? a.nz - 1 : 0;
-			x = (k % per) % a.nx;
-			y = (k % per) / a.nx;
-		}
-		// precedence: the reference applies faces 0..5 in order, so scan 5..0
-		const uint64_t coord[3] = { x, y, z };
-		const uint64_t last[3] = { a.nx - 1, a.ny - 1, a.nz - 1 };
-		for (int fi = 5; fi >= 0; fi--)
-		{
-			if (!(a.face_mask & (1u << fi)))
-				continue;
-			const int axis = fi >> 1, side = fi & 1;
-			if (coord[axis] != (side ? last[axis] : 0))
-				continue;
-			if (a.conds[fi * a.S + s])
-			{
-				f[(z * a.ny + y) * a.pitch + x * a.S + s] = vals[fi * a.S + s];
-				break;
-			}
-		}
-	}
+		fielddev::face_item<T>(a, idx);
 }
 
 template <typename T>
@@ -90,8 +29,7 @@ __global__ void dirichlet_interior_kernel(T* field, const uint64_t* offsets, con
 	}
 }
 
-// A warp per row; each lane walks the row's (x,s) run with its substrate index
-// advanced incrementally.
+// A warp per row.
 template <typename T, bool PER_VOXEL>
 __global__ void bulk_kernel(T* field, const T* supply, const T* uptake, const T* target, uint64_t row_len,
 							uint64_t pitch, uint64_t rows, uint32_t S, T dt)
@@ -99,33 +37,8 @@ __global__ void bulk_kernel(T* field, const T* supply, const T* uptake, const T*
 	const int lane = threadIdx.x & 31;
 	const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
 	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-	const uint32_t s_step = 32 % S;
 	for (uint64_t r = warp; r < rows; r += nwarps)
-	{
-		T* row = field + r * pitch;
-		uint32_t s = (uint32_t)lane % S;
-		for (uint64_t k = lane; k < row_len; k += 32)
-		{
-			T Sr, U, Tt;
-			if (PER_VOXEL)
-			{
-				const uint64_t o = r * pitch + k;
-				Sr = supply[o];
-				U = uptake[o];
-				Tt = target[o];
-			}
-			else
-			{
-				Sr = supply[s];
-				U = uptake[s];
-				Tt = target[s];
-			}
-			row[k] = (row[k] + dt * Sr * Tt) / (T(1) + dt * (U + Sr));
-			s += s_step;
-			if (s >= S)
-				s -= S;
-		}
-	}
+		fielddev::bulk_row<T, PER_VOXEL>(field, supply, uptake, target, row_len, pitch, r, S, dt, lane);
 }
 
 // FP64 mass per substrate: a warp per row, one substrate at a time.
@@ -224,26 +137,9 @@ unsigned grid_for(const Context* c, uint64_t work, unsigned block)
 template <typename T>
 static int run_dirichlet(Context* c)
 {
-	const uint64_t nx = c->n[0], ny = c->n[1], nz = c->n[2];
-	uint32_t mask = 0;
-	for (int axis = 0; axis < c->dims; axis++)
-		for (int side = 0; side < 2; side++)
-			if (c->face_on[axis][side])
-				mask |= 1u << (axis * 2 + side);
-	if (mask)
+	const FaceArgs a = make_face_args(c);
+	if (a.face_mask)
 	{
-		FaceArgs a {};
-		a.field = c->field.ptr;
-		a.values = c->face_values.ptr;
-		a.conds = static_cast<const uint8_t*>(c->face_conds.ptr);
-		a.face_mask = mask;
-		a.S = c->S;
-		a.nx = nx, a.ny = ny, a.nz = nz;
-		a.pitch = c->pitch;
-		a.cnt_x = (mask & 0x3) ? 2 * ny * nz : 0;
-		a.cnt_y = (mask & 0xc) ? 2 * nx * nz : 0;
-		a.cnt_z = (mask & 0x30) ? 2 * nx * ny : 0;
-		a.total = a.cnt_x + a.cnt_y + a.cnt_z;
 		cudaEvent_t ev;
 		launch_begin(c, K_DIRICHLET_FACES, (double)(a.total * c->S * sizeof(T)), &ev);
 		dirichlet_faces_kernel<T><<<grid_for(c, a.total * c->S, 256), 256, 0, c->stream>>>(a);

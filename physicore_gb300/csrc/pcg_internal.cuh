@@ -60,6 +60,7 @@ enum KernelId : int
 	K_CELLS_RELEASE,
 	K_MASS,
 	K_LAYOUT,
+	K_CELLS_CLEAR,
 	K_COUNT
 };
 
@@ -156,6 +157,9 @@ struct Context
 	// device state
 	bool initialized = false;
 	bool recompute_cells = true;
+	// bumped by every call that may reallocate a device buffer or change a
+	// parameter; batches compare it with the value they captured
+	uint64_t generation = 0;
 	DeviceBuffer field;
 	DeviceBuffer coef[3];
 	// TMA tensor maps of the field for the y and z sweeps: the field as a 3-D tensor
@@ -256,6 +260,27 @@ struct CellStepBuffers
 };
 int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream);
 
+// context lifecycle (capi.cu)
+int initialize_context(Context* c);  // allocates and uploads on first use
+int check_context(Context* c);       // synchronises and reports the device error word
+std::string device_error_text(uint32_t word);
+
+struct DeviceGuard
+{
+	int prev = -1;
+	explicit DeviceGuard(int dev)
+	{
+		cudaGetDevice(&prev);
+		if (prev != dev)
+			cudaSetDevice(dev);
+	}
+	~DeviceGuard()
+	{
+		if (prev >= 0)
+			cudaSetDevice(prev);
+	}
+};
+
 // geometry helpers shared by the launchers and the feasibility checks
 uint64_t coef_table_len(uint64_t n, uint64_t S, size_t wsize);
 uint64_t coef_row_pitch(uint64_t n);
@@ -263,8 +288,16 @@ uint64_t sweep_x_smem_pitch(uint64_t row_len, uint64_t S, size_t wsize);
 uint64_t x_threads_per_row(uint64_t S, size_t wsize);
 uint64_t sweep_smem_bytes(const Context* c, int axis);
 int prepare_sweep_maps(Context* c);
+// y/z chunk geometry: points per TMA box and boxes per line
+void box_geometry(uint64_t n, uint32_t& box_rows, uint32_t& boxes);
+// TMA map of the field as the tensor (x*S+s, y, z) with boxes of 32 x box_rows
+// points along `axis` (1 or 2)
+int encode_field_map(const Context* c, int axis, uint32_t box_rows, CUtensorMap* out);
 
 } // namespace pcg
+
+struct pcg_context : pcg::Context
+{};
 
 // ------------------------------------------------------------------ device helpers
 

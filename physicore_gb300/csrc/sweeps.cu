@@ -31,45 +31,13 @@
 //    each; rows are TPR (mod 8) chunks apart so quarter-warps hit distinct banks.
 //  * Every wait is bounded; a timeout sets a device error bit instead of trapping.
 #include "pcg_internal.cuh"
+#include "sweep_solvers.cuh"
 
 namespace pcg {
 
 namespace {
 
-constexpr int kBlock = 8;      // recurrence steps per pipelined block (y/z, one point per step)
-constexpr int kChunkBlock = 4; // 16-byte chunks per pipelined block (x, several points per chunk)
-
-template <typename T>
-struct Vec16;
-template <>
-struct Vec16<float>
-{
-	using type = float4;
-	static constexpr int N = 4;
-};
-template <>
-struct Vec16<double>
-{
-	using type = double2;
-	static constexpr int N = 2;
-};
-
-template <typename V, typename T>
-__device__ __forceinline__ T vget(const V& v, int u)
-{
-	return reinterpret_cast<const T*>(&v)[u];
-}
-template <typename V, typename T>
-__device__ __forceinline__ void vset(V& v, int u, T x)
-{
-	reinterpret_cast<T*>(&v)[u] = x;
-}
-
-template <typename V>
-__device__ __forceinline__ V ldg_vec(const V* p)
-{
-	return __ldg(p);
-}
+using namespace solvers;
 
 // ------------------------------------------------------------------ y / z
 
@@ -314,296 +282,6 @@ __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __g
 
 // ------------------------------------------------------------------ x
 
-// S*sizeof(T) a multiple of 16 bytes: thread h of a row's TPR threads owns chunk
-// slot h of every x position (VN substrates, VN independent recurrences).
-template <typename T, int TPR>
-__device__ __forceinline__ void solve_row_chunks(T* row, const T* __restrict__ cB, const T* __restrict__ cE,
-												 const T* __restrict__ cC, uint32_t n, int h)
-{
-	using V = typename Vec16<T>::type;
-	constexpr int VN = Vec16<T>::N, P = kChunkBlock;
-	V* __restrict__ vrow = reinterpret_cast<V*>(row) + h;
-	const V* vE = reinterpret_cast<const V*>(cE) + h;
-	const V* vB = reinterpret_cast<const V*>(cB) + h;
-	const uint32_t nb = n / P;
-	T d[VN], c[VN];
-#pragma unroll
-	for (int u = 0; u < VN; u++)
-	{
-		d[u] = T(0);
-		c[u] = __ldg(cC + h * VN + u);
-	}
-	auto step_fwd = [&](V& v, const V& e) {
-#pragma unroll
-		for (int u = 0; u < VN; u++)
-		{
-			d[u] = dev::fmadd(vget<V, T>(e, u), d[u], vget<V, T>(v, u));
-			vset<V, T>(v, u, d[u]);
-		}
-	};
-	auto step_bwd = [&](V& v, const V& b) {
-#pragma unroll
-		for (int u = 0; u < VN; u++)
-		{
-			d[u] = dev::fmadd(c[u], d[u], vget<V, T>(v, u)) * vget<V, T>(b, u);
-			vset<V, T>(v, u, d[u]);
-		}
-	};
-	{
-		V x[P], xn[P], e[P], en[P];
-		if (nb)
-#pragma unroll
-			for (int q = 0; q < P; q++)
-			{
-				x[q] = vrow[q * TPR];
-				e[q] = ldg_vec(vE + q * TPR);
-			}
-		for (uint32_t b = 0; b < nb; b++)
-		{
-			const uint32_t i0 = b * P;
-			if (b + 1 < nb)
-#pragma unroll
-				for (int q = 0; q < P; q++)
-				{
-					xn[q] = vrow[(i0 + P + q) * TPR];
-					en[q] = ldg_vec(vE + (i0 + P + q) * TPR);
-				}
-#pragma unroll
-			for (int q = 0; q < P; q++)
-			{
-				step_fwd(x[q], e[q]);
-				vrow[(i0 + q) * TPR] = x[q];
-			}
-#pragma unroll
-			for (int q = 0; q < P; q++)
-			{
-				x[q] = xn[q];
-				e[q] = en[q];
-			}
-		}
-		for (uint32_t i = nb * P; i < n; i++)
-		{
-			V v = vrow[i * TPR];
-			step_fwd(v, ldg_vec(vE + i * TPR));
-			vrow[i * TPR] = v;
-		}
-	}
-#pragma unroll
-	for (int u = 0; u < VN; u++)
-		d[u] = T(0);
-	for (int i = (int)n - 1; i >= (int)(nb * P); i--)
-	{
-		V v = vrow[i * TPR];
-		step_bwd(v, ldg_vec(vB + i * TPR));
-		vrow[i * TPR] = v;
-	}
-	{
-		V x[P], xn[P], bb[P], bn[P];
-		if (nb)
-#pragma unroll
-			for (int q = 0; q < P; q++)
-			{
-				x[q] = vrow[((nb - 1) * P + q) * TPR];
-				bb[q] = ldg_vec(vB + ((nb - 1) * P + q) * TPR);
-			}
-		for (int b = (int)nb - 1; b >= 0; b--)
-		{
-			const uint32_t i0 = (uint32_t)b * P;
-			if (b > 0)
-#pragma unroll
-				for (int q = 0; q < P; q++)
-				{
-					xn[q] = vrow[(i0 - P + q) * TPR];
-					bn[q] = ldg_vec(vB + (i0 - P + q) * TPR);
-				}
-#pragma unroll
-			for (int q = P - 1; q >= 0; q--)
-			{
-				step_bwd(x[q], bb[q]);
-				vrow[(i0 + q) * TPR] = x[q];
-			}
-#pragma unroll
-			for (int q = 0; q < P; q++)
-			{
-				x[q] = xn[q];
-				bb[q] = bn[q];
-			}
-		}
-	}
-}
-
-// ST substrates (1..8) not filling whole chunks: the row is a stream of chunks,
-// element k of substrate k % ST.  Blocks of NB chunks hold whole groups of
-// lcm(ST, VN) elements, so each element's substrate is a compile-time index.
-template <typename T, int ST>
-__device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, const T* __restrict__ cE,
-											  const T* __restrict__ cC, uint32_t n)
-{
-	using V = typename Vec16<T>::type;
-	constexpr int VN = Vec16<T>::N;
-	constexpr int GE = group_elems(ST, VN);
-	constexpr int U = GE / VN;
-	constexpr int NB = U * ((kChunkBlock + U - 1) / U); // chunks per block
-	const uint32_t total = n * ST;
-	const uint32_t nchunks = (total + GE - 1) / GE * U; // whole groups (tail elements predicated)
-	V* __restrict__ vrow = reinterpret_cast<V*>(row);
-	const V* vE = reinterpret_cast<const V*>(cE);
-	const V* vB = reinterpret_cast<const V*>(cB);
-	T d[ST], c[ST];
-#pragma unroll
-	for (int s = 0; s < ST; s++)
-	{
-		d[s] = T(0);
-		c[s] = __ldg(cC + s);
-	}
-	// In a block or group starting at chunk k0 (k0*VN a multiple of ST), element
-	// k0*VN + q*VN + u has substrate (q*VN + u) % ST.
-	auto fwd_chunk = [&](V& v, const V& e, int q, uint32_t k) {
-#pragma unroll
-		for (int u = 0; u < VN; u++)
-		{
-			const int s = (q * VN + u) % ST;
-			if (k * VN + u < total)
-			{
-				d[s] = dev::fmadd(vget<V, T>(e, u), d[s], vget<V, T>(v, u));
-				vset<V, T>(v, u, d[s]);
-			}
-		}
-	};
-	auto bwd_chunk = [&](V& v, const V& b, int q, uint32_t k) {
-#pragma unroll
-		for (int u = VN - 1; u >= 0; u--)
-		{
-			const int s = (q * VN + u) % ST;
-			if (k * VN + u < total)
-			{
-				d[s] = dev::fmadd(c[s], d[s], vget<V, T>(v, u)) * vget<V, T>(b, u);
-				vset<V, T>(v, u, d[s]);
-			}
-		}
-	};
-	const uint32_t nb = nchunks / NB;
-	{
-		V x[NB], xn[NB], e[NB], en[NB];
-		if (nb)
-#pragma unroll
-			for (int q = 0; q < NB; q++)
-			{
-				x[q] = vrow[q];
-				e[q] = ldg_vec(vE + q);
-			}
-		for (uint32_t b = 0; b < nb; b++)
-		{
-			const uint32_t k0 = b * NB;
-			if (b + 1 < nb)
-#pragma unroll
-				for (int q = 0; q < NB; q++)
-				{
-					xn[q] = vrow[k0 + NB + q];
-					en[q] = ldg_vec(vE + k0 + NB + q);
-				}
-#pragma unroll
-			for (int q = 0; q < NB; q++)
-			{
-				fwd_chunk(x[q], e[q], q, k0 + q);
-				vrow[k0 + q] = x[q];
-			}
-#pragma unroll
-			for (int q = 0; q < NB; q++)
-			{
-				x[q] = xn[q];
-				e[q] = en[q];
-			}
-		}
-		// remaining whole groups (fewer than NB chunks)
-		for (uint32_t k0 = nb * NB; k0 < nchunks; k0 += U)
-		{
-#pragma unroll
-			for (int q = 0; q < U; q++)
-			{
-				V v = vrow[k0 + q];
-				fwd_chunk(v, ldg_vec(vE + k0 + q), q, k0 + q);
-				vrow[k0 + q] = v;
-			}
-		}
-	}
-#pragma unroll
-	for (int s = 0; s < ST; s++)
-		d[s] = T(0);
-	for (int k0 = (int)nchunks - U; k0 >= (int)(nb * NB); k0 -= U)
-	{
-#pragma unroll
-		for (int q = U - 1; q >= 0; q--)
-		{
-			V v = vrow[k0 + q];
-			bwd_chunk(v, ldg_vec(vB + k0 + q), q, (uint32_t)(k0 + q));
-			vrow[k0 + q] = v;
-		}
-	}
-	{
-		V x[NB], xn[NB], bb[NB], bn[NB];
-		if (nb)
-#pragma unroll
-			for (int q = 0; q < NB; q++)
-			{
-				x[q] = vrow[(nb - 1) * NB + q];
-				bb[q] = ldg_vec(vB + (nb - 1) * NB + q);
-			}
-		for (int b = (int)nb - 1; b >= 0; b--)
-		{
-			const uint32_t k0 = (uint32_t)b * NB;
-			if (b > 0)
-#pragma unroll
-				for (int q = 0; q < NB; q++)
-				{
-					xn[q] = vrow[k0 - NB + q];
-					bn[q] = ldg_vec(vB + k0 - NB + q);
-				}
-#pragma unroll
-			for (int q = NB - 1; q >= 0; q--)
-			{
-				bwd_chunk(x[q], bb[q], q, k0 + q);
-				vrow[k0 + q] = x[q];
-			}
-#pragma unroll
-			for (int q = 0; q < NB; q++)
-			{
-				x[q] = xn[q];
-				bb[q] = bn[q];
-			}
-		}
-	}
-}
-
-// Any S: one recurrence at a time, scalar shared-memory accesses.
-template <typename T>
-__device__ __forceinline__ void solve_row_generic(T* row, const T* cB, const T* cE, const T* cC, uint32_t n,
-												  uint32_t S)
-{
-	for (uint32_t s = 0; s < S; s++)
-	{
-		T d = T(0);
-		for (uint32_t i = 0; i < n; i++)
-		{
-			d = dev::fmadd(__ldg(cE + i * S + s), d, row[i * S + s]);
-			row[i * S + s] = d;
-		}
-		const T c = __ldg(cC + s);
-		d = T(0);
-		for (int i = (int)n - 1; i >= 0; i--)
-		{
-			d = dev::fmadd(c, d, row[i * S + s]) * __ldg(cB + i * S + s);
-			row[i * S + s] = d;
-		}
-	}
-}
-
-template <typename T, int ST>
-constexpr int x_tpr()
-{
-	return (ST > 0 && ST <= 8 && (ST * (int)sizeof(T)) % 16 == 0) ? ST * (int)sizeof(T) / 16 : 1;
-}
-
 // A tile is rows_per_tile consecutive rows; the CTA has rows_per_tile * TPR threads (<= 32).
 template <typename T, int ST>
 __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
@@ -664,8 +342,6 @@ __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 	}
 	dev::bulk_wait_all();
 }
-
-void box_geometry(uint64_t n, uint32_t& box_rows, uint32_t& boxes);
 
 struct Plan
 {
@@ -802,6 +478,29 @@ int run_sweep_yz(Context* c, int axis)
 	return PCG_OK;
 }
 
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+								   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+								   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+	static EncodeTiledFn fn = nullptr;
+	if (!fn)
+	{
+		void* p = nullptr;
+		cudaDriverEntryPointQueryResult q {};
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+				cudaSuccess &&
+			q == cudaDriverEntryPointSuccess)
+			fn = reinterpret_cast<EncodeTiledFn>(p);
+	}
+	return fn;
+}
+
+} // namespace
+
+// -------------------------------------------------------------------- host side
+
 // Chunk geometry of the y/z zipper: R points per chunk (a multiple of the solver
 // block, at most 256, the TMA box limit).  The first size in order of preference
 // (about 32 points: enough chunks to pipeline, few TMA operations) that pads the
@@ -829,28 +528,6 @@ void box_geometry(uint64_t n, uint32_t& box_rows, uint32_t& boxes)
 	}
 }
 
-using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-								   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-								   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn()
-{
-	static EncodeTiledFn fn = nullptr;
-	if (!fn)
-	{
-		void* p = nullptr;
-		cudaDriverEntryPointQueryResult q {};
-		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-				cudaSuccess &&
-			q == cudaDriverEntryPointSuccess)
-			fn = reinterpret_cast<EncodeTiledFn>(p);
-	}
-	return fn;
-}
-
-} // namespace
-
-// -------------------------------------------------------------------- host side
 
 uint64_t coef_table_len(uint64_t n, uint64_t S, size_t wsize)
 {
@@ -878,8 +555,7 @@ uint64_t sweep_x_smem_pitch(uint64_t row_len, uint64_t S, size_t wsize)
 	return chunks * vn;
 }
 
-// Encodes the TMA tensor maps of the y and z sweeps for the current field buffer.
-int prepare_sweep_maps(Context* c)
+int encode_field_map(const Context* c, int axis, uint32_t box_rows, CUtensorMap* out)
 {
 	EncodeTiledFn enc = encode_fn();
 	if (!enc)
@@ -888,16 +564,24 @@ int prepare_sweep_maps(Context* c)
 	const cuuint64_t strides[2] = { c->pitch * c->wsize, c->n[1] * c->pitch * c->wsize };
 	const cuuint32_t estr[3] = { 1, 1, 1 };
 	const CUtensorMapDataType dt = c->wsize == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+	const cuuint32_t box[3] = { (cuuint32_t)kLanes, axis == 1 ? box_rows : 1u, axis == 2 ? box_rows : 1u };
+	CUresult r = enc(out, dt, 3, c->field.ptr, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+					 CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+	if (r != CUDA_SUCCESS)
+		return fail(PCG_ERR_CUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r));
+	return PCG_OK;
+}
+
+// Encodes the TMA tensor maps of the y and z sweeps for the current field buffer.
+int prepare_sweep_maps(Context* c)
+{
 	for (int axis = 1; axis < c->dims; axis++)
 	{
 		uint32_t box_rows, boxes;
 		box_geometry(c->n[axis], box_rows, boxes);
-		const cuuint32_t box[3] = { (cuuint32_t)kLanes, axis == 1 ? box_rows : 1u, axis == 2 ? box_rows : 1u };
-		CUresult r = enc(&c->tmap[axis], dt, 3, c->field.ptr, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-						 CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-						 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-		if (r != CUDA_SUCCESS)
-			return fail(PCG_ERR_CUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r));
+		const int rc = encode_field_map(c, axis, box_rows, &c->tmap[axis]);
+		if (rc)
+			return rc;
 		c->tmap_box_rows[axis] = box_rows;
 		c->tmap_boxes[axis] = boxes;
 	}

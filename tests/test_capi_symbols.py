@@ -33,9 +33,8 @@ def test_library_exports_every_declared_symbol(pcg):
 
 def test_python_binding_covers_header(pcg):
     covered = set(pcg.SIGNATURES) | {"pcg_last_error"}
-    assert set(declared_symbols()) <= covered | {n for n in declared_symbols() if n.startswith("pcg_batch")} \
-        | {n for n in declared_symbols() if n.startswith("pcg_server")} | {n for n in declared_symbols()
-                                                                           if n.endswith("_noalloc")}
+    # the allocation-free entry point is bound where it is used (its own test)
+    assert set(declared_symbols()) <= covered | {n for n in declared_symbols() if n.endswith("_noalloc")}
 
 
 def test_create_without_gpu_fails_cleanly(pcg):
