@@ -289,9 +289,110 @@ def run_gb300(args, w):
                               "algorithmic_bytes_per_step": step_bytes},
             "kernels": kernels, "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e,
             "cpu_baseline": cpu}
+    if args.batch_domains > 0:
+        line["batched"] = run_batched(args, local, ClockSampler)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_batched(args, local, clock_sampler=None):
+    """The batched workload (256 uneven domains, FP32): the same contexts stepped one
+    after another on one stream (the plain path: pcg_solve per domain) and then
+    together through a batch (one launch per phase, CUDA-graph replay, autotuned)."""
+    import torch
+
+    import physicore_gb300 as pcg
+    from physicore_gb300 import workloads as W
+    t0 = time.perf_counter()
+    solvers = [W.apply(pcg.Solver(pcg.FP32, device=local), p)
+               for p in W.batched_uneven(count=args.batch_domains)]
+    setup_s = time.perf_counter() - t0
+    vss_step = sum(s.voxels * s.S for s in solvers)
+    steps, warm = args.batch_steps, max(3, args.warmup)
+
+    # one stream owned here (it must outlive every context that uses it)
+    cs = torch.cuda.Stream()
+    for s in solvers:
+        s.set_stream(cs.cuda_stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(warm):
+        for s in solvers:
+            s.solve(1)
+    solvers[0].synchronize()
+    l0 = sum(s.launch_count() for s in solvers)
+    ev0.record(cs)
+    for _ in range(steps):
+        for s in solvers:
+            s.solve(1)
+    ev1.record(cs)
+    ev1.synchronize()
+    plain_ms = ev0.elapsed_time(ev1)
+    plain_launches = sum(s.launch_count() for s in solvers) - l0
+
+    b = pcg.Batch(solvers)
+    t0 = time.perf_counter()
+    b.autotune()
+    b.synchronize()
+    tune_s = time.perf_counter() - t0
+    bs = torch.cuda.ExternalStream(b.stream())
+    for _ in range(warm):
+        b.solve(1)
+    b.synchronize()
+    b.reset_kernel_stats()
+    sampler = clock_sampler(local) if clock_sampler else None
+    if sampler:
+        sampler.__enter__()
+    ev0.record(bs)
+    b.solve(steps)
+    ev1.record(bs)
+    ev1.synchronize()
+    if sampler:
+        sampler.__exit__(None, None, None)
+    batched_ms = ev0.elapsed_time(ev1)
+    batched_launches = b.launch_count()
+    step_bytes = sum(v["bytes"] for v in b.kernel_stats().values()) / steps
+    # per-kernel times from a short run of direct (event-timed) launches
+    b.set_kernel_timing(True)
+    b.reset_kernel_stats()
+    kt = min(steps, 20)
+    b.solve(kt)
+    b.synchronize()
+    stats = b.kernel_stats()
+    b.set_kernel_timing(False)
+    peak, peak_src = measured_peaks()
+    timed = {k: v for k, v in stats.items() if v["launches"] and v["ms"] > 0}
+    total_ms = sum(v["ms"] for v in timed.values())
+    kernels = {k: {"launches": v["launches"], "share": round(v["ms"] / total_ms, 4),
+                   "us_per_launch": round(1e3 * v["ms"] / v["launches"], 1),
+                   "gbps": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1)} for k, v in timed.items()}
+    dom = max(timed, key=lambda k: timed[k]["ms"])
+    dgb = timed[dom]["bytes"] / (timed[dom]["ms"] / 1e3) / 1e9
+    tuned = b.describe()
+    b.close()
+    for s in solvers:
+        s.set_stream(None)
+        s.close()
+    plain_v = vss_step * steps / (plain_ms / 1e3)
+    batched_v = vss_step * steps / (batched_ms / 1e3)
+    out = {"workload": f"batched_{args.batch_domains}: {args.batch_domains} domains, sides log-uniform [32,160] "
+                       "per axis, 1-6 substrates, 100-50,000 agents, FP32, x-face Dirichlet + interior nodes",
+           "vss_per_step": vss_step, "steps": steps, "warmup": warm, "setup_s": round(setup_s, 1),
+           "plain": {"value": plain_v, "ms_per_step": plain_ms / steps, "gpu_launches": int(plain_launches),
+                     "path": "pcg_solve(1) per domain, one domain after another on one stream"},
+           "batched": {"value": batched_v, "ms_per_step": batched_ms / steps, "gpu_launches": int(batched_launches),
+                       "path": "pcg_batch_solve: one launch per phase over all domains, CUDA-graph replay",
+                       "autotune_s": round(tune_s, 2)},
+           "speedup": batched_v / plain_v, "unit": UNIT,
+           "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(dgb, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(dgb / peak, 4), "peak_source": peak_src},
+           "step_roofline": {"achieved": round(step_bytes / (batched_ms / steps / 1e3) / 1e9, 1), "peak": peak,
+                             "frac": round(step_bytes / (batched_ms / steps / 1e3) / 1e9 / peak, 4),
+                             "algorithmic_bytes_per_step": step_bytes},
+           "kernels": kernels, "autotune": tuned["buckets"]}
+    if sampler:
+        out["clocks"] = sampler.summary()
+    return out
 
 
 def main():
@@ -304,12 +405,19 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n", type=int, default=WORKLOAD["n"], help="grid side (default: the 320^3 workload)")
+    ap.add_argument("--batch-domains", type=int, default=256, help="domains of the batched workload (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=200)
+    ap.add_argument("--only-batched", action="store_true", help="run only the batched workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     w = dict(WORKLOAD, n=args.n)
     if args.impl == "reference":
         run_reference(args, w)
+    elif args.only_batched:
+        import torch
+        torch.cuda.set_device(dist_env()[2])
+        print(json.dumps(run_batched(args, dist_env()[2], ClockSampler)), flush=True)
     else:
         run_gb300(args, w)
 

@@ -90,7 +90,8 @@ int pcg_destroy(pcg_context* ctx);
 /* Text of the last error raised on this thread ("" when none). */
 const char* pcg_last_error(void);
 /* Runs later work of this context on `stream` (a cudaStream_t); NULL restores
- * the context's own stream. */
+ * the context's own stream.  The caller keeps `stream` alive while the context
+ * uses it (pcg_destroy synchronises the current stream). */
 int pcg_set_stream(pcg_context* ctx, void* stream);
 int pcg_get_stream(pcg_context* ctx, void** stream);
 
@@ -212,12 +213,14 @@ int pcg_batch_set_graph(pcg_batch* batch, int enable);
  * bucket (line length, substrates) present in the batch and keeps the fastest;
  * results are cached for the process.  Field contents are restored afterwards. */
 int pcg_batch_autotune(pcg_batch* batch);
-/* Overrides the autotuner for one sweep axis of every domain (tests, experiments):
- * mapping PCG_MAP_ROW (a thread owns a row) or PCG_MAP_SUBSTRATE (a thread owns
- * one substrate of a row; x only), rows = rows per x tile or points per y/z chunk
- * (0: the default); clamped per domain to what fits.  mapping < 0 removes it. */
+/* Overrides the autotuner for one sweep axis of every domain (tests, experiments).
+ * x: mapping PCG_MAP_ROW (a thread owns a row) or PCG_MAP_SUBSTRATE (a thread owns
+ * one substrate of a row); y/z: PCG_MAP_COLUMN (a lane owns one (x,s) column).
+ * rows = rows per x tile or points per y/z TMA box (0: the default), clamped per
+ * domain to what fits.  mapping < 0 removes the override. */
 #define PCG_MAP_ROW 0
 #define PCG_MAP_SUBSTRATE 1
+#define PCG_MAP_COLUMN 0
 int pcg_batch_force_config(pcg_batch* batch, int axis, int mapping, uint32_t rows);
 /* Writes a JSON description of the per-bucket choices (NUL-terminated, at most
  * cap bytes); *needed receives the full length including the NUL. */

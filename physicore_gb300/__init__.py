@@ -294,6 +294,8 @@ class Solver:
         return p.value, eb.value, pitch.value
 
     def set_stream(self, stream_handle):
+        """Queues this context's work on `stream_handle` (None: its own stream).  The
+        stream must outlive its use by the context."""
         self._check(self._L.pcg_set_stream(self._h, ctypes.c_void_p(stream_handle)))
 
     def stream(self):

@@ -32,6 +32,7 @@
 //   y/z: points per TMA chunk (how early a line's solve can start vs. how many
 //        copies a tile takes).
 #include <algorithm>
+#include <array>
 #include <map>
 #include <mutex>
 #include <numeric>
@@ -54,9 +55,10 @@ enum : uint32_t
 {
 	kMapRow = 0,       // x: a thread owns a row (all substrates)
 	kMapSubstrate = 1, // x: a thread owns one substrate of a row
+	kMapColumn = 0,    // y/z: a lane owns one (x,s) column
 };
 
-constexpr uint32_t kMaxChunks = 64;        // y/z chunks per line (one parity bit each)
+constexpr uint32_t kMaxChunks = 64;        // y/z boxes per line (TMA operations per tile)
 constexpr uint64_t kClearChunk = 4096;     // voxels of the ballot counts cleared per warp item
 constexpr uint64_t kXSmemDefault = 32768;  // default shared-memory budget of an x tile
 
@@ -69,10 +71,12 @@ struct BatchDomain
 	uint32_t x_rows; // rows per x tile
 	uint32_t x_mode; // kMapRow or kMapSubstrate
 	uint64_t x_smem_pitch;
-	uint64_t xblocks; // 32-element column blocks of a row (y/z tiles)
 	uint32_t box_rows[3], boxes[3];
+	uint64_t yz_xblocks;       // y/z: tiles across a row (32 elements each)
 	const void* coef[3];
 	uint64_t coef_len[3];
+	uint64_t coef_comp_off[3]; // compressed tables (elements into coef)
+	uint32_t coef_head[3];     // head points of the compressed tables
 	FaceArgs faces;
 	const uint64_t* dir_offsets;
 	const void* dir_values;
@@ -101,7 +105,6 @@ struct BatchArgs
 	uint32_t* counter;        // tile counter of this launch (zeroed at the start of every step)
 	uint32_t* err;            // [0] DEV_ERR_* bits, [1] lowest failing domain
 	const uint8_t* recompute; // per domain: rebuild the ballot this step
-	uint32_t max_boxes;
 };
 
 __device__ __forceinline__ uint32_t find_entry(const WorkList& l, uint64_t u)
@@ -286,7 +289,11 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 		{
 			const uint32_t rl = tid / S, s = tid % S;
 			if (rl < nrows)
-				solve_row_strided<T>(tile + rl * spitch, cB, cE, cC, n, S, s);
+			{
+				const LineCoef<T> L =
+					line_coef<T>(static_cast<const T*>(D.coef[0]) + D.coef_comp_off[0], S, D.coef_head[0], n, s);
+				solve_line<T, 0>(tile + rl * spitch + s, n, S, L);
+			}
 		}
 		dev::fence_proxy_async_smem();
 		__syncthreads();
@@ -300,28 +307,26 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 	dev::bulk_wait_all();
 }
 
-// y/z: a tile is 32 consecutive (x,s) columns at every point of one line set of
-// one domain; its chunks arrive through the domain's tensor map, each on its own
-// mbarrier, and are stored back as back substitution finishes them.
+// y/z: a tile is 32 consecutive (x,s) columns at every point of one line
+// set of one domain; its boxes arrive through the domain's tensor map on one
+// mbarrier, the warp solves it in place, and the boxes are stored back before the
+// next tile is requested (several single-warp CTAs per SM overlap these phases).
 template <typename T, int AXIS>
 __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 {
 	extern __shared__ __align__(128) unsigned char smem[];
 	uint64_t* full = reinterpret_cast<uint64_t*>(smem);
-	T* base = reinterpret_cast<T*>(smem + round_up(b.max_boxes * 8, 128));
+	T* base = reinterpret_cast<T*>(smem + 128);
 	const uint32_t lane = threadIdx.x;
 	if (lane == 0)
 	{
-		for (uint32_t c = 0; c < b.max_boxes; c++)
-			dev::mbar_init(&full[c], 1);
+		dev::mbar_init(full, 1);
 		dev::fence_mbar_init();
 	}
 	__syncwarp();
-	uint64_t parity = 0; // bit c: parity of barrier c's next completion
-	uint32_t prev = 0xffffffffu;
+	uint32_t phase = 0, prev = 0xffffffffu, bad = 0;
 	bool ok = true;
-	uint32_t bad = 0;
-	for (;;)
+	for (;; phase ^= 1)
 	{
 		uint32_t t32 = 0;
 		if (lane == 0)
@@ -333,8 +338,8 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 		const uint32_t di = __ldg(b.list.dom + k);
 		const BatchDomain& D = b.doms[di];
 		const uint64_t lt = t - __ldg(b.list.base + k);
-		const int x0 = (int)((lt % D.xblocks) * kLanes);
-		const int o = (int)(lt / D.xblocks);
+		const int x0 = (int)((lt % D.yz_xblocks) * kLanes);
+		const int o = (int)(lt / D.yz_xblocks);
 		const uint32_t R = D.box_rows[AXIS], nc = D.boxes[AXIS], n = D.n[AXIS], S = D.S;
 		const uint32_t chunk_elems = R * kLanes;
 		const CUtensorMap* map = b.tmaps + 2 * di + (AXIS - 1);
@@ -342,48 +347,43 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 		{
 			if (di != prev)
 				fence_tensormap_acquire(map);
+			dev::mbar_arrive_expect_tx(full, nc * chunk_elems * (uint32_t)sizeof(T));
 			for (uint32_t c = 0; c < nc; c++)
 			{
-				dev::mbar_arrive_expect_tx(&full[c], chunk_elems * (uint32_t)sizeof(T));
 				if (AXIS == 1)
-					dev::tma_load_3d(base + c * chunk_elems, map, x0, (int)(c * R), o, &full[c]);
+					dev::tma_load_3d(base + c * chunk_elems, map, x0, (int)(c * R), o, full);
 				else
-					dev::tma_load_3d(base + c * chunk_elems, map, x0, o, (int)(c * R), &full[c]);
+					dev::tma_load_3d(base + c * chunk_elems, map, x0, o, (int)(c * R), full);
 			}
 		}
 		prev = di;
-		const T* cB = static_cast<const T*>(D.coef[AXIS]);
-		const T* cE = cB + D.coef_len[AXIS];
-		const T* cC = cE + D.coef_len[AXIS];
-		const uint64_t cp = D.coef_len[AXIS] / S;
-		const uint32_t s = (uint64_t)(x0 + lane) < D.row_len ? (uint32_t)((x0 + lane) % S) : 0;
-		solve_column_chunked<T>(
-			base + lane, n, R, cB + s * cp, cE + s * cp, __ldg(cC + s),
-			[&](uint32_t ch) {
-				ok = dev::mbar_wait(&full[ch], (uint32_t)(parity >> ch) & 1u) && ok;
-				parity ^= 1ull << ch;
-			},
-			[&](uint32_t ch) {
-				dev::fence_proxy_async_smem();
-				__syncwarp();
-				if (lane == 0)
-				{
-					if (AXIS == 1)
-						dev::tma_store_3d(map, x0, (int)(ch * R), o, base + ch * chunk_elems);
-					else
-						dev::tma_store_3d(map, x0, o, (int)(ch * R), base + ch * chunk_elems);
-					dev::bulk_commit();
-				}
-				__syncwarp();
-			});
-		if (lane == 0)
-			dev::bulk_wait_read();
-		__syncwarp();
-		if (!__all_sync(0xffffffffu, ok))
+		ok = __all_sync(0xffffffffu, dev::mbar_wait(full, phase));
+		if (!ok)
 		{
 			bad = di;
 			break;
 		}
+		{
+			const uint32_t s = (uint64_t)(x0 + lane) < D.row_len ? (uint32_t)((x0 + lane) % S) : 0;
+			const LineCoef<T> L = line_coef<T>(static_cast<const T*>(D.coef[AXIS]) + D.coef_comp_off[AXIS], S,
+											   D.coef_head[AXIS], n, s);
+			solve_line<T, kLanes>(base + lane, n, 0, L);
+		}
+		dev::fence_proxy_async_smem();
+		__syncwarp();
+		if (lane == 0)
+		{
+			for (uint32_t c = 0; c < nc; c++)
+			{
+				if (AXIS == 1)
+					dev::tma_store_3d(map, x0, (int)(c * R), o, base + c * chunk_elems);
+				else
+					dev::tma_store_3d(map, x0, o, (int)(c * R), base + c * chunk_elems);
+			}
+			dev::bulk_commit();
+			dev::bulk_wait_read();
+		}
+		__syncwarp();
 	}
 	if (!ok && lane == 0)
 		report(b, DEV_ERR_WAIT_TIMEOUT, bad);
@@ -612,13 +612,16 @@ uint64_t batch_x_pitch(const Context* c)
 	return chunks * vn;
 }
 
-uint64_t x_row_stage_bytes(const Context* c) { return batch_x_pitch(c) * c->wsize; }
+uint64_t x_row_stage_bytes(const Context* c, uint32_t mode)
+{
+	return (mode == kMapSubstrate ? sweep_x_sub_pitch(c->row_len, c->S, c->wsize) : batch_x_pitch(c)) * c->wsize;
+}
 
 // Largest valid rows-per-tile of a mapping under a shared-memory budget.
 uint32_t x_rows_cap(const Context* c, uint32_t mode, uint64_t smem_budget)
 {
 	const uint64_t lanes_per_row = mode == kMapRow ? 1 : c->S;
-	uint64_t r = smem_budget / x_row_stage_bytes(c);
+	uint64_t r = smem_budget / x_row_stage_bytes(c, mode);
 	const uint64_t cap = kLanes / lanes_per_row;
 	r = std::min(r, cap);
 	return (uint32_t)std::max<uint64_t>(r, 1);
@@ -672,7 +675,6 @@ struct pcg_batch
 	DeviceBuffer d_doms, d_tmaps, d_lists, d_counters, d_err, d_recompute;
 	pcg::WorkList lists[pcg::L_COUNT] {};
 	uint64_t smem[3] = { 0, 0, 0 };
-	uint32_t max_boxes[3] = { 0, 0, 0 };
 	unsigned grid[3] = { 0, 0, 0 };
 	int max_dims = 0;
 	bool built = false;
@@ -686,6 +688,10 @@ struct pcg_batch
 	pcg::KernelStat graph_step[pcg::K_COUNT]; // launches and bytes of one replayed step
 
 	bool timing = false;
+	double step_bytes[pcg::K_COUNT] = {}; // algorithmic bytes of one launch of each kernel
+	// per domain: bytes of the ballot-rebuild kernels (clear, locate, ballot,
+	// reduce), which only count for domains that rebuild in the current call
+	std::vector<std::array<double, 4>> rebuild_bytes;
 	pcg::KernelStat stats[pcg::K_COUNT];
 	uint64_t launches = 0;
 	struct Pending
@@ -748,12 +754,17 @@ BatchDomain describe_domain(pcg_batch* b, size_t d)
 	const AxisConfig& x = b->cfg[0][d];
 	D.x_rows = x.rows;
 	D.x_mode = x.mode;
-	D.x_smem_pitch = batch_x_pitch(c);
-	D.xblocks = (c->row_len + kLanes - 1) / kLanes;
+	D.x_smem_pitch = x.mode == kMapSubstrate ? sweep_x_sub_pitch(c->row_len, c->S, c->wsize) : batch_x_pitch(c);
 	for (int a = 1; a < c->dims; a++)
 	{
 		D.box_rows[a] = b->cfg[a][d].rows;
 		D.boxes[a] = (uint32_t)((c->n[a] + D.box_rows[a] - 1) / D.box_rows[a]);
+	}
+	D.yz_xblocks = (c->row_len + kLanes - 1) / kLanes;
+	for (int a = 0; a < c->dims; a++)
+	{
+		D.coef_comp_off[a] = c->coef_comp_off[a];
+		D.coef_head[a] = c->coef_head[a];
 	}
 	D.faces = make_face_args(c);
 	D.dir_offsets = static_cast<const uint64_t*>(c->dir_offsets.ptr);
@@ -791,11 +802,11 @@ void list_units(pcg_batch* b, int id, size_t d, uint64_t& units, double& cost)
 		break;
 	case L_Y:
 		if (c->dims >= 2)
-			units = D.xblocks * c->n[2], cost = (double)c->n[1];
+			units = D.yz_xblocks * c->n[2], cost = (double)c->n[1];
 		break;
 	case L_Z:
 		if (c->dims >= 3)
-			units = D.xblocks * c->n[1], cost = (double)c->n[2];
+			units = D.yz_xblocks * c->n[1], cost = (double)c->n[2];
 		break;
 	case L_FACES: units = D.faces.face_mask ? D.faces.total * c->S : 0; break;
 	case L_INTERIOR: units = c->K * c->S; break;
@@ -862,9 +873,6 @@ int upload_lists(DeviceBuffer& buf, const std::vector<HostList>& hl, WorkList* o
 	return PCG_OK;
 }
 
-template <typename T>
-int set_sweep_attributes(pcg_batch* b);
-
 // Encodes the y/z tensor maps of domain d with its current chunk sizes.
 int encode_maps(pcg_batch* b, size_t d)
 {
@@ -904,10 +912,9 @@ void drop_graph(pcg_batch* b)
 }
 
 template <typename T>
-uint64_t sweep_smem(pcg_batch* b, int axis, const std::vector<size_t>& subset, uint32_t* max_boxes)
+uint64_t sweep_smem(pcg_batch* b, int axis, const std::vector<size_t>& subset)
 {
 	uint64_t best = 0;
-	uint32_t mb = 1;
 	for (size_t d : subset)
 	{
 		Context* c = C(b, d);
@@ -917,15 +924,10 @@ uint64_t sweep_smem(pcg_batch* b, int axis, const std::vector<size_t>& subset, u
 		if (axis == 0)
 			best = std::max<uint64_t>(best, 16 + (uint64_t)D.x_rows * D.x_smem_pitch * sizeof(T));
 		else
-		{
-			mb = std::max(mb, D.boxes[axis]);
 			best = std::max<uint64_t>(best, (uint64_t)D.boxes[axis] * D.box_rows[axis] * kLanes * sizeof(T));
-		}
 	}
 	if (axis > 0)
-		best += round_up((uint64_t)mb * 8, 128);
-	if (max_boxes)
-		*max_boxes = mb;
+		best += 128; // the tile's mbarrier
 	return best;
 }
 
@@ -996,9 +998,34 @@ int build_t(pcg_batch* b)
 		b->smem[axis] = 0;
 		if (b->lists[axis].total == 0)
 			continue;
-		b->smem[axis] = sweep_smem<T>(b, axis, all, &b->max_boxes[axis]);
+		b->smem[axis] = sweep_smem<T>(b, axis, all);
 		if ((rc = sweep_grid<T>(b, axis, b->smem[axis], b->lists[axis].total, &b->grid[axis])))
 			return rc;
+	}
+	// algorithmic bytes per launch, with the single-domain launchers' per-item counts
+	std::fill(b->step_bytes, b->step_bytes + K_COUNT, 0.0);
+	b->rebuild_bytes.assign(N, { 0.0, 0.0, 0.0, 0.0 });
+	const double w = (double)sizeof(T);
+	for (size_t d = 0; d < N; d++)
+	{
+		const Context* c = C(b, d);
+		const double V = (double)c->V, S = (double)c->S, A = (double)c->A;
+		for (int a = 0; a < c->dims; a++)
+			b->step_bytes[K_SWEEP_X + a] += 2.0 * V * S * w;
+		const FaceArgs& f = b->h_doms[d].faces;
+		if (f.face_mask)
+			b->step_bytes[K_DIRICHLET_FACES] += (double)f.total * S * w;
+		b->step_bytes[K_DIRICHLET_INTERIOR] += (double)c->K * (8 + S * (2 * w + 1));
+		if (c->bulk_mode != PCG_BULK_NONE)
+			b->step_bytes[K_BULK] += V * S * w * (c->bulk_mode == PCG_BULK_PER_VOXEL ? 5.0 : 2.0);
+		if (c->A)
+		{
+			b->rebuild_bytes[d] = { 4.0 * V, A * (8.0 * c->dims + 1 + 5 * S * 8 + 8 + 6 * S * w + 4), A * 12,
+									A * (8 + 6 * S * w) };
+			b->step_bytes[K_CELLS_APPLY] += A * (8 + 5 * S * w + (c->compute_internalized ? 16 * S : 0));
+			if (c->compute_internalized)
+				b->step_bytes[K_CELLS_INTERNALIZE] += A * (8 + 4 * S * w + 16 * S);
+		}
 	}
 	b->built = true;
 	drop_graph(b);
@@ -1071,7 +1098,6 @@ BatchArgs args_for(pcg_batch* b, int list, int counter)
 	a.counter = static_cast<uint32_t*>(b->d_counters.ptr) + counter;
 	a.err = static_cast<uint32_t*>(b->d_err.ptr);
 	a.recompute = static_cast<const uint8_t*>(b->d_recompute.ptr);
-	a.max_boxes = list <= L_Z ? b->max_boxes[list] : 0;
 	return a;
 }
 
@@ -1080,14 +1106,6 @@ unsigned flat_grid(pcg_batch* b, uint64_t work, unsigned block)
 	uint64_t g = (work + block - 1) / block;
 	const uint64_t cap = (uint64_t)b->sm_count * 16;
 	return (unsigned)std::max<uint64_t>(1, std::min(g, cap));
-}
-
-double field_bytes(pcg_batch* b)
-{
-	double s = 0;
-	for (size_t d = 0; d < b->ctx.size(); d++)
-		s += (double)(C(b, d)->V * C(b, d)->S);
-	return s * (double)b->wsize;
 }
 
 // Launches one sweep axis over a work list (used by the step and by the tuner).
@@ -1109,31 +1127,30 @@ int launch_sweep(pcg_batch* b, int axis, const BatchArgs& a, unsigned grid, uint
 template <typename T>
 int launch_step(pcg_batch* b)
 {
-	const double w = (double)sizeof(T);
-	const double fb = field_bytes(b);
+	const double* sb = b->step_bytes;
 	PCG_CUDA_TRY(cudaMemsetAsync(b->d_counters.ptr, 0, 4 * sizeof(uint32_t), b->stream));
 	int rc;
 	for (int axis = 0; axis < 3; axis++)
-		if (b->lists[axis].total &&
-			(rc = launch_sweep<T>(b, axis, args_for(b, axis, axis), b->grid[axis], b->smem[axis], 2.0 * fb)))
+		if (b->lists[axis].total && (rc = launch_sweep<T>(b, axis, args_for(b, axis, axis), b->grid[axis],
+														   b->smem[axis], sb[K_SWEEP_X + axis])))
 			return rc;
 	if (b->lists[L_FACES].total)
 	{
-		LaunchScope s(b, K_DIRICHLET_FACES, (double)b->lists[L_FACES].total * w);
+		LaunchScope s(b, K_DIRICHLET_FACES, sb[K_DIRICHLET_FACES]);
 		batch_faces_kernel<T><<<flat_grid(b, b->lists[L_FACES].total, 256), 256, 0, b->stream>>>(
 			args_for(b, L_FACES, 3));
 		PCG_CUDA_TRY(cudaGetLastError());
 	}
 	if (b->lists[L_INTERIOR].total)
 	{
-		LaunchScope s(b, K_DIRICHLET_INTERIOR, (double)b->lists[L_INTERIOR].total * (2 * w + 1));
+		LaunchScope s(b, K_DIRICHLET_INTERIOR, sb[K_DIRICHLET_INTERIOR]);
 		batch_interior_kernel<T><<<flat_grid(b, b->lists[L_INTERIOR].total, 256), 256, 0, b->stream>>>(
 			args_for(b, L_INTERIOR, 3));
 		PCG_CUDA_TRY(cudaGetLastError());
 	}
 	if (b->lists[L_BULK].total)
 	{
-		LaunchScope s(b, K_BULK, 2.0 * fb);
+		LaunchScope s(b, K_BULK, sb[K_BULK]);
 		batch_bulk_kernel<T><<<flat_grid(b, b->lists[L_BULK].total * 32, 256), 256, 0, b->stream>>>(
 			args_for(b, L_BULK, 3));
 		PCG_CUDA_TRY(cudaGetLastError());
@@ -1143,33 +1160,33 @@ int launch_step(pcg_batch* b)
 	{
 		const unsigned g = (unsigned)((A + 255) / 256);
 		{
-			LaunchScope s(b, K_CELLS_CLEAR, 0);
+			LaunchScope s(b, K_CELLS_CLEAR, sb[K_CELLS_CLEAR]);
 			batch_clear_counts_kernel<<<flat_grid(b, b->lists[L_CLEAR].total * 32, 256), 256, 0, b->stream>>>(
 				args_for(b, L_CLEAR, 3));
 			PCG_CUDA_TRY(cudaGetLastError());
 		}
 		{
-			LaunchScope s(b, K_CELLS_LOCATE, 0);
+			LaunchScope s(b, K_CELLS_LOCATE, sb[K_CELLS_LOCATE]);
 			batch_cells_locate_kernel<T><<<g, 256, 0, b->stream>>>(args_for(b, L_AGENTS, 3));
 			PCG_CUDA_TRY(cudaGetLastError());
 		}
 		{
-			LaunchScope s(b, K_CELLS_BALLOT, 0);
+			LaunchScope s(b, K_CELLS_BALLOT, sb[K_CELLS_BALLOT]);
 			batch_cells_ballot_kernel<<<g, 256, 0, b->stream>>>(args_for(b, L_AGENTS, 3));
 			PCG_CUDA_TRY(cudaGetLastError());
 		}
 		{
-			LaunchScope s(b, K_CELLS_REDUCE, 0);
+			LaunchScope s(b, K_CELLS_REDUCE, sb[K_CELLS_REDUCE]);
 			batch_cells_reduce_kernel<T><<<g, 256, 0, b->stream>>>(args_for(b, L_AGENTS, 3));
 			PCG_CUDA_TRY(cudaGetLastError());
 		}
 		{
-			LaunchScope s(b, K_CELLS_APPLY, (double)A * (8 + 5 * w * 3.5));
+			LaunchScope s(b, K_CELLS_APPLY, sb[K_CELLS_APPLY]);
 			batch_cells_apply_kernel<T><<<g, 256, 0, b->stream>>>(args_for(b, L_AGENTS, 3));
 			PCG_CUDA_TRY(cudaGetLastError());
 		}
 		{
-			LaunchScope s(b, K_CELLS_INTERNALIZE, 0);
+			LaunchScope s(b, K_CELLS_INTERNALIZE, sb[K_CELLS_INTERNALIZE]);
 			batch_cells_internalize_kernel<T><<<g, 256, 0, b->stream>>>(args_for(b, L_AGENTS, 3));
 			PCG_CUDA_TRY(cudaGetLastError());
 		}
@@ -1299,6 +1316,15 @@ int upload_recompute(pcg_batch* b)
 	const size_t N = b->ctx.size();
 	for (size_t d = 0; d < N; d++)
 		b->h_recompute[d] = C(b, d)->recompute_cells ? 1 : 0;
+	static const int rebuild_kernels[4] = { K_CELLS_CLEAR, K_CELLS_LOCATE, K_CELLS_BALLOT, K_CELLS_REDUCE };
+	for (int k = 0; k < 4; k++)
+	{
+		double sum = 0;
+		for (size_t d = 0; d < N; d++)
+			sum += b->h_recompute[d] ? b->rebuild_bytes[d][k] : 0.0;
+		b->step_bytes[rebuild_kernels[k]] = sum;
+		b->graph_step[rebuild_kernels[k]].bytes = sum;
+	}
 	if (b->dev_recompute_valid && b->dev_recompute == b->h_recompute)
 		return PCG_OK;
 	PCG_CUDA_TRY(cudaMemcpyAsync(b->d_recompute.ptr, b->h_recompute.data(), N, cudaMemcpyHostToDevice, b->stream));
@@ -1339,8 +1365,7 @@ int time_axis(pcg_batch* b, int axis, const std::vector<size_t>& subset, double*
 	WorkList wl {};
 	if ((rc = upload_lists(lbuf, hl, &wl, b->stream)))
 		return rc;
-	uint32_t mb = 1;
-	const uint64_t smem = sweep_smem<T>(b, axis, subset, &mb);
+	const uint64_t smem = sweep_smem<T>(b, axis, subset);
 	unsigned grid = 0;
 	if ((rc = sweep_grid<T>(b, axis, smem, wl.total, &grid)))
 	{
@@ -1349,7 +1374,6 @@ int time_axis(pcg_batch* b, int axis, const std::vector<size_t>& subset, double*
 	}
 	BatchArgs a = args_for(b, axis, axis);
 	a.list = wl;
-	a.max_boxes = mb;
 	cudaEvent_t e0, e1;
 	cudaEventCreate(&e0);
 	cudaEventCreate(&e1);
@@ -1400,10 +1424,10 @@ std::vector<AxisConfig> candidates(const Context* c, int axis)
 		return out;
 	}
 	const uint64_t n = c->n[axis];
-	for (uint32_t R : { 8u, 16u, 32u, 64u })
+	for (uint32_t R : { 16u, 32u, 64u, 128u })
 		if (R < n)
-			add({ 0, fit_chunk(n, R) });
-	add({ 0, fit_chunk(n, (uint32_t)round_up(n, kBlock)) }); // one chunk per line
+			add({ kMapColumn, fit_chunk(n, R) });
+	add({ kMapColumn, fit_chunk(n, (uint32_t)round_up(n, kBlock)) }); // fewest boxes per line
 	return out;
 }
 
@@ -1517,7 +1541,7 @@ std::string describe(pcg_batch* b)
 			if (r.axis == 0)
 				return std::string("{\"mapping\": \"") + (a.mode == kMapRow ? "row-per-thread" : "substrate-per-thread") +
 					   "\", \"rows_per_tile\": " + std::to_string(a.rows) + "}";
-			return std::string("{\"mapping\": \"column-per-lane\", \"chunk_points\": ") + std::to_string(a.rows) + "}";
+			return std::string("{\"mapping\": \"column-per-lane\", \"box_points\": ") + std::to_string(a.rows) + "}";
 		};
 		s += "{\"axis\": " + std::to_string(r.axis) + ", \"line_bucket\": " + std::to_string(r.n_bucket) +
 			 ", \"substrates\": " + std::to_string(r.S) + ", \"domains\": " + std::to_string(r.domains) +
@@ -1703,10 +1727,10 @@ int pcg_batch_force_config(pcg_batch* b, int axis, int mapping, uint32_t rows)
 	BATCH_CHECK(b);
 	if (axis < 0 || axis > 2)
 		return fail(PCG_ERR_INVALID, "axis must be 0, 1 or 2");
-	if (mapping > PCG_MAP_SUBSTRATE || (axis > 0 && mapping == PCG_MAP_SUBSTRATE))
+	if (mapping > 1 || (axis > 0 && mapping > 0))
 		return fail(PCG_ERR_INVALID, "unknown mapping for this axis");
 	b->forced[axis] = mapping >= 0;
-	b->force[axis].mode = mapping == PCG_MAP_SUBSTRATE ? pcg::kMapSubstrate : pcg::kMapRow;
+	b->force[axis].mode = (uint32_t)std::max(mapping, 0);
 	b->force[axis].rows = rows;
 	b->built = false;
 	return PCG_OK;

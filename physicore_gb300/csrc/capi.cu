@@ -190,9 +190,45 @@ static int upload_coefficients(Context* c)
 		const uint64_t cp = coef_row_pitch(n);
 		const uint64_t len = axis == 0 ? coef_table_len(n, S, sizeof(T)) : S * cp;
 		const uint64_t total = 2 * len + round_up(S, 16 / sizeof(T));
+		// Compressed tables.  b'_i and e_i converge to a constant within a few
+		// points, so a line needs only a head of H points (the first index from which
+		// every stored value up to n-2 equals the value at n-2, rounded up to the solver
+		// block and taken over all substrates), that middle constant and the values of
+		// the last point.  Stored values are the same rounded numbers as the full table.
+		const uint64_t vn = 16 / sizeof(T);
+		uint64_t H = 0;
+		{
+			for (uint64_t sub = 0; sub < S; sub++)
+			{
+				uint64_t h = n;
+				if (n >= 2)
+				{
+					const T bm = (T)b[(n - 2) * S + sub];
+					const T em = n >= 3 ? (T)e[(n - 3) * S + sub] : T(0);
+					h = n - 2;
+					while (h > 0)
+					{
+						const uint64_t i = h - 1;
+						const T bi = (T)b[i * S + sub];
+						const T ei = i == 0 ? T(0) : (T)e[(i - 1) * S + sub];
+						if (bi != bm || ei != em)
+							break;
+						h = i;
+					}
+				}
+				H = std::max(H, h);
+			}
+			H = round_up(std::max<uint64_t>(H, 1), kBlockPoints);
+			if (H >= n)
+				H = round_up(n, kBlockPoints); // the whole line lives in the head
+		}
+		const uint64_t kS = round_up(S, vn);
+		const uint64_t comp_total = 2 * S * H + 5 * kS;
 		c->coef_len[axis] = len;
 		c->coef_elems[axis] = total;
-		std::vector<T> tab(total, T(0));
+		c->coef_comp_off[axis] = total;
+		c->coef_head[axis] = (uint32_t)H;
+		std::vector<T> tab(total + comp_total, T(0));
 		for (uint64_t i = 0; i < n; i++)
 			for (uint64_t s = 0; s < S; s++)
 			{
@@ -202,6 +238,25 @@ static int upload_coefficients(Context* c)
 			}
 		for (uint64_t s = 0; s < S; s++)
 			tab[2 * len + s] = (T)cc[s];
+		{
+			T* hB = tab.data() + total;
+			T* hE = hB + S * H;
+			T* k = hE + S * H; // [mid b' | mid e | last b' | last e | c], each kS long
+			for (uint64_t sub = 0; sub < S; sub++)
+			{
+				for (uint64_t i = 0; i < std::min(H, n); i++)
+				{
+					hB[sub * H + i] = (T)b[i * S + sub];
+					hE[sub * H + i] = i == 0 ? T(0) : (T)e[(i - 1) * S + sub];
+				}
+				const uint64_t m = n >= 2 ? n - 2 : 0;
+				k[sub] = (T)b[m * S + sub];
+				k[kS + sub] = m == 0 ? T(0) : (T)e[(m - 1) * S + sub];
+				k[2 * kS + sub] = (T)b[(n - 1) * S + sub];
+				k[3 * kS + sub] = n == 1 ? T(0) : (T)e[(n - 2) * S + sub];
+				k[4 * kS + sub] = (T)cc[sub];
+			}
+		}
 		int rc = dalloc(c, c->coef[axis], tab.size() * sizeof(T));
 		if (rc)
 			return rc;

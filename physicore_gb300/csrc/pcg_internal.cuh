@@ -72,6 +72,7 @@ constexpr int kLanes = 32;           // lines per y/z tile, rows per x tile (one
 constexpr int kStages = 2;           // shared-memory ring depth of the persistent sweeps
 constexpr uint64_t kMaxSmemBytes = 227 * 1024;
 constexpr uint64_t kCoefSmemLimit = 64 * 1024; // larger coefficient tables stay in global memory
+constexpr uint64_t kBlockPoints = 8;           // line points per pipelined solver block
 
 __host__ __device__ constexpr uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
 __host__ __device__ constexpr int gcd_i(int a, int b) { return b == 0 ? a : gcd_i(b, a % b); }
@@ -100,6 +101,8 @@ struct SweepArgs
 	uint64_t xblocks;
 	uint32_t box_rows;    // line points per TMA box (<= 256)
 	uint32_t boxes;       // boxes per tile (boxes * box_rows >= n)
+	uint64_t comp_off;    // compressed coefficient tables (elements into coef)
+	uint32_t head;        // head points of the compressed tables
 	// x sweep: a tile is rows_per_tile whole rows
 	uint64_t rows;        // ny*nz
 	uint64_t smem_pitch;  // shared-memory row pitch (elements); in 16-byte chunks == threads per row (mod 8)
@@ -169,6 +172,8 @@ struct Context
 	uint32_t tmap_boxes[3] = { 0, 0, 0 };
 	uint64_t coef_len[3] = { 0, 0, 0 };
 	uint64_t coef_elems[3] = { 0, 0, 0 };
+	uint64_t coef_comp_off[3] = { 0, 0, 0 }; // compressed tables (head rows, constants)
+	uint32_t coef_head[3] = { 0, 0, 0 };     // head points per substrate of the compressed tables
 	DeviceBuffer err;      // uint32 device error word
 	DeviceBuffer flags;    // uint32 [4]: [0] ballot conflict
 	DeviceBuffer mass;     // double [S]
@@ -285,14 +290,17 @@ struct DeviceGuard
 uint64_t coef_table_len(uint64_t n, uint64_t S, size_t wsize);
 uint64_t coef_row_pitch(uint64_t n);
 uint64_t sweep_x_smem_pitch(uint64_t row_len, uint64_t S, size_t wsize);
+// x mapping of the single-domain sweep: substrate-per-thread (true) or row-per-thread
+bool x_substrate_mapping(uint64_t S);
+uint64_t sweep_x_sub_pitch(uint64_t row_len, uint64_t S, size_t wsize);
 uint64_t x_threads_per_row(uint64_t S, size_t wsize);
 uint64_t sweep_smem_bytes(const Context* c, int axis);
 int prepare_sweep_maps(Context* c);
 // y/z chunk geometry: points per TMA box and boxes per line
 void box_geometry(uint64_t n, uint32_t& box_rows, uint32_t& boxes);
-// TMA map of the field as the tensor (x*S+s, y, z) with boxes of 32 x box_rows
-// points along `axis` (1 or 2)
-int encode_field_map(const Context* c, int axis, uint32_t box_rows, CUtensorMap* out);
+// TMA map of the field as the tensor (x*S+s, y, z) with boxes of box_cols x
+// box_rows points along `axis` (1 or 2)
+int encode_field_map(const Context* c, int axis, uint32_t box_rows, CUtensorMap* out, uint32_t box_cols = 32);
 
 } // namespace pcg
 

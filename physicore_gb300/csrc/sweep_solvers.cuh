@@ -46,17 +46,83 @@ __device__ __forceinline__ V ldg_vec(const V* p)
 }
 
 
-// One line at col[j*kLanes], j < n, in shared memory; eE/eB are the line's
-// substrate rows of a [s][j] coefficient table (16-byte aligned, padded to a
-// multiple of kBlock).  Blocks of kBlock points are pipelined: the next block's
-// points and coefficients are requested before the current block's chain.
+// One lane's coefficients along a line, from the compressed tables of an axis:
+// points j < H read the substrate's head rows, points H <= j < n-1 share the middle
+// constants, and point n-1 has its own (when H >= n the head holds the whole line).
+// H is a multiple of kBlock, so a block of points is either all head or all
+// middle/last.  The stored values are the full table's (the host picks H so that
+// every point from H to n-2 holds exactly the middle value).
 template <typename T>
-__device__ __forceinline__ void solve_column(T* __restrict__ col, uint32_t n, const T* __restrict__ eB,
-											 const T* __restrict__ eE, T c)
+struct LineCoef
+{
+	const T* hB;
+	const T* hE;
+	uint32_t H, n;
+	T mB, mE, lB, lE, c;
+};
+
+// Compressed table of an axis: [head b' (S x H) | head e (S x H) | mid b' | mid e |
+// last b' | last e | c], the five constant arrays kS = S rounded up to 16 bytes long.
+template <typename T>
+__device__ __forceinline__ LineCoef<T> line_coef(const T* comp, uint32_t S, uint32_t H, uint32_t n, uint32_t s)
+{
+	constexpr uint32_t VN = 16 / sizeof(T);
+	const uint32_t kS = (S + VN - 1) / VN * VN;
+	const T* k = comp + 2ull * S * H;
+	LineCoef<T> L;
+	L.hB = comp + (uint64_t)s * H;
+	L.hE = comp + (uint64_t)S * H + (uint64_t)s * H;
+	L.H = H;
+	L.n = n;
+	L.mB = __ldg(k + s);
+	L.mE = __ldg(k + kS + s);
+	L.lB = __ldg(k + 2 * kS + s);
+	L.lE = __ldg(k + 3 * kS + s);
+	L.c = __ldg(k + 4 * kS + s);
+	return L;
+}
+
+// Coefficients of the block of kBlock points starting at j0 (a multiple of kBlock).
+template <typename T, typename V, int NV>
+__device__ __forceinline__ void fetch_block(const T* head, uint32_t H, T mid, T last, uint32_t n, uint32_t j0,
+											V (&out)[NV])
+{
+	constexpr int VN = Vec16<T>::N;
+	if (j0 + kBlock <= H)
+	{
+#pragma unroll
+		for (int v = 0; v < NV; v++)
+			out[v] = __ldg(reinterpret_cast<const V*>(head + j0) + v);
+	}
+	else
+	{
+#pragma unroll
+		for (int v = 0; v < NV; v++)
+#pragma unroll
+			for (int u = 0; u < VN; u++)
+				vset<V, T>(out[v], u, j0 + v * VN + u == n - 1 ? last : mid);
+	}
+}
+
+template <typename T>
+__device__ __forceinline__ T coef_at(const T* head, uint32_t H, T mid, T last, uint32_t n, uint32_t j)
+{
+	return j < H ? __ldg(head + j) : (j == n - 1 ? last : mid);
+}
+
+// One line of n points at col[j * stride] in shared memory (stride = STRIDE, or the
+// run-time value when STRIDE is 0) with the lane's coefficients L.  Blocks of
+// kBlock points are pipelined: the next block's points and coefficients are
+// requested before the current block's dependent chain, so load latency overlaps
+// it; most blocks take their coefficients from registers (the middle constants).
+template <typename T, int STRIDE>
+__device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint32_t rt_stride, const LineCoef<T>& L)
 {
 	using V = typename Vec16<T>::type;
 	constexpr int P = kBlock, VN = Vec16<T>::N, NV = P / VN;
+	const uint32_t st = STRIDE ? (uint32_t)STRIDE : rt_stride;
 	const uint32_t nb = n / P;
+	const T c = L.c;
 	T d = T(0);
 	{
 		T x[P], xn[P];
@@ -65,28 +131,24 @@ __device__ __forceinline__ void solve_column(T* __restrict__ col, uint32_t n, co
 		{
 #pragma unroll
 			for (int q = 0; q < P; q++)
-				x[q] = col[q * kLanes];
-#pragma unroll
-			for (int v = 0; v < NV; v++)
-				e[v] = __ldg(reinterpret_cast<const V*>(eE) + v);
+				x[q] = col[q * st];
+			fetch_block<T, V, NV>(L.hE, L.H, L.mE, L.lE, n, 0, e);
 		}
 		for (uint32_t b = 0; b < nb; b++)
 		{
-			T* blk = col + (uint64_t)b * P * kLanes;
+			T* blk = col + (uint64_t)b * P * st;
 			if (b + 1 < nb)
 			{
 #pragma unroll
 				for (int q = 0; q < P; q++)
-					xn[q] = blk[(P + q) * kLanes];
-#pragma unroll
-				for (int v = 0; v < NV; v++)
-					en[v] = __ldg(reinterpret_cast<const V*>(eE + (b + 1) * P) + v);
+					xn[q] = blk[(P + q) * st];
+				fetch_block<T, V, NV>(L.hE, L.H, L.mE, L.lE, n, (b + 1) * P, en);
 			}
 #pragma unroll
 			for (int q = 0; q < P; q++)
 			{
 				d = dev::fmadd(vget<V, T>(e[q / VN], q % VN), d, x[q]);
-				blk[q * kLanes] = d;
+				blk[q * st] = d;
 			}
 #pragma unroll
 			for (int q = 0; q < P; q++)
@@ -97,46 +159,42 @@ __device__ __forceinline__ void solve_column(T* __restrict__ col, uint32_t n, co
 		}
 		for (uint32_t j = nb * P; j < n; j++)
 		{
-			d = dev::fmadd(__ldg(eE + j), d, col[(uint64_t)j * kLanes]);
-			col[(uint64_t)j * kLanes] = d;
+			d = dev::fmadd(coef_at(L.hE, L.H, L.mE, L.lE, n, j), d, col[(uint64_t)j * st]);
+			col[(uint64_t)j * st] = d;
 		}
 	}
 	d = T(0);
 	for (int j = (int)n - 1; j >= (int)(nb * P); j--)
 	{
-		d = dev::fmadd(c, d, col[(uint64_t)j * kLanes]) * __ldg(eB + j);
-		col[(uint64_t)j * kLanes] = d;
+		d = dev::fmadd(c, d, col[(uint64_t)j * st]) * coef_at(L.hB, L.H, L.mB, L.lB, n, (uint32_t)j);
+		col[(uint64_t)j * st] = d;
 	}
 	{
 		T x[P], xn[P];
 		V bb[NV], bn[NV];
 		if (nb)
 		{
-			const T* blk = col + (uint64_t)(nb - 1) * P * kLanes;
+			const T* blk = col + (uint64_t)(nb - 1) * P * st;
 #pragma unroll
 			for (int q = 0; q < P; q++)
-				x[q] = blk[q * kLanes];
-#pragma unroll
-			for (int v = 0; v < NV; v++)
-				bb[v] = __ldg(reinterpret_cast<const V*>(eB + (nb - 1) * P) + v);
+				x[q] = blk[q * st];
+			fetch_block<T, V, NV>(L.hB, L.H, L.mB, L.lB, n, (nb - 1) * P, bb);
 		}
 		for (int b = (int)nb - 1; b >= 0; b--)
 		{
-			T* blk = col + (uint64_t)b * P * kLanes;
+			T* blk = col + (uint64_t)b * P * st;
 			if (b > 0)
 			{
 #pragma unroll
 				for (int q = 0; q < P; q++)
-					xn[q] = blk[(q - P) * kLanes];
-#pragma unroll
-				for (int v = 0; v < NV; v++)
-					bn[v] = __ldg(reinterpret_cast<const V*>(eB + (b - 1) * P) + v);
+					xn[q] = blk[(q - P) * (int)st];
+				fetch_block<T, V, NV>(L.hB, L.H, L.mB, L.lB, n, (uint32_t)(b - 1) * P, bn);
 			}
 #pragma unroll
 			for (int q = P - 1; q >= 0; q--)
 			{
 				d = dev::fmadd(c, d, x[q]) * vget<V, T>(bb[q / VN], q % VN);
-				blk[q * kLanes] = d;
+				blk[q * st] = d;
 			}
 #pragma unroll
 			for (int q = 0; q < P; q++)
@@ -148,176 +206,6 @@ __device__ __forceinline__ void solve_column(T* __restrict__ col, uint32_t n, co
 	}
 }
 
-
-// solve_column over a line whose points arrive in chunks of R points (R a
-// multiple of kBlock): ready(ch) is called before chunk ch is first read, and
-// done(ch) once back substitution has finished every point of chunk ch.  All
-// lanes of the warp make the same calls, so the hooks may synchronise the warp.
-template <typename T, typename Ready, typename Done>
-__device__ __forceinline__ void solve_column_chunked(T* __restrict__ col, uint32_t n, uint32_t R,
-													 const T* __restrict__ eB, const T* __restrict__ eE, T c,
-													 Ready&& ready, Done&& done)
-{
-	using V = typename Vec16<T>::type;
-	constexpr int P = kBlock, VN = Vec16<T>::N, NV = P / VN;
-	const uint32_t nb = n / P, tail = n - nb * P;
-	T d = T(0);
-	ready(0u);
-	{
-		T x[P], xn[P];
-		V e[NV], en[NV];
-		if (nb)
-		{
-#pragma unroll
-			for (int q = 0; q < P; q++)
-				x[q] = col[q * kLanes];
-#pragma unroll
-			for (int v = 0; v < NV; v++)
-				e[v] = __ldg(reinterpret_cast<const V*>(eE) + v);
-		}
-		for (uint32_t b = 0; b < nb; b++)
-		{
-			T* blk = col + (uint64_t)b * P * kLanes;
-			if (b + 1 < nb)
-			{
-				if (((b + 1) * P) % R == 0)
-					ready((b + 1) * P / R);
-#pragma unroll
-				for (int q = 0; q < P; q++)
-					xn[q] = blk[(P + q) * kLanes];
-#pragma unroll
-				for (int v = 0; v < NV; v++)
-					en[v] = __ldg(reinterpret_cast<const V*>(eE + (b + 1) * P) + v);
-			}
-#pragma unroll
-			for (int q = 0; q < P; q++)
-			{
-				d = dev::fmadd(vget<V, T>(e[q / VN], q % VN), d, x[q]);
-				blk[q * kLanes] = d;
-			}
-#pragma unroll
-			for (int q = 0; q < P; q++)
-				x[q] = xn[q];
-#pragma unroll
-			for (int v = 0; v < NV; v++)
-				e[v] = en[v];
-		}
-		if (tail && nb && (nb * P) % R == 0)
-			ready(nb * P / R);
-		for (uint32_t j = nb * P; j < n; j++)
-		{
-			d = dev::fmadd(__ldg(eE + j), d, col[(uint64_t)j * kLanes]);
-			col[(uint64_t)j * kLanes] = d;
-		}
-	}
-	d = T(0);
-	for (int j = (int)n - 1; j >= (int)(nb * P); j--)
-	{
-		d = dev::fmadd(c, d, col[(uint64_t)j * kLanes]) * __ldg(eB + j);
-		col[(uint64_t)j * kLanes] = d;
-	}
-	if (tail && (nb * P) % R == 0)
-		done(nb * P / R);
-	{
-		T x[P], xn[P];
-		V bb[NV], bn[NV];
-		if (nb)
-		{
-			const T* blk = col + (uint64_t)(nb - 1) * P * kLanes;
-#pragma unroll
-			for (int q = 0; q < P; q++)
-				x[q] = blk[q * kLanes];
-#pragma unroll
-			for (int v = 0; v < NV; v++)
-				bb[v] = __ldg(reinterpret_cast<const V*>(eB + (nb - 1) * P) + v);
-		}
-		for (int b = (int)nb - 1; b >= 0; b--)
-		{
-			T* blk = col + (uint64_t)b * P * kLanes;
-			if (b > 0)
-			{
-#pragma unroll
-				for (int q = 0; q < P; q++)
-					xn[q] = blk[(q - P) * kLanes];
-#pragma unroll
-				for (int v = 0; v < NV; v++)
-					bn[v] = __ldg(reinterpret_cast<const V*>(eB + (b - 1) * P) + v);
-			}
-#pragma unroll
-			for (int q = P - 1; q >= 0; q--)
-			{
-				d = dev::fmadd(c, d, x[q]) * vget<V, T>(bb[q / VN], q % VN);
-				blk[q * kLanes] = d;
-			}
-			if (((uint32_t)b * P) % R == 0)
-				done((uint32_t)b * P / R);
-#pragma unroll
-			for (int q = 0; q < P; q++)
-				x[q] = xn[q];
-#pragma unroll
-			for (int v = 0; v < NV; v++)
-				bb[v] = bn[v];
-		}
-	}
-}
-
-// One substrate s of a row (stride S in shared memory): the substrate-per-thread
-// mapping of the x sweep, with the same per-step arithmetic as the row solvers.
-template <typename T>
-__device__ __forceinline__ void solve_row_strided(T* row, const T* __restrict__ cB, const T* __restrict__ cE,
-												  const T* __restrict__ cC, uint32_t n, uint32_t S, uint32_t s)
-{
-	constexpr int P = kBlock;
-	T* __restrict__ r = row + s;
-	const T* __restrict__ e = cE + s;
-	const T* __restrict__ b = cB + s;
-	const uint32_t nb = n / P;
-	T d = T(0);
-	for (uint32_t k = 0; k < nb; k++)
-	{
-		T x[P], ee[P];
-#pragma unroll
-		for (int q = 0; q < P; q++)
-		{
-			x[q] = r[(k * P + q) * S];
-			ee[q] = __ldg(e + (k * P + q) * S);
-		}
-#pragma unroll
-		for (int q = 0; q < P; q++)
-		{
-			d = dev::fmadd(ee[q], d, x[q]);
-			r[(k * P + q) * S] = d;
-		}
-	}
-	for (uint32_t i = nb * P; i < n; i++)
-	{
-		d = dev::fmadd(__ldg(e + i * S), d, r[i * S]);
-		r[i * S] = d;
-	}
-	const T c = __ldg(cC + s);
-	d = T(0);
-	for (int i = (int)n - 1; i >= (int)(nb * P); i--)
-	{
-		d = dev::fmadd(c, d, r[i * S]) * __ldg(b + i * S);
-		r[i * S] = d;
-	}
-	for (int k = (int)nb - 1; k >= 0; k--)
-	{
-		T x[P], bb[P];
-#pragma unroll
-		for (int q = 0; q < P; q++)
-		{
-			x[q] = r[(k * P + q) * S];
-			bb[q] = __ldg(b + (k * P + q) * S);
-		}
-#pragma unroll
-		for (int q = P - 1; q >= 0; q--)
-		{
-			d = dev::fmadd(c, d, x[q]) * bb[q];
-			r[(k * P + q) * S] = d;
-		}
-	}
-}
 
 // S*sizeof(T) a multiple of 16 bytes: thread h of a row's TPR threads owns chunk
 // slot h of every x position (VN substrates, VN independent recurrences).

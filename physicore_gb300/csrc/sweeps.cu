@@ -16,9 +16,10 @@
 //    coefficient tables are read through L1 (__ldg, 16-byte vectors), and tile
 //    sizes are chosen so that several CTAs share an SM and all four schedulers
 //    have warps to issue.
-//  * Persistent CTAs (one warp) walk their tiles: a TMA bulk-copy load completes on
-//    an mbarrier, the warp solves the tile in place, and a TMA bulk store writes it
-//    back; the next load is issued as soon as the store has read shared memory.
+//  * Persistent CTAs (one warp) walk their tiles: TMA loads complete on an
+//    mbarrier, the warp solves the tile in place, and TMA stores write it back; the
+//    next load is issued as soon as the stores have read shared memory.  Several
+//    such CTAs per SM overlap one another's loads, compute and stores.
 //  * Solvers run in blocks of P steps without per-step predicates; the next block's
 //    points and coefficients are requested before the current block's dependent
 //    chain, so load latency overlaps the chain.
@@ -41,236 +42,68 @@ using namespace solvers;
 
 // ------------------------------------------------------------------ y / z
 
-// The y/z sweep as a "zipper" pipeline over one shared-memory buffer per CTA.
-//
-// A tile (32 consecutive (x,s) elements at all n points of the lines of one outer
-// index) is split into nc chunks of R points; each chunk moves as one TMA tensor
-// box (32, R) of the field described as the 3-D tensor (x*S+s, y, z).  Chunk c of
-// the CTA's k-th tile sits in slot c when k is even and in slot nc-1-c when k is
-// odd.  Back substitution finishes chunks from the top (c = nc-1 first); each
-// finished chunk is stored, and its slot immediately receives chunk nc-1-c of the
-// next tile -- exactly the chunk order in which that tile's forward elimination
-// will want them.  Loads, stores and both passes therefore overlap inside one
-// buffer, so all shared memory holds line data.  Each slot has an mbarrier that
-// completes once per tile.
+// The y/z sweep.  A tile is 32 consecutive (x,s) elements at all n points of the
+// lines of one outer index; it arrives as nc TMA tensor boxes (32, R) of the field
+// described as the 3-D tensor (x*S+s, y, z), all completing on one mbarrier.  The
+// warp solves the tile in place and stores it back with nc box stores; the next
+// tile's loads start once the stores have read shared memory.  Loads and compute
+// overlap across the several single-warp CTAs an SM holds; within a CTA the solver
+// runs without per-chunk bookkeeping.  Coefficients come from the compressed
+// tables (head rows, then per-substrate constants), so most points need no
+// coefficient load at all.
 template <typename T, int AXIS>
 __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __grid_constant__ CUtensorMap tmap)
 {
-	using V = typename Vec16<T>::type;
-	constexpr int P = kBlock, VN = Vec16<T>::N, NV = P / VN;
 	extern __shared__ __align__(128) unsigned char smem[];
-	const uint32_t n = a.n, S = a.S;
-	const uint32_t R = a.box_rows; // points per chunk, a multiple of P
-	const uint32_t nc = a.boxes;   // chunks per line
-	const uint32_t chunk_elems = R * kLanes;
-	const uint32_t chunk_bytes = chunk_elems * (uint32_t)sizeof(T);
 	uint64_t* full = reinterpret_cast<uint64_t*>(smem);
-	T* base = reinterpret_cast<T*>(smem + round_up(nc * 8, 128));
-	const int lane = threadIdx.x;
-	const T* cB = static_cast<const T*>(a.coef);
-	const T* cE = cB + a.coef_len;
-	const T* cC = cE + a.coef_len;
-	const uint64_t cp = a.coef_len / S; // per-substrate row pitch of the [s][j] tables
-	const uint32_t nb = n / P;          // full blocks; blocks never straddle chunks
-
+	T* base = reinterpret_cast<T*>(smem + 128);
+	const uint32_t lane = threadIdx.x;
+	const uint32_t n = a.n, S = a.S, R = a.box_rows, nc = a.boxes;
+	const uint32_t chunk_elems = R * kLanes;
+	const T* comp = static_cast<const T*>(a.coef) + a.comp_off;
 	if (lane == 0)
 	{
-		for (uint32_t c = 0; c < nc; c++)
-			dev::mbar_init(&full[c], 1);
+		dev::mbar_init(full, 1);
 		dev::fence_mbar_init();
 	}
 	__syncwarp();
-
-	auto coords = [&](uint64_t t, int& x0, int& o) {
-		x0 = (int)((t % a.xblocks) * kLanes);
-		o = (int)(t / a.xblocks);
-	};
-	auto load_chunk = [&](uint64_t t, uint32_t c, uint32_t slot) { // lane 0
-		int x0, o;
-		coords(t, x0, o);
-		dev::mbar_arrive_expect_tx(&full[slot], chunk_bytes);
-		if (AXIS == 1)
-			dev::tma_load_3d(base + slot * chunk_elems, &tmap, x0, (int)(c * R), o, &full[slot]);
-		else
-			dev::tma_load_3d(base + slot * chunk_elems, &tmap, x0, o, (int)(c * R), &full[slot]);
-	};
-	auto store_chunk = [&](uint64_t t, uint32_t c, uint32_t slot) { // lane 0
-		int x0, o;
-		coords(t, x0, o);
-		if (AXIS == 1)
-			dev::tma_store_3d(&tmap, x0, (int)(c * R), o, base + slot * chunk_elems);
-		else
-			dev::tma_store_3d(&tmap, x0, o, (int)(c * R), base + slot * chunk_elems);
-		dev::bulk_commit();
-	};
-
-	uint64_t t = blockIdx.x;
-	if (t < a.tiles && lane == 0)
-		for (uint32_t c = 0; c < nc; c++)
-			load_chunk(t, c, c);
-	const uint32_t BPC = R / P;           // blocks per chunk
-	const uint32_t tail = n - nb * P;     // rows after the last full block (all in the last chunk)
-	const uint32_t blk_elems = P * kLanes;
 	bool ok = true;
-	for (uint32_t k = 0; t < a.tiles && ok; t += gridDim.x, k++)
+	uint32_t phase = 0;
+	for (uint64_t t = blockIdx.x; t < a.tiles; t += gridDim.x, phase ^= 1)
 	{
-		const bool rev = (k & 1) != 0;
-		const uint32_t par = k & 1;
-		const uint64_t tn = t + gridDim.x;
-		const bool has_next = tn < a.tiles;
-		int x0, o;
-		coords(t, x0, o);
-		const uint32_t s = (uint64_t)(x0 + lane) < a.row_len ? (uint32_t)((x0 + lane) % S) : 0;
-		const T* __restrict__ eB = cB + s * cp;
-		const T* __restrict__ eE = cE + s * cp;
-		const T cc = cC[s];
-		// this lane's column of chunk ch (lanes past the row hold zero-filled, never-stored columns)
-		auto chunk_ptr = [&](uint32_t ch) { return base + (rev ? nc - 1 - ch : ch) * chunk_elems + lane; };
-		auto wait_chunk = [&](uint32_t ch) { return dev::mbar_wait(&full[rev ? nc - 1 - ch : ch], par); };
-
-		// ---- forward elimination, block by block; a block never straddles chunks
-		T d = T(0);
-		ok = wait_chunk(0);
-		T* pcur = chunk_ptr(0);
-		uint32_t ch = 0, bin = 0; // chunk and block-in-chunk of pcur
+		const int x0 = (int)((t % a.xblocks) * kLanes);
+		const int o = (int)(t / a.xblocks);
+		if (lane == 0)
 		{
-			T x[P], xn[P];
-			V e[NV], en[NV];
-			const V* ve = reinterpret_cast<const V*>(eE);
-			if (nb)
+			dev::mbar_arrive_expect_tx(full, nc * chunk_elems * (uint32_t)sizeof(T));
+			for (uint32_t c = 0; c < nc; c++)
 			{
-#pragma unroll
-				for (int q = 0; q < P; q++)
-					x[q] = pcur[q * kLanes];
-#pragma unroll
-				for (int v = 0; v < NV; v++)
-					e[v] = __ldg(ve + v);
-			}
-			for (uint32_t b = 0; b < nb; b++)
-			{
-				T* pnext = pcur + blk_elems;
-				if (++bin == BPC)
-				{
-					bin = 0;
-					if (++ch < nc)
-					{
-						ok = ok && wait_chunk(ch);
-						pnext = chunk_ptr(ch);
-					}
-				}
-				if (b + 1 < nb)
-				{
-#pragma unroll
-					for (int q = 0; q < P; q++)
-						xn[q] = pnext[q * kLanes];
-#pragma unroll
-					for (int v = 0; v < NV; v++)
-						en[v] = __ldg(ve + (b + 1) * NV + v);
-				}
-#pragma unroll
-				for (int q = 0; q < P; q++)
-				{
-					d = dev::fmadd(vget<V, T>(e[q / VN], q % VN), d, x[q]);
-					pcur[q * kLanes] = d;
-				}
-				pcur = pnext;
-#pragma unroll
-				for (int q = 0; q < P; q++)
-					x[q] = xn[q];
-#pragma unroll
-				for (int v = 0; v < NV; v++)
-					e[v] = en[v];
-			}
-			// pcur now addresses row nb*P (the tail, inside the last chunk)
-			for (uint32_t j = 0; j < tail; j++)
-			{
-				d = dev::fmadd(__ldg(eE + nb * P + j), d, pcur[j * kLanes]);
-				pcur[j * kLanes] = d;
+				if (AXIS == 1)
+					dev::tma_load_3d(base + c * chunk_elems, &tmap, x0, (int)(c * R), o, full);
+				else
+					dev::tma_load_3d(base + c * chunk_elems, &tmap, x0, o, (int)(c * R), full);
 			}
 		}
+		// lanes past the row hold zero-filled columns that are never stored
+		const uint32_t s = (uint64_t)(x0 + lane) < a.row_len ? (uint32_t)((x0 + lane) % S) : 0;
+		const LineCoef<T> L = line_coef<T>(comp, S, a.head, n, s);
+		ok = __all_sync(0xffffffffu, dev::mbar_wait(full, phase));
 		if (!ok)
 			break;
-
-		// ---- back substitution; finished chunks are stored and their slots refilled
-		int pending = -1; // finished chunk whose slot awaits the next tile's load
-		auto finish_chunk = [&](uint32_t fch) {
-			dev::fence_proxy_async_smem();
-			__syncwarp();
-			if (lane == 0)
-			{
-				store_chunk(t, fch, rev ? nc - 1 - fch : fch);
-				if (has_next && pending >= 0)
-				{
-					dev::bulk_wait_read_allbut1(); // the previous chunk's store has read its slot
-					const uint32_t pc = (uint32_t)pending;
-					load_chunk(tn, nc - 1 - pc, rev ? nc - 1 - pc : pc);
-				}
-			}
-			pending = (int)fch;
-			__syncwarp();
-		};
-		d = T(0);
-		for (int j = (int)tail - 1; j >= 0; j--)
+		solve_line<T, kLanes>(base + lane, n, 0, L);
+		dev::fence_proxy_async_smem();
+		__syncwarp();
+		if (lane == 0)
 		{
-			d = dev::fmadd(cc, d, pcur[j * kLanes]) * __ldg(eB + nb * P + j);
-			pcur[j * kLanes] = d;
-		}
-		if (tail && nb % BPC == 0)
-			finish_chunk(nb / BPC); // the last chunk holds tail rows only
-		if (nb)
-		{
-			ch = (nb - 1) / BPC;
-			bin = (nb - 1) % BPC;
-			pcur = chunk_ptr(ch) + bin * blk_elems;
-			T x[P], xn[P];
-			V bb[NV], bn[NV];
-			const V* vb = reinterpret_cast<const V*>(eB);
-#pragma unroll
-			for (int q = 0; q < P; q++)
-				x[q] = pcur[q * kLanes];
-#pragma unroll
-			for (int v = 0; v < NV; v++)
-				bb[v] = __ldg(vb + (nb - 1) * NV + v);
-			for (int b = (int)nb - 1; b >= 0; b--)
+			for (uint32_t c = 0; c < nc; c++)
 			{
-				T* pnext = bin ? pcur - blk_elems : (ch ? chunk_ptr(ch - 1) + (BPC - 1) * blk_elems : pcur);
-				if (b > 0)
-				{
-#pragma unroll
-					for (int q = 0; q < P; q++)
-						xn[q] = pnext[q * kLanes];
-#pragma unroll
-					for (int v = 0; v < NV; v++)
-						bn[v] = __ldg(vb + (b - 1) * NV + v);
-				}
-#pragma unroll
-				for (int q = P - 1; q >= 0; q--)
-				{
-					d = dev::fmadd(cc, d, x[q]) * vget<V, T>(bb[q / VN], q % VN);
-					pcur[q * kLanes] = d;
-				}
-				if (bin == 0)
-				{
-					finish_chunk(ch);
-					bin = BPC - 1;
-					ch--;
-				}
+				if (AXIS == 1)
+					dev::tma_store_3d(&tmap, x0, (int)(c * R), o, base + c * chunk_elems);
 				else
-					bin--;
-				pcur = pnext;
-#pragma unroll
-				for (int q = 0; q < P; q++)
-					x[q] = xn[q];
-#pragma unroll
-				for (int v = 0; v < NV; v++)
-					bb[v] = bn[v];
+					dev::tma_store_3d(&tmap, x0, o, (int)(c * R), base + c * chunk_elems);
 			}
-		}
-		if (lane == 0 && has_next && pending >= 0)
-		{
+			dev::bulk_commit();
 			dev::bulk_wait_read();
-			const uint32_t pc = (uint32_t)pending;
-			load_chunk(tn, nc - 1 - pc, rev ? nc - 1 - pc : pc);
 		}
 		__syncwarp();
 	}
@@ -282,7 +115,9 @@ __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __g
 
 // ------------------------------------------------------------------ x
 
-// A tile is rows_per_tile consecutive rows; the CTA has rows_per_tile * TPR threads (<= 32).
+// Row-per-thread mapping: a tile is rows_per_tile consecutive rows and the CTA has
+// rows_per_tile * TPR threads (<= 32); TPR threads share a row when its substrates
+// fill whole 16-byte chunks.
 template <typename T, int ST>
 __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 {
@@ -316,11 +151,11 @@ __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 		__syncthreads();
 		if ((uint32_t)tid < nrows)
 			dev::bulk_g2s(tile + tid * a.smem_pitch, g + tid * a.pitch, row_bytes, bar);
-		if (!dev::mbar_wait(bar, phase))
+		if (!__syncthreads_and(dev::mbar_wait(bar, phase)))
 		{
 			if (tid == 0)
 				atomicOr(a.err, DEV_ERR_WAIT_TIMEOUT);
-			return;
+			break;
 		}
 		if ((uint32_t)r_local < nrows)
 		{
@@ -343,6 +178,58 @@ __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 	dev::bulk_wait_all();
 }
 
+// Substrate-per-thread mapping: a tile is rows_per_tile rows and thread
+// (r, s) = (tid / S, tid % S) solves substrate s of row r, a line of n points
+// S elements apart in shared memory, with the compressed coefficients of s (most
+// points need no coefficient load).  Row pitches are chosen so that the lanes of
+// a warp touch distinct banks.
+template <typename T>
+__global__ void __launch_bounds__(kLanes) sweep_x_sub_kernel(SweepArgs a)
+{
+	extern __shared__ __align__(128) unsigned char smem[];
+	uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+	T* tile = reinterpret_cast<T*>(smem + 16);
+	const uint32_t tid = threadIdx.x;
+	const uint32_t R = a.rows_per_tile, S = a.S, n = a.n;
+	const uint32_t r_local = tid / S, s = tid % S;
+	const uint32_t row_bytes = (uint32_t)round_up(a.row_len * sizeof(T), 16);
+	const LineCoef<T> L = line_coef<T>(static_cast<const T*>(a.coef) + a.comp_off, S, a.head, n, s);
+	if (tid == 0)
+	{
+		dev::mbar_init(bar, 1);
+		dev::fence_mbar_init();
+	}
+	__syncthreads();
+	uint32_t phase = 0;
+	for (uint64_t t = blockIdx.x; t < a.tiles; t += gridDim.x, phase ^= 1)
+	{
+		const uint64_t r0 = t * R;
+		const uint32_t nrows = (uint32_t)(a.rows - r0 < (uint64_t)R ? a.rows - r0 : (uint64_t)R);
+		T* g = static_cast<T*>(a.field) + r0 * a.pitch;
+		if (tid == 0)
+			dev::mbar_arrive_expect_tx(bar, nrows * row_bytes);
+		__syncthreads();
+		if (tid < nrows)
+			dev::bulk_g2s(tile + tid * a.smem_pitch, g + tid * a.pitch, row_bytes, bar);
+		if (!__syncthreads_and(dev::mbar_wait(bar, phase)))
+		{
+			if (tid == 0)
+				atomicOr(a.err, DEV_ERR_WAIT_TIMEOUT);
+			break;
+		}
+		if (r_local < nrows)
+			solve_line<T, 0>(tile + r_local * a.smem_pitch + s, n, S, L);
+		dev::fence_proxy_async_smem();
+		__syncthreads();
+		if (tid < nrows)
+			dev::bulk_s2g(g + tid * a.pitch, tile + tid * a.smem_pitch, row_bytes);
+		dev::bulk_commit();
+		dev::bulk_wait_read();
+		__syncthreads();
+	}
+	dev::bulk_wait_all();
+}
+
 struct Plan
 {
 	uint64_t smem;
@@ -354,6 +241,16 @@ template <typename T>
 Plan plan(const Context* c, int axis)
 {
 	Plan p {};
+	if (axis == 0 && x_substrate_mapping(c->S))
+	{
+		const uint64_t row_stage = sweep_x_sub_pitch(c->row_len, c->S, sizeof(T)) * sizeof(T);
+		uint64_t rows = std::min<uint64_t>((kMaxSmemBytes / 4) / row_stage, kLanes / c->S);
+		rows = std::max<uint64_t>(rows, 1);
+		p.rows_per_tile = rows;
+		p.smem = 16 + rows * row_stage;
+		p.threads = (int)(rows * c->S);
+		return p;
+	}
 	if (axis == 0)
 	{
 		const uint64_t row_stage = sweep_x_smem_pitch(c->row_len, c->S, sizeof(T)) * sizeof(T);
@@ -369,7 +266,7 @@ Plan plan(const Context* c, int axis)
 	}
 	uint32_t box_rows, boxes;
 	box_geometry(c->n[axis], box_rows, boxes);
-	p.smem = round_up((uint64_t)boxes * 8, 128) + (uint64_t)boxes * box_rows * kLanes * sizeof(T);
+	p.smem = 128 + (uint64_t)boxes * box_rows * kLanes * sizeof(T);
 	p.threads = kLanes;
 	return p;
 }
@@ -413,13 +310,18 @@ template <typename T>
 int run_sweep_x(Context* c)
 {
 	SweepArgs a = base_args(c, 0);
-	a.smem_pitch = sweep_x_smem_pitch(c->row_len, c->S, sizeof(T));
+	const bool sub = x_substrate_mapping(c->S);
+	a.smem_pitch = sub ? sweep_x_sub_pitch(c->row_len, c->S, sizeof(T)) : sweep_x_smem_pitch(c->row_len, c->S, sizeof(T));
+	a.comp_off = c->coef_comp_off[0];
+	a.head = c->coef_head[0];
 	const Plan p = plan<T>(c, 0);
 	if (p.smem > kMaxSmemBytes)
 		return fail(PCG_ERR_UNSUPPORTED, "x rows too long for the shared-memory x sweep");
 	a.rows_per_tile = (uint32_t)p.rows_per_tile;
 	a.tiles = (c->rows + p.rows_per_tile - 1) / p.rows_per_tile;
 	const double bytes = 2.0 * (double)(c->V * c->S) * (double)sizeof(T);
+	if (sub)
+		return launch_persistent(c, sweep_x_sub_kernel<T>, a, p, K_SWEEP_X, bytes);
 	switch (c->S)
 	{
 	case 1: return launch_persistent(c, sweep_x_kernel<T, 1>, a, p, K_SWEEP_X, bytes);
@@ -454,6 +356,8 @@ int run_sweep_yz(Context* c, int axis)
 	a.tiles *= a.xblocks;
 	a.box_rows = c->tmap_box_rows[axis];
 	a.boxes = c->tmap_boxes[axis];
+	a.comp_off = c->coef_comp_off[axis];
+	a.head = c->coef_head[axis];
 	const Plan p = plan<T>(c, axis);
 	if (p.smem > kMaxSmemBytes)
 		return fail(PCG_ERR_UNSUPPORTED, "lines too long for the shared-memory y/z sweep");
@@ -501,33 +405,15 @@ EncodeTiledFn encode_fn()
 
 // -------------------------------------------------------------------- host side
 
-// Chunk geometry of the y/z zipper: R points per chunk (a multiple of the solver
-// block, at most 256, the TMA box limit).  The first size in order of preference
-// (about 32 points: enough chunks to pipeline, few TMA operations) that pads the
-// line by at most 1/8 wins; otherwise the size with the fewest padded points.
+// Box geometry of a y/z tile: the fewest TMA boxes of at most 256 points (the box
+// limit) that cover a line, each a multiple of the solver block, with the least
+// padding.
 void box_geometry(uint64_t n, uint32_t& box_rows, uint32_t& boxes)
 {
-	static const uint32_t pref[] = { 32, 40, 48, 24, 56, 64, 16, 72, 80, 96, 112, 128, 8, 160, 192, 256 };
-	uint64_t best = ~0ull;
-	for (uint32_t R : pref)
-	{
-		const uint64_t nc = (n + R - 1) / R;
-		const uint64_t rows = nc * R;
-		if ((rows - n) * 8 <= n)
-		{
-			box_rows = R;
-			boxes = (uint32_t)nc;
-			return;
-		}
-		if (rows < best)
-		{
-			best = rows;
-			box_rows = R;
-			boxes = (uint32_t)nc;
-		}
-	}
+	const uint64_t nc = (n + 255) / 256;
+	boxes = (uint32_t)nc;
+	box_rows = (uint32_t)round_up((n + nc - 1) / nc, 8);
 }
-
 
 uint64_t coef_table_len(uint64_t n, uint64_t S, size_t wsize)
 {
@@ -540,6 +426,22 @@ uint64_t coef_row_pitch(uint64_t n) { return round_up(n, kBlock); }
 uint64_t x_threads_per_row(uint64_t S, size_t wsize)
 {
 	return (S <= 8 && (S * wsize) % 16 == 0) ? S * wsize / 16 : 1;
+}
+
+bool x_substrate_mapping(uint64_t S) { return S >= 3 && S <= kLanes; }
+
+// Shared-memory row pitch (elements) of the substrate-per-thread x mapping: whole
+// 16-byte chunks, and rows S elements (rounded up to a chunk) apart modulo the 32
+// banks, so that lane (r, s) of a warp reads bank r*S + s (mod 32) for FP32.
+uint64_t sweep_x_sub_pitch(uint64_t row_len, uint64_t S, size_t wsize)
+{
+	const uint64_t vn = 16 / wsize;
+	const uint64_t mod = 128 / wsize; // elements spanning the 32 banks
+	const uint64_t want = round_up(S, vn) % mod;
+	uint64_t p = round_up(row_len, vn);
+	while (p % mod != want)
+		p += vn;
+	return p;
 }
 
 uint64_t sweep_x_smem_pitch(uint64_t row_len, uint64_t S, size_t wsize)
@@ -555,7 +457,7 @@ uint64_t sweep_x_smem_pitch(uint64_t row_len, uint64_t S, size_t wsize)
 	return chunks * vn;
 }
 
-int encode_field_map(const Context* c, int axis, uint32_t box_rows, CUtensorMap* out)
+int encode_field_map(const Context* c, int axis, uint32_t box_rows, CUtensorMap* out, uint32_t box_cols)
 {
 	EncodeTiledFn enc = encode_fn();
 	if (!enc)
@@ -564,7 +466,7 @@ int encode_field_map(const Context* c, int axis, uint32_t box_rows, CUtensorMap*
 	const cuuint64_t strides[2] = { c->pitch * c->wsize, c->n[1] * c->pitch * c->wsize };
 	const cuuint32_t estr[3] = { 1, 1, 1 };
 	const CUtensorMapDataType dt = c->wsize == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
-	const cuuint32_t box[3] = { (cuuint32_t)kLanes, axis == 1 ? box_rows : 1u, axis == 2 ? box_rows : 1u };
+	const cuuint32_t box[3] = { box_cols, axis == 1 ? box_rows : 1u, axis == 2 ? box_rows : 1u };
 	CUresult r = enc(out, dt, 3, c->field.ptr, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
 					 CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 	if (r != CUDA_SUCCESS)

@@ -12,6 +12,13 @@ Named workloads restate the benchmark configurations of this backend:
                 plus 10,000 interior voxels, 1,000,000 agents
   dense_200     200^3 voxels, 4 substrates, 4,000,000 agents from a Gaussian
                 cluster (sigma 200 um) at the domain centre
+  batched_256   256 independent domains, each side log-uniform in [32, 160] voxels
+                per axis, 1-6 substrates, 100-50,000 agents (log-uniform), with the
+                per-domain recipe of large_320 (D, decay, field, x-face Dirichlet,
+                interior nodes at the same density)
+  served        a Poisson request stream of independent simulations (sides
+                log-uniform [32, 256] per axis, 1-8 substrates, 0-200,000 agents,
+                10-1,000 steps log-uniform)
 A problem is a plain dict; `apply(solver, problem)` feeds it to any object with
 the Solver call surface (physicore_gb300.Solver or the oracle).
 """
@@ -184,3 +191,43 @@ def _takes_layout(solver):
         return "layout" in inspect.signature(solver.set_field).parameters
     except (TypeError, ValueError):
         return False
+
+
+def _domain(rng, name, sides, S, A, interior_density=1e4 / 320 ** 3):
+    """One 3-D domain with the per-domain recipe of large_320."""
+    nx, ny, nz = sides
+    ext = [n * VOXEL for n in sides]
+    D = log_uniform(rng, 10.0, 1e5, S)
+    decay = log_uniform(rng, 1e-4, 1.0, S)
+    field = rng.random((S, nz, ny, nx), dtype=np.float32)
+    faces = [(0, side, rng.random(S), [1] * S) for side in (0, 1)]
+    V = nx * ny * nz
+    K = int(round(V * interior_density))
+    inter = None
+    if K:
+        lin = np.unique(rng.integers(0, V, K))
+        vox = np.stack([lin % nx, (lin // nx) % ny, lin // (nx * ny)], axis=1).astype(np.uint64)
+        inter = (vox, rng.random((vox.shape[0], S)), np.ones((vox.shape[0], S), np.uint8))
+    pos = uniform_positions(rng, A, 3, np.zeros(3), np.array(ext, dtype=np.float64))
+    return dict(name=name, dims=3, bbmin=(0, 0, 0), bbmax=tuple(ext), voxel=(VOXEL,) * 3, dt=0.01, D=D,
+                decay=decay, initial=np.zeros(S), field=field, field_layout="planar", boundary=faces,
+                interior=inter, bulk=None, agents=agents_block(rng, A, S, pos), compute_internalized=True)
+
+
+def batched_sizes(seed=3, count=256, side_lo=32, side_hi=160, S_hi=6, agents_lo=100, agents_hi=50_000):
+    """(sides, S, agents) of the batched workload's domains, without their arrays."""
+    rng = _rng(seed)
+    out = []
+    for _ in range(count):
+        sides = tuple(int(round(v)) for v in log_uniform(rng, side_lo, side_hi, 3))
+        S = int(rng.integers(1, S_hi + 1))
+        A = int(round(float(log_uniform(rng, agents_lo, agents_hi))))
+        out.append((sides, S, A))
+    return out
+
+
+def batched_uneven(seed=3, count=256, **kw):
+    """Yields the batched workload's domains one at a time (their fields are large
+    together: about 1.8 GB of FP32 for 256 domains)."""
+    for i, (sides, S, A) in enumerate(batched_sizes(seed, count, **kw)):
+        yield _domain(_rng((seed, i)), f"batched_{i}", sides, S, A)
