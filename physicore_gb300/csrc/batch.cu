@@ -121,6 +121,23 @@ __device__ __forceinline__ uint32_t find_entry(const WorkList& l, uint64_t u)
 	return lo;
 }
 
+// find_entry for the 32 lanes of a warp holding ascending units (all lanes must
+// call it): lane 0 searches once and the others step forward from its entry,
+// usually not at all, since consecutive units rarely cross a domain.  Units past
+// the list's end map to its last entry.
+__device__ __forceinline__ uint32_t warp_entry(const WorkList& l, uint64_t u)
+{
+	const uint64_t uc = u < l.total ? u : l.total - 1;
+	const uint64_t u0 = __shfl_sync(0xffffffffu, uc, 0);
+	uint32_t k = 0;
+	if ((threadIdx.x & 31) == 0)
+		k = find_entry(l, u0);
+	k = __shfl_sync(0xffffffffu, k, 0);
+	while (k + 1 < l.count && __ldg(l.base + k + 1) <= uc)
+		k++;
+	return k;
+}
+
 __device__ __forceinline__ void report(const BatchArgs& b, uint32_t bits, uint32_t d)
 {
 	atomicOr(b.err, bits);
@@ -368,6 +385,11 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 			const LineCoef<T> L = line_coef<T>(static_cast<const T*>(D.coef[AXIS]) + D.coef_comp_off[AXIS], S,
 											   D.coef_head[AXIS], n, s);
 			solve_line<T, kLanes>(base + lane, n, 0, L);
+			// the last sweep of the domain writes its boundary faces (the batch's
+			// Dirichlet launch then covers interior nodes and 1-D domains only)
+			if (D.dims == AXIS + 1)
+				fielddev::faces_on_column<T, AXIS>(D.faces, base + lane, n, kLanes, (uint64_t)x0 + lane,
+												   (uint64_t)o);
 		}
 		dev::fence_proxy_async_smem();
 		__syncwarp();
@@ -393,24 +415,33 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 
 // ------------------------------------------------------------------ Dirichlet, bulk
 
+// Grid-stride loops below step whole warps together (a warp's first unit decides),
+// so that every lane takes part in warp_entry.
 template <typename T>
 __global__ void batch_faces_kernel(BatchArgs b)
 {
-	for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < b.list.total;
-		 u += (uint64_t)gridDim.x * blockDim.x)
+	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+	const uint64_t w0 = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u);
+	for (uint64_t wu = w0; wu < b.list.total; wu += stride)
 	{
-		const uint32_t k = find_entry(b.list, u);
-		fielddev::face_item<T>(b.doms[__ldg(b.list.dom + k)].faces, u - __ldg(b.list.base + k));
+		const uint64_t u = wu + (threadIdx.x & 31);
+		const uint32_t k = warp_entry(b.list, u);
+		if (u < b.list.total)
+			fielddev::face_item<T>(b.doms[__ldg(b.list.dom + k)].faces, u - __ldg(b.list.base + k));
 	}
 }
 
 template <typename T>
 __global__ void batch_interior_kernel(BatchArgs b)
 {
-	for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < b.list.total;
-		 u += (uint64_t)gridDim.x * blockDim.x)
+	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+	const uint64_t w0 = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u);
+	for (uint64_t wu = w0; wu < b.list.total; wu += stride)
 	{
-		const uint32_t k = find_entry(b.list, u);
+		const uint64_t u = wu + (threadIdx.x & 31);
+		const uint32_t k = warp_entry(b.list, u);
+		if (u >= b.list.total)
+			continue;
 		const BatchDomain& D = b.doms[__ldg(b.list.dom + k)];
 		const uint64_t i = u - __ldg(b.list.base + k);
 		if (D.dir_conds[i])
@@ -427,7 +458,7 @@ __global__ void batch_bulk_kernel(BatchArgs b)
 	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
 	for (uint64_t u = warp; u < b.list.total; u += nwarps)
 	{
-		const uint32_t k = find_entry(b.list, u);
+		const uint32_t k = warp_entry(b.list, u);
 		const BatchDomain& D = b.doms[__ldg(b.list.dom + k)];
 		const uint64_t r = u - __ldg(b.list.base + k);
 		const T* sp = static_cast<const T*>(D.bulk[0]);
@@ -453,7 +484,7 @@ __global__ void batch_clear_counts_kernel(BatchArgs b)
 	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
 	for (uint64_t u = warp; u < b.list.total; u += nwarps)
 	{
-		const uint32_t k = find_entry(b.list, u);
+		const uint32_t k = warp_entry(b.list, u);
 		const uint32_t di = __ldg(b.list.dom + k);
 		if (!b.recompute[di])
 			continue;
@@ -470,9 +501,9 @@ template <typename T>
 __global__ void batch_cells_locate_kernel(BatchArgs b)
 {
 	const uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+	const uint32_t k = warp_entry(b.list, u);
 	if (u >= b.list.total)
 		return;
-	const uint32_t k = find_entry(b.list, u);
 	const uint32_t di = __ldg(b.list.dom + k);
 	if (!b.recompute[di])
 		return;
@@ -490,9 +521,9 @@ __global__ void batch_cells_ballot_kernel(BatchArgs b)
 	uint64_t key = ~0ull;
 	uint32_t v = kNoAgent, di = 0;
 	uint64_t i = 0;
+	const uint32_t k = warp_entry(b.list, u);
 	if (u < b.list.total)
 	{
-		const uint32_t k = find_entry(b.list, u);
 		di = __ldg(b.list.dom + k);
 		if (b.recompute[di])
 		{
@@ -520,9 +551,9 @@ __global__ void batch_cells_reduce_kernel(BatchArgs b)
 	const uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	bool conflict = false;
 	uint32_t di = 0;
+	const uint32_t k = warp_entry(b.list, u);
 	if (u < b.list.total)
 	{
-		const uint32_t k = find_entry(b.list, u);
 		di = __ldg(b.list.dom + k);
 		if (b.recompute[di])
 		{
@@ -541,9 +572,9 @@ template <typename T>
 __global__ void batch_cells_apply_kernel(BatchArgs b)
 {
 	const uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+	const uint32_t k = warp_entry(b.list, u);
 	if (u >= b.list.total)
 		return;
-	const uint32_t k = find_entry(b.list, u);
 	agent_apply<T>(b.doms[__ldg(b.list.dom + k)].cells, u - __ldg(b.list.base + k));
 }
 
@@ -551,9 +582,9 @@ template <typename T>
 __global__ void batch_cells_internalize_kernel(BatchArgs b)
 {
 	const uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+	const uint32_t k = warp_entry(b.list, u);
 	if (u >= b.list.total)
 		return;
-	const uint32_t k = find_entry(b.list, u);
 	const CellArgs& a = b.doms[__ldg(b.list.dom + k)].cells;
 	if (a.internalized)
 		agent_internalize<T>(a, u - __ldg(b.list.base + k));
@@ -808,7 +839,7 @@ void list_units(pcg_batch* b, int id, size_t d, uint64_t& units, double& cost)
 		if (c->dims >= 3)
 			units = D.yz_xblocks * c->n[1], cost = (double)c->n[2];
 		break;
-	case L_FACES: units = D.faces.face_mask ? D.faces.total * c->S : 0; break;
+	case L_FACES: units = (D.faces.face_mask && c->dims == 1) ? D.faces.total * c->S : 0; break; // else fused
 	case L_INTERIOR: units = c->K * c->S; break;
 	case L_BULK: units = c->bulk_mode != PCG_BULK_NONE ? c->rows : 0; break;
 	case L_CLEAR: units = c->A ? (c->V + kClearChunk - 1) / kClearChunk : 0; break;
@@ -1013,7 +1044,7 @@ int build_t(pcg_batch* b)
 		for (int a = 0; a < c->dims; a++)
 			b->step_bytes[K_SWEEP_X + a] += 2.0 * V * S * w;
 		const FaceArgs& f = b->h_doms[d].faces;
-		if (f.face_mask)
+		if (f.face_mask && c->dims == 1) // otherwise written by the last sweep
 			b->step_bytes[K_DIRICHLET_FACES] += (double)f.total * S * w;
 		b->step_bytes[K_DIRICHLET_INTERIOR] += (double)c->K * (8 + S * (2 * w + 1));
 		if (c->bulk_mode != PCG_BULK_NONE)

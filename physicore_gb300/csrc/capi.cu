@@ -358,16 +358,20 @@ static int upload_bulk(Context* c)
 static int run_phases(Context* c, uint32_t phases, bool recompute)
 {
 	int rc;
+	// with both phases in this call, the last sweep writes the boundary faces into
+	// its tiles before storing them (the reference's next step, dirichlet_solver.cpp:
+	// 59-83), which saves a pass of scattered writes
+	const bool fuse = (phases & PCG_PHASE_DIFFUSION) && (phases & PCG_PHASE_DIRICHLET) && faces_fusable(c);
 	if (phases & PCG_PHASE_DIFFUSION)
 	{
 		if ((rc = launch_sweep_x(c)))
 			return rc;
-		if (c->dims >= 2 && (rc = launch_sweep_yz(c, 1)))
+		if (c->dims >= 2 && (rc = launch_sweep_yz(c, 1, fuse && c->dims == 2)))
 			return rc;
-		if (c->dims >= 3 && (rc = launch_sweep_yz(c, 2)))
+		if (c->dims >= 3 && (rc = launch_sweep_yz(c, 2, fuse)))
 			return rc;
 	}
-	if ((phases & PCG_PHASE_DIRICHLET) && (rc = launch_dirichlet(c)))
+	if ((phases & PCG_PHASE_DIRICHLET) && (rc = launch_dirichlet(c, fuse)))
 		return rc;
 	if ((phases & PCG_PHASE_BULK) && (rc = launch_bulk(c)))
 		return rc;
@@ -504,6 +508,8 @@ int pcg_create(pcg_context** out, int precision, int device)
 	int rc = pcg::dalloc(c, c->err, sizeof(uint32_t) * 4);
 	if (!rc)
 		rc = pcg::dalloc(c, c->flags, sizeof(uint32_t) * 4);
+	if (rc == PCG_OK)
+		rc = pcg::dalloc(c, c->tickets, sizeof(uint32_t) * 4);
 	if (rc)
 	{
 		pcg_destroy(c);
@@ -524,7 +530,7 @@ int pcg_destroy(pcg_context* c)
 		cudaStreamSynchronize(c->stream);
 	pcg::collect_timings(c);
 	pcg::DeviceBuffer* all[] = { &c->field,		 &c->coef[0],	&c->coef[1],	&c->coef[2],	 &c->a_vox,
-								 &c->err,		&c->flags,		 &c->mass,
+								 &c->err,		&c->flags,		 &c->mass,		&c->tickets,
 								 &c->staging,	 &c->dir_offsets, &c->dir_values, &c->dir_conds, &c->face_values,
 								 &c->face_conds, &c->bulk[0],	&c->bulk[1],	&c->bulk[2],	 &c->a_pos,
 								 &c->a_sec,		 &c->a_sat,		&c->a_upt,		&c->a_net,		 &c->a_vol,

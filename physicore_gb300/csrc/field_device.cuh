@@ -133,6 +133,51 @@ __device__ __forceinline__ void bulk_row(T* field, const T* supply, const T* upt
 	}
 }
 
+// The boundary faces of the voxels of one solved y/z column in shared memory (the
+// last sweep of the step, so these are the values the reference's Dirichlet pass
+// would write next).  The column is element c = x*S + s of a row at all n points
+// of the swept axis (stride `stride`); `o` is the index along the third axis.
+// Faces apply in the reference's order x-min, x-max, y-min, y-max, z-min, z-max,
+// a later face winning: first the faces whose plane holds the whole column, then
+// the two faces of the swept axis at its ends.
+template <typename T, int AXIS>
+__device__ __forceinline__ void faces_on_column(const FaceArgs& f, T* col, uint32_t n, uint32_t stride, uint64_t c,
+												uint64_t o)
+{
+	if (!f.face_mask || c >= f.nx * f.S)
+		return;
+	const T* vals = static_cast<const T*>(f.values);
+	const uint32_t s = (uint32_t)(c % f.S);
+	const uint64_t x = c / f.S;
+	bool has = false;
+	T v = T(0);
+	auto take = [&](int fi) {
+		if (((f.face_mask >> fi) & 1u) && f.conds[fi * f.S + s])
+		{
+			v = vals[fi * f.S + s];
+			has = true;
+		}
+	};
+	if (x == 0)
+		take(0);
+	if (x == f.nx - 1)
+		take(1);
+	const uint64_t n_other = AXIS == 2 ? f.ny : f.nz; // the axis that is neither x nor swept
+	const int f_other = AXIS == 2 ? 2 : 4;
+	if (o == 0)
+		take(f_other);
+	if (o == n_other - 1)
+		take(f_other + 1);
+	if (has)
+		for (uint32_t j = 0; j < n; j++)
+			col[(uint64_t)j * stride] = v;
+	const int f_swept = AXIS == 2 ? 4 : 2;
+	if (((f.face_mask >> f_swept) & 1u) && f.conds[f_swept * f.S + s])
+		col[0] = vals[f_swept * f.S + s];
+	if (((f.face_mask >> (f_swept + 1)) & 1u) && f.conds[(f_swept + 1) * f.S + s])
+		col[(uint64_t)(n - 1) * stride] = vals[(f_swept + 1) * f.S + s];
+}
+
 } // namespace fielddev
 #endif
 

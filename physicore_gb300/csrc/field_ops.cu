@@ -135,10 +135,10 @@ unsigned grid_for(const Context* c, uint64_t work, unsigned block)
 } // namespace
 
 template <typename T>
-static int run_dirichlet(Context* c)
+static int run_dirichlet(Context* c, bool faces_done)
 {
 	const FaceArgs a = make_face_args(c);
-	if (a.face_mask)
+	if (a.face_mask && !faces_done)
 	{
 		cudaEvent_t ev;
 		launch_begin(c, K_DIRICHLET_FACES, (double)(a.total * c->S * sizeof(T)), &ev);
@@ -159,7 +159,10 @@ static int run_dirichlet(Context* c)
 	return PCG_OK;
 }
 
-int launch_dirichlet(Context* c) { return c->wsize == 4 ? run_dirichlet<float>(c) : run_dirichlet<double>(c); }
+int launch_dirichlet(Context* c, bool faces_done)
+{
+	return c->wsize == 4 ? run_dirichlet<float>(c, faces_done) : run_dirichlet<double>(c, faces_done);
+}
 
 template <typename T>
 static int run_bulk(Context* c)

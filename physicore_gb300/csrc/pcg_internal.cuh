@@ -73,6 +73,7 @@ constexpr int kStages = 2;           // shared-memory ring depth of the persiste
 constexpr uint64_t kMaxSmemBytes = 227 * 1024;
 constexpr uint64_t kCoefSmemLimit = 64 * 1024; // larger coefficient tables stay in global memory
 constexpr uint64_t kBlockPoints = 8;           // line points per pipelined solver block
+constexpr uint64_t kXTileBytes = 32 * 1024;    // shared memory of a substrate-mapped x tile
 
 __host__ __device__ constexpr uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
 __host__ __device__ constexpr int gcd_i(int a, int b) { return b == 0 ? a : gcd_i(b, a % b); }
@@ -108,6 +109,14 @@ struct SweepArgs
 	uint64_t smem_pitch;  // shared-memory row pitch (elements); in 16-byte chunks == threads per row (mod 8)
 	uint32_t rows_per_tile;
 	uint32_t* err;
+	uint32_t* ticket; // tile counter of the launch (zeroed before it), tiles handed out in order
+	// y/z, last sweep of a step that also applies Dirichlet: the boundary faces
+	// are written into each solved tile before it is stored (FaceArgs in
+	// field_device.cuh); face_mask 0 when not fused
+	const void* face_values;
+	const uint8_t* face_conds;
+	uint32_t face_mask;
+	uint64_t nx, ny, nz;
 };
 
 // ------------------------------------------------------------------ context
@@ -175,6 +184,7 @@ struct Context
 	uint64_t coef_comp_off[3] = { 0, 0, 0 }; // compressed tables (head rows, constants)
 	uint32_t coef_head[3] = { 0, 0, 0 };     // head points per substrate of the compressed tables
 	DeviceBuffer err;      // uint32 device error word
+	DeviceBuffer tickets;  // uint32 [4]: tile counters of the persistent sweeps
 	DeviceBuffer flags;    // uint32 [4]: [0] ballot conflict
 	DeviceBuffer mass;     // double [S]
 	DeviceBuffer staging;  // layout conversion
@@ -232,8 +242,11 @@ void collect_timings(Context* c);
 // ------------------------------------------------------------------ kernel launchers (defined in .cu files)
 
 int launch_sweep_x(Context* c);
-int launch_sweep_yz(Context* c, int axis);
-int launch_dirichlet(Context* c);
+int launch_sweep_yz(Context* c, int axis, bool fuse_faces = false);
+// Dirichlet faces (unless the last sweep already wrote them) and interior nodes
+int launch_dirichlet(Context* c, bool faces_done = false);
+// true when the last sweep of c can apply the boundary faces itself
+bool faces_fusable(const Context* c);
 int launch_bulk(Context* c);
 int launch_cells(Context* c, bool recompute);
 int launch_release(Context* c, uint64_t agent);

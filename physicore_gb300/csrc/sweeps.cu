@@ -31,6 +31,7 @@
 //    voxel's substrates fill whole chunks, TPR threads share a row, one chunk slot
 //    each; rows are TPR (mod 8) chunks apart so quarter-warps hit distinct banks.
 //  * Every wait is bounded; a timeout sets a device error bit instead of trapping.
+#include "field_device.cuh"
 #include "pcg_internal.cuh"
 #include "sweep_solvers.cuh"
 
@@ -68,9 +69,14 @@ __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __g
 	}
 	__syncwarp();
 	bool ok = true;
-	uint32_t phase = 0;
-	for (uint64_t t = blockIdx.x; t < a.tiles; t += gridDim.x, phase ^= 1)
+	for (uint32_t phase = 0;; phase ^= 1)
 	{
+		uint32_t t32 = 0;
+		if (lane == 0)
+			t32 = atomicAdd(a.ticket, 1u);
+		const uint64_t t = __shfl_sync(0xffffffffu, t32, 0);
+		if (t >= a.tiles)
+			break;
 		const int x0 = (int)((t % a.xblocks) * kLanes);
 		const int o = (int)(t / a.xblocks);
 		if (lane == 0)
@@ -91,6 +97,16 @@ __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __g
 		if (!ok)
 			break;
 		solve_line<T, kLanes>(base + lane, n, 0, L);
+		if (a.face_mask)
+		{
+			FaceArgs f {};
+			f.values = a.face_values;
+			f.conds = a.face_conds;
+			f.face_mask = a.face_mask;
+			f.S = S;
+			f.nx = a.nx, f.ny = a.ny, f.nz = a.nz;
+			fielddev::faces_on_column<T, AXIS>(f, base + lane, n, kLanes, (uint64_t)x0 + lane, (uint64_t)o);
+		}
 		dev::fence_proxy_async_smem();
 		__syncwarp();
 		if (lane == 0)
@@ -124,6 +140,7 @@ __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 	constexpr int TPR = x_tpr<T, ST>();
 	extern __shared__ __align__(128) unsigned char smem[];
 	uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+	uint32_t& ticket = *reinterpret_cast<uint32_t*>(smem + 8);
 	T* tile = reinterpret_cast<T*>(smem + 16);
 	const int tid = threadIdx.x;
 	const uint32_t R = a.rows_per_tile;
@@ -140,9 +157,14 @@ __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 	}
 	__syncthreads();
 
-	uint32_t phase = 0;
-	for (uint64_t t = blockIdx.x; t < a.tiles; t += gridDim.x, phase ^= 1)
+	for (uint32_t phase = 0;; phase ^= 1)
 	{
+		if (tid == 0)
+			ticket = atomicAdd(a.ticket, 1u);
+		__syncthreads();
+		const uint64_t t = ticket;
+		if (t >= a.tiles)
+			break;
 		const uint64_t r0 = t * R;
 		const uint32_t nrows = (uint32_t)(a.rows - r0 < (uint64_t)R ? a.rows - r0 : (uint64_t)R);
 		T* g = static_cast<T*>(a.field) + r0 * a.pitch;
@@ -188,6 +210,7 @@ __global__ void __launch_bounds__(kLanes) sweep_x_sub_kernel(SweepArgs a)
 {
 	extern __shared__ __align__(128) unsigned char smem[];
 	uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+	uint32_t& ticket = *reinterpret_cast<uint32_t*>(smem + 8);
 	T* tile = reinterpret_cast<T*>(smem + 16);
 	const uint32_t tid = threadIdx.x;
 	const uint32_t R = a.rows_per_tile, S = a.S, n = a.n;
@@ -200,9 +223,14 @@ __global__ void __launch_bounds__(kLanes) sweep_x_sub_kernel(SweepArgs a)
 		dev::fence_mbar_init();
 	}
 	__syncthreads();
-	uint32_t phase = 0;
-	for (uint64_t t = blockIdx.x; t < a.tiles; t += gridDim.x, phase ^= 1)
+	for (uint32_t phase = 0;; phase ^= 1)
 	{
+		if (tid == 0)
+			ticket = atomicAdd(a.ticket, 1u);
+		__syncthreads();
+		const uint64_t t = ticket;
+		if (t >= a.tiles)
+			break;
 		const uint64_t r0 = t * R;
 		const uint32_t nrows = (uint32_t)(a.rows - r0 < (uint64_t)R ? a.rows - r0 : (uint64_t)R);
 		T* g = static_cast<T*>(a.field) + r0 * a.pitch;
@@ -244,11 +272,12 @@ Plan plan(const Context* c, int axis)
 	if (axis == 0 && x_substrate_mapping(c->S))
 	{
 		const uint64_t row_stage = sweep_x_sub_pitch(c->row_len, c->S, sizeof(T)) * sizeof(T);
-		uint64_t rows = std::min<uint64_t>((kMaxSmemBytes / 4) / row_stage, kLanes / c->S);
+		// ~32 KB tiles: more CTAs (warps) per SM beat fuller warps here
+		uint64_t rows = std::min<uint64_t>(kXTileBytes / row_stage, kLanes / c->S);
 		rows = std::max<uint64_t>(rows, 1);
 		p.rows_per_tile = rows;
 		p.smem = 16 + rows * row_stage;
-		p.threads = (int)(rows * c->S);
+		p.threads = kLanes; // lanes past rows * S idle
 		return p;
 	}
 	if (axis == 0)
@@ -282,6 +311,7 @@ int launch_persistent(Context* c, KernelT kernel, const SweepArgs& a, const Plan
 	uint64_t grid = (uint64_t)per_sm * (uint64_t)c->sm_count;
 	if (grid > a.tiles)
 		grid = a.tiles;
+	PCG_CUDA_TRY(cudaMemsetAsync(a.ticket, 0, sizeof(uint32_t), c->stream));
 	cudaEvent_t ev;
 	launch_begin(c, kid, bytes, &ev);
 	kernel<<<(unsigned)grid, p.threads, p.smem, c->stream>>>(a);
@@ -303,6 +333,7 @@ SweepArgs base_args(const Context* c, int axis)
 	a.pitch = c->pitch;
 	a.rows = c->rows;
 	a.err = static_cast<uint32_t*>(c->err.ptr);
+	a.ticket = static_cast<uint32_t*>(c->tickets.ptr) + axis;
 	return a;
 }
 
@@ -337,9 +368,17 @@ int run_sweep_x(Context* c)
 }
 
 template <typename T>
-int run_sweep_yz(Context* c, int axis)
+int run_sweep_yz(Context* c, int axis, bool fuse_faces)
 {
 	SweepArgs a = base_args(c, axis);
+	if (fuse_faces)
+	{
+		const FaceArgs f = make_face_args(c);
+		a.face_values = f.values;
+		a.face_conds = f.conds;
+		a.face_mask = f.face_mask;
+		a.nx = c->n[0], a.ny = c->n[1], a.nz = c->n[2];
+	}
 	if (axis == 1)
 	{
 		a.line_stride = c->pitch;
@@ -374,6 +413,7 @@ int run_sweep_yz(Context* c, int axis)
 	uint64_t grid = (uint64_t)per_sm * (uint64_t)c->sm_count;
 	if (grid > a.tiles)
 		grid = a.tiles;
+	PCG_CUDA_TRY(cudaMemsetAsync(a.ticket, 0, sizeof(uint32_t), c->stream));
 	cudaEvent_t ev;
 	launch_begin(c, kid, bytes, &ev);
 	kernel<<<(unsigned)grid, p.threads, p.smem, c->stream>>>(a, c->tmap[axis]);
@@ -497,9 +537,11 @@ uint64_t sweep_smem_bytes(const Context* c, int axis)
 
 int launch_sweep_x(Context* c) { return c->wsize == 4 ? run_sweep_x<float>(c) : run_sweep_x<double>(c); }
 
-int launch_sweep_yz(Context* c, int axis)
+int launch_sweep_yz(Context* c, int axis, bool fuse_faces)
 {
-	return c->wsize == 4 ? run_sweep_yz<float>(c, axis) : run_sweep_yz<double>(c, axis);
+	return c->wsize == 4 ? run_sweep_yz<float>(c, axis, fuse_faces) : run_sweep_yz<double>(c, axis, fuse_faces);
 }
+
+bool faces_fusable(const Context* c) { return c->dims >= 2; }
 
 } // namespace pcg
