@@ -135,6 +135,10 @@ int pcg_set_internalized(pcg_context* ctx, const double* internalized);
  * conditions, precomputes the Thomas coefficients in FP64
  * (openmp_solver.cpp:8-21, diffusion_solver.cpp:29-113).  Idempotent. */
 int pcg_initialize(pcg_context* ctx);
+/* Device memory the context will hold once initialised (field, tables, agents and
+ * their scratch, transfer staging), for admission control.  Before initialize a
+ * context holds no device memory: agents set earlier are staged on the host. */
+int pcg_estimate_device_bytes(pcg_context* ctx, uint64_t* bytes);
 /* solver::solve(m, iterations) (openmp_solver.cpp:23-40): diffusion x->y->z,
  * Dirichlet, bulk, cells per iteration; ballots are rebuilt during every
  * iteration of a call that follows initialize or pcg_recompute_positional_data. */
@@ -230,6 +234,73 @@ int pcg_batch_get_kernel_stats(pcg_batch* batch, pcg_kernel_stat* stats, uint64_
 int pcg_batch_reset_kernel_stats(pcg_batch* batch);
 /* Kernels launched by this batch (graph replays count their kernels). */
 int pcg_batch_get_launch_count(pcg_batch* batch, uint64_t* launches);
+
+/* ---- serving: continuous batching of independent simulations ------------- */
+
+/* No counterpart in the reference, which runs one simulation per process.  A
+ * server owns a worker thread that admits requests by free device memory, keeps
+ * them resident, steps all admitted ones together through one batch (regrouped
+ * between ticks as requests finish and arrive), and hands finished ones back.
+ *  - A request is a context configured with the setters but NOT initialised (it
+ *    holds no device memory yet: agents set before initialize are staged on the
+ *    host); the server initialises it on admission.  From submit until it comes
+ *    back from pcg_server_poll the server owns it: do not call into it meanwhile.
+ *  - A returned context holds its results (read them with pcg_get_field etc.)
+ *    and its device memory until the caller destroys it, so poll and destroy
+ *    promptly: the memory of finished requests is what later admissions use.
+ *  - Admission: requests are taken in arrival order while the next one's device
+ *    bytes (pcg_estimate_device_bytes) plus reserve_bytes fit in free memory;
+ *    while active requests hold memory a request waits; one that cannot fit with
+ *    nothing active is refused.  memory_limit_bytes (0: the device's free memory)
+ *    caps the memory the server may use. */
+typedef struct pcg_server pcg_server;
+
+typedef struct pcg_server_options
+{
+	uint64_t max_active;         /* simulations stepped together (0: 1024) */
+	uint64_t steps_per_tick;     /* steps between admission points (0: 8) */
+	uint64_t reserve_bytes;      /* free memory kept back at admission */
+	uint64_t max_queue;          /* queued requests before submissions are refused (0: 2^20) */
+	uint64_t memory_limit_bytes; /* 0: use the device's free memory */
+	int autotune;                /* autotune new size buckets when the batch is regrouped */
+} pcg_server_options;
+
+#define PCG_REQUEST_DONE 0
+#define PCG_REQUEST_CANCELLED 1
+#define PCG_REQUEST_REFUSED 2
+#define PCG_REQUEST_FAILED 3
+
+typedef struct pcg_server_result
+{
+	pcg_context* ctx;
+	uint64_t tag;
+	uint64_t steps;
+	int status;               /* PCG_REQUEST_* */
+	int code;                 /* PCG_ERR_* behind a refusal or failure */
+	double t_submit, t_admit, t_done; /* seconds since the server started; t_admit < 0: never admitted */
+	uint64_t device_bytes;    /* estimate used for admission */
+	char error[160];
+} pcg_server_result;
+
+typedef struct pcg_server_stats
+{
+	uint64_t submitted, admitted, completed, cancelled, refused, failed;
+	uint64_t ticks, rebuilds, steps;
+	uint64_t vss;            /* voxel-substrate-steps performed */
+	uint64_t active_bytes;   /* device bytes of the admitted set */
+	uint64_t queued, active, in_flight;
+	double uptime_s;
+} pcg_server_stats;
+
+int pcg_server_create(pcg_server** out, int precision, int device, const pcg_server_options* options);
+/* Stops the worker; contexts the server still holds are destroyed. */
+int pcg_server_destroy(pcg_server* server);
+int pcg_server_submit(pcg_server* server, pcg_context* request, uint64_t steps, uint64_t tag);
+/* Cancels a queued or running request (it comes back with PCG_REQUEST_CANCELLED). */
+int pcg_server_cancel(pcg_server* server, uint64_t tag);
+/* Up to `cap` finished requests; waits up to wait_ms for the first. */
+int pcg_server_poll(pcg_server* server, pcg_server_result* results, uint64_t cap, uint64_t* count, int wait_ms);
+int pcg_server_get_stats(pcg_server* server, pcg_server_stats* stats);
 
 /* ---- allocation-free cell step ------------------------------------------- */
 

@@ -55,6 +55,7 @@ SIGNATURES = {
     "pcg_update_agents": [_P, _P, _P],
     "pcg_set_internalized": [_P, _P],
     "pcg_initialize": [_P],
+    "pcg_estimate_device_bytes": [_P, _P],
     "pcg_solve": [_P, _u64],
     "pcg_run_phases": [_P, _u32, _i32],
     "pcg_recompute_positional_data": [_P],
@@ -85,6 +86,12 @@ SIGNATURES = {
     "pcg_batch_get_kernel_stats": [_P, _P, _u64, _P],
     "pcg_batch_reset_kernel_stats": [_P],
     "pcg_batch_get_launch_count": [_P, _P],
+    "pcg_server_create": [_P, _i32, _i32, _P],
+    "pcg_server_destroy": [_P],
+    "pcg_server_submit": [_P, _P, _u64, _u64],
+    "pcg_server_cancel": [_P, _u64],
+    "pcg_server_poll": [_P, _P, _u64, _P, _i32],
+    "pcg_server_get_stats": [_P, _P],
 }
 
 _lib = None
@@ -225,6 +232,11 @@ class Solver:
     # -- solver surface ----------------------------------------------------
     def initialize(self):
         self._check(self._L.pcg_initialize(self._h))
+
+    def estimate_device_bytes(self):
+        v = ctypes.c_uint64()
+        self._check(self._L.pcg_estimate_device_bytes(self._h, ctypes.byref(v)))
+        return v.value
 
     def solve(self, iterations=1):
         self._check(self._L.pcg_solve(self._h, iterations))
@@ -396,3 +408,93 @@ class Batch:
         v = ctypes.c_uint64()
         self._check(self._L.pcg_batch_get_launch_count(self._h, ctypes.byref(v)))
         return v.value
+
+
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("max_active", ctypes.c_uint64), ("steps_per_tick", ctypes.c_uint64),
+                ("reserve_bytes", ctypes.c_uint64), ("max_queue", ctypes.c_uint64),
+                ("memory_limit_bytes", ctypes.c_uint64), ("autotune", ctypes.c_int)]
+
+
+class ServerResult(ctypes.Structure):
+    _fields_ = [("ctx", ctypes.c_void_p), ("tag", ctypes.c_uint64), ("steps", ctypes.c_uint64),
+                ("status", ctypes.c_int), ("code", ctypes.c_int), ("t_submit", ctypes.c_double),
+                ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double), ("device_bytes", ctypes.c_uint64),
+                ("error", ctypes.c_char * 160)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "admitted", "completed", "cancelled", "refused",
+                                               "failed", "ticks", "rebuilds", "steps", "vss", "active_bytes",
+                                               "queued", "active", "in_flight")] + [("uptime_s", ctypes.c_double)]
+
+
+REQUEST_DONE, REQUEST_CANCELLED, REQUEST_REFUSED, REQUEST_FAILED = 0, 1, 2, 3
+REQUEST_STATUS = {0: "done", 1: "cancelled", 2: "refused", 3: "failed"}
+
+
+class Server:
+    """Continuous batching of independent simulations on one device (pcg_server_*).
+
+    submit() hands a configured, NOT initialised Solver to the server, which owns it
+    until poll() returns it; the returned Solver holds the results and its device
+    memory until it is closed."""
+
+    def __init__(self, precision: int = FP32, device: int = 0, max_active: int = 0, steps_per_tick: int = 0,
+                 reserve_bytes: int = 1 << 30, max_queue: int = 0, memory_limit_bytes: int = 0,
+                 autotune: bool = False):
+        self._L = load_library()
+        opts = ServerOptions(max_active, steps_per_tick, reserve_bytes, max_queue, memory_limit_bytes,
+                             int(bool(autotune)))
+        h = ctypes.c_void_p()
+        self._check(self._L.pcg_server_create(ctypes.byref(h), precision, device, ctypes.byref(opts)))
+        self._h = h
+        self._held = {}  # tag -> Solver owned by the server
+
+    def _check(self, rc):
+        if rc != 0:
+            raise PcgError(rc, self._L.pcg_last_error().decode())
+
+    def submit(self, solver: "Solver", steps: int, tag: int):
+        if tag in self._held:
+            raise ValueError(f"tag {tag} is already in flight")
+        self._check(self._L.pcg_server_submit(self._h, solver.handle, steps, tag))
+        self._held[tag] = solver
+
+    def cancel(self, tag: int):
+        self._check(self._L.pcg_server_cancel(self._h, tag))
+
+    def poll(self, max_results: int = 256, wait_ms: int = 0):
+        arr = (ServerResult * max_results)()
+        n = ctypes.c_uint64()
+        self._check(self._L.pcg_server_poll(self._h, arr, max_results, ctypes.byref(n), wait_ms))
+        out = []
+        for i in range(n.value):
+            r = arr[i]
+            out.append({"solver": self._held.pop(r.tag), "tag": r.tag, "steps": r.steps,
+                        "status": REQUEST_STATUS.get(r.status, r.status), "code": r.code,
+                        "t_submit": r.t_submit, "t_admit": r.t_admit, "t_done": r.t_done,
+                        "device_bytes": r.device_bytes, "error": r.error.decode()})
+        return out
+
+    def stats(self):
+        st = ServerStats()
+        self._check(self._L.pcg_server_get_stats(self._h, ctypes.byref(st)))
+        return {name: getattr(st, name) for name, _ in ServerStats._fields_}
+
+    def in_flight(self):
+        return len(self._held)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.pcg_server_destroy(self._h)
+            self._h = None
+            for s in self._held.values():  # destroyed by the server
+                s._h = None
+            self._held.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

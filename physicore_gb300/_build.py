@@ -2,6 +2,8 @@
 
 The translation units compile in parallel into physicore_gb300/_build/ and link
 into physicore_gb300/libphysicore_gb300.so (static CUDA runtime, no torch types).
+The C++20 host mirror of the reference's solver plugin surface (csrc/host/*.cpp)
+links against it as libphysicore_gb300_host.so.
 """
 from __future__ import annotations
 
@@ -16,6 +18,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libphysicore_gb300.so")
+HOST_LIB = os.path.join(PKG, "libphysicore_gb300_host.so")
+HOST = os.path.join(CSRC, "host")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -64,7 +68,28 @@ def build(force: bool = False, extra: list[str] | None = None, jobs: int | None 
         tmp = LIB + f".tmp{os.getpid()}"
         subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs], check=True)
         os.replace(tmp, LIB)
+    build_host()
     return LIB
+
+
+def cxx() -> str:
+    for cand in (os.environ.get("CXX"), shutil.which("g++"), shutil.which("c++")):
+        if cand:
+            return cand
+    raise RuntimeError("no C++ compiler found")
+
+
+def build_host() -> str:
+    """The host mirror: solver interface, registry and the gb300_solver plugin."""
+    srcs = sorted(glob.glob(os.path.join(HOST, "*.cpp")))
+    deps = srcs + sorted(glob.glob(os.path.join(HOST, "*.h"))) + headers() + [LIB, __file__]
+    if _stale(HOST_LIB, deps):
+        tmp = HOST_LIB + f".tmp{os.getpid()}"
+        subprocess.run([cxx(), "-std=c++20", "-O2", "-fPIC", "-shared", "-Wall", "-Wextra", *srcs,
+                        "-I", os.path.join(ROOT, "include"), "-L", PKG, "-lphysicore_gb300",
+                        "-Wl,-rpath,$ORIGIN", "-o", tmp], check=True)
+        os.replace(tmp, HOST_LIB)
+    return HOST_LIB
 
 
 if __name__ == "__main__":

@@ -392,6 +392,10 @@ static int derive_layout(Context* c)
 	return PCG_OK;
 }
 
+int upload_agents(Context* c, uint64_t A, const double* positions, const double* secretion, const double* saturation,
+				  const double* uptake, const double* net_export, const double* volumes, const uint8_t* is_active,
+				  const double* internalized, const double* fraction_released, bool compute_internalized);
+
 static int do_initialize(Context* c)
 {
 	if (c->initialized)
@@ -423,6 +427,15 @@ static int do_initialize(Context* c)
 		if (sweep_smem_bytes(c, axis) > kMaxSmemBytes)
 			return fail(PCG_ERR_UNSUPPORTED, "a line of axis " + std::to_string(axis) +
 												 " exceeds the shared-memory sweep limit");
+	if (c->staged_agents)
+	{
+		const Context::HostAgents& h = *c->staged_agents;
+		rc = upload_agents(c, c->A, h.pos.data(), h.sec.data(), h.sat.data(), h.upt.data(), h.net.data(),
+						   h.vol.data(), h.active.data(), h.internal.data(), h.frac.data(), c->compute_internalized);
+		if (rc)
+			return rc;
+		c->staged_agents.reset();
+	}
 	c->initialized = true;
 	c->generation++;
 	return check_device(c);
@@ -459,6 +472,68 @@ static int alloc_agents(Context* c, uint64_t A)
 	if ((rc = dalloc(c, c->counts, c->V * sizeof(uint32_t))))
 		return rc;
 	return PCG_OK;
+}
+
+int upload_agents(Context* c, uint64_t A, const double* positions, const double* secretion, const double* saturation,
+				  const double* uptake, const double* net_export, const double* volumes, const uint8_t* is_active,
+				  const double* internalized, const double* fraction_released, bool compute_internalized)
+{
+	int rc = alloc_agents(c, A);
+	if (rc)
+		return rc;
+	c->A = A;
+	c->compute_internalized = compute_internalized;
+	const uint64_t S = c->S;
+	if (A)
+	{
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_pos.ptr, positions, A * c->dims * sizeof(double), cudaMemcpyHostToDevice,
+									 c->stream));
+		const double* rates[4] = { secretion, saturation, uptake, net_export };
+		DeviceBuffer* dst[4] = { &c->a_sec, &c->a_sat, &c->a_upt, &c->a_net };
+		for (int k = 0; k < 4; k++)
+			PCG_CUDA_TRY(cudaMemcpyAsync(dst[k]->ptr, rates[k], A * S * sizeof(double), cudaMemcpyHostToDevice,
+										 c->stream));
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_vol.ptr, volumes, A * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_active.ptr, is_active, A, cudaMemcpyHostToDevice, c->stream));
+		if (internalized)
+			PCG_CUDA_TRY(cudaMemcpyAsync(c->a_internal.ptr, internalized, A * S * sizeof(double),
+										 cudaMemcpyHostToDevice, c->stream));
+		else
+			PCG_CUDA_TRY(cudaMemsetAsync(c->a_internal.ptr, 0, A * S * sizeof(double), c->stream));
+		if (fraction_released)
+			PCG_CUDA_TRY(cudaMemcpyAsync(c->a_frac.ptr, fraction_released, A * S * sizeof(double),
+										 cudaMemcpyHostToDevice, c->stream));
+		else
+			PCG_CUDA_TRY(cudaMemsetAsync(c->a_frac.ptr, 0, A * S * sizeof(double), c->stream));
+		PCG_CUDA_TRY(cudaMemsetAsync(c->counts.ptr, 0, c->V * sizeof(uint32_t), c->stream));
+		PCG_CUDA_TRY(cudaStreamSynchronize(c->stream)); // the caller may free its arrays on return
+	}
+	c->recompute_cells = true;
+	return PCG_OK;
+}
+
+// Field, coefficient tables, error/flag/ticket words, Dirichlet and bulk tables,
+// agents with their cell scratch, and the layout staging buffer a host transfer
+// allocates.
+uint64_t estimate_device_bytes(const Context* c)
+{
+	if (!c->mesh_set || c->S == 0)
+		return 0;
+	const uint64_t w = c->wsize, S = c->S, V = c->V, A = c->A;
+	const uint64_t row_len = c->n[0] * S, pitch = round_up(row_len, 32 / w), rows = c->n[1] * c->n[2];
+	uint64_t b = rows * pitch * w;               // field
+	b += V * S * w;                              // staging of pcg_get_field / pcg_set_field
+	for (int a = 0; a < c->dims; a++)            // coefficient tables (full and compressed)
+		b += (4 * c->n[a] * S + 64 * S + 64) * w;
+	b += 3 * 256 + 2 * S * 8;                    // words, mass
+	b += c->K * (8 + S * (w + 1)) + 12 * S * (w + 1);
+	if (c->bulk_mode == PCG_BULK_UNIFORM)
+		b += 3 * S * w;
+	else if (c->bulk_mode == PCG_BULK_PER_VOXEL)
+		b += 3 * rows * pitch * w;
+	if (A)
+		b += A * (c->dims * 8 + 6 * S * 8 + 8 + 1 + 8 + 6 * S * w) + V * 8;
+	return b;
 }
 
 } // namespace pcg
@@ -703,47 +778,47 @@ int pcg_set_agents(pcg_context* c, uint64_t A, const double* positions, const do
 		return fail(PCG_ERR_UNSUPPORTED, "at most 2^32-2 agents are supported");
 	if (A && (!positions || !secretion || !saturation || !uptake || !net_export || !volumes || !is_active))
 		return fail(PCG_ERR_INVALID, "null agent arrays");
-	pcg::DeviceGuard g(c->device);
-	int rc = pcg::alloc_agents(c, A);
-	if (rc)
-		return rc;
-	c->A = A;
-	c->compute_internalized = compute_internalized != 0;
-	const uint64_t S = c->S;
-	if (A)
+	const uint64_t S = c->S, D = (uint64_t)c->dims;
+	if (!c->initialized)
 	{
-		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_pos.ptr, positions, A * c->dims * sizeof(double), cudaMemcpyHostToDevice,
-									 c->stream));
-		const double* rates[4] = { secretion, saturation, uptake, net_export };
-		pcg::DeviceBuffer* dst[4] = { &c->a_sec, &c->a_sat, &c->a_upt, &c->a_net };
-		for (int k = 0; k < 4; k++)
-			PCG_CUDA_TRY(cudaMemcpyAsync(dst[k]->ptr, rates[k], A * S * sizeof(double), cudaMemcpyHostToDevice,
-										 c->stream));
-		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_vol.ptr, volumes, A * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_active.ptr, is_active, A, cudaMemcpyHostToDevice, c->stream));
-		if (internalized)
-			PCG_CUDA_TRY(cudaMemcpyAsync(c->a_internal.ptr, internalized, A * S * sizeof(double),
-										 cudaMemcpyHostToDevice, c->stream));
-		else
-			PCG_CUDA_TRY(cudaMemsetAsync(c->a_internal.ptr, 0, A * S * sizeof(double), c->stream));
-		if (fraction_released)
-			PCG_CUDA_TRY(cudaMemcpyAsync(c->a_frac.ptr, fraction_released, A * S * sizeof(double),
-										 cudaMemcpyHostToDevice, c->stream));
-		else
-			PCG_CUDA_TRY(cudaMemsetAsync(c->a_frac.ptr, 0, A * S * sizeof(double), c->stream));
-		PCG_CUDA_TRY(cudaMemsetAsync(c->counts.ptr, 0, c->V * sizeof(uint32_t), c->stream));
-		PCG_CUDA_TRY(cudaStreamSynchronize(c->stream)); // the caller may free its arrays on return
+		// staged on the host until initialize
+		auto h = std::make_unique<Context::HostAgents>();
+		h->pos.assign(positions, positions + A * D);
+		h->sec.assign(secretion, secretion + A * S);
+		h->sat.assign(saturation, saturation + A * S);
+		h->upt.assign(uptake, uptake + A * S);
+		h->net.assign(net_export, net_export + A * S);
+		h->vol.assign(volumes, volumes + A);
+		h->active.assign(is_active, is_active + A);
+		h->internal = internalized ? std::vector<double>(internalized, internalized + A * S)
+								   : std::vector<double>(A * S, 0.0);
+		h->frac = fraction_released ? std::vector<double>(fraction_released, fraction_released + A * S)
+									: std::vector<double>(A * S, 0.0);
+		c->staged_agents = std::move(h);
+		c->A = A;
+		c->compute_internalized = compute_internalized != 0;
+		c->recompute_cells = true;
+		return PCG_OK;
 	}
-	c->recompute_cells = true;
-	return PCG_OK;
+	pcg::DeviceGuard g(c->device);
+	return pcg::upload_agents(c, A, positions, secretion, saturation, uptake, net_export, volumes, is_active,
+							  internalized, fraction_released, compute_internalized != 0);
 }
 
 int pcg_update_agents(pcg_context* c, const double* positions, const uint8_t* is_active)
 {
 	CTX_CHECK(c);
-	pcg::DeviceGuard g(c->device);
 	if (c->A == 0)
 		return PCG_OK;
+	if (c->staged_agents)
+	{
+		if (positions)
+			c->staged_agents->pos.assign(positions, positions + c->A * c->dims);
+		if (is_active)
+			c->staged_agents->active.assign(is_active, is_active + c->A);
+		return PCG_OK;
+	}
+	pcg::DeviceGuard g(c->device);
 	if (positions)
 		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_pos.ptr, positions, c->A * c->dims * sizeof(double),
 									 cudaMemcpyHostToDevice, c->stream));
@@ -756,12 +831,26 @@ int pcg_update_agents(pcg_context* c, const double* positions, const uint8_t* is
 int pcg_set_internalized(pcg_context* c, const double* internalized)
 {
 	CTX_CHECK(c);
-	pcg::DeviceGuard g(c->device);
 	if (c->A == 0)
 		return PCG_OK;
+	if (c->staged_agents)
+	{
+		c->staged_agents->internal.assign(internalized, internalized + c->A * c->S);
+		return PCG_OK;
+	}
+	pcg::DeviceGuard g(c->device);
 	PCG_CUDA_TRY(cudaMemcpyAsync(c->a_internal.ptr, internalized, c->A * c->S * sizeof(double),
 								 cudaMemcpyHostToDevice, c->stream));
 	PCG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+	return PCG_OK;
+}
+
+int pcg_estimate_device_bytes(pcg_context* c, uint64_t* bytes)
+{
+	CTX_CHECK(c);
+	if (!bytes)
+		return fail(PCG_ERR_INVALID, "null argument");
+	*bytes = pcg::estimate_device_bytes(c);
 	return PCG_OK;
 }
 
@@ -900,6 +989,11 @@ int pcg_get_density(pcg_context* c, uint64_t s, uint64_t x, uint64_t y, uint64_t
 int pcg_get_internalized(pcg_context* c, double* host)
 {
 	CTX_CHECK(c);
+	if (c->staged_agents)
+	{
+		std::copy(c->staged_agents->internal.begin(), c->staged_agents->internal.end(), host);
+		return PCG_OK;
+	}
 	pcg::DeviceGuard g(c->device);
 	int rc = pcg::check_device(c);
 	if (rc)

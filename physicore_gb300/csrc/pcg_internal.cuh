@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -211,6 +212,14 @@ struct Context
 	// agents
 	uint64_t A = 0;
 	bool compute_internalized = false;
+	// Agents set before initialize wait here (host copies) and reach the device in
+	// initialize, so that an uninitialised context holds no device memory.
+	struct HostAgents
+	{
+		std::vector<double> pos, sec, sat, upt, net, vol, internal, frac;
+		std::vector<uint8_t> active;
+	};
+	std::unique_ptr<HostAgents> staged_agents;
 	DeviceBuffer a_pos, a_sec, a_sat, a_upt, a_net, a_vol, a_active, a_internal, a_frac;
 	// cell scratch
 	DeviceBuffer a_vox;                   // uint32 [A]: linear voxel index (x + nx*(y + ny*z)), or ~0
@@ -277,6 +286,9 @@ struct CellStepBuffers
 	float *num, *den, *fac, *rnum, *rden, *rfac;
 };
 int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream);
+
+// Device bytes a context needs once initialised (admission control).
+uint64_t estimate_device_bytes(const Context* c);
 
 // context lifecycle (capi.cu)
 int initialize_context(Context* c);  // allocates and uploads on first use

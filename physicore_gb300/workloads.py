@@ -158,8 +158,10 @@ def random_small(seed, max_side=24, max_S=9, max_agents=300, allow_bulk=True):
                 bulk=bulk, agents=ag, compute_internalized=bool(rng.random() < 0.6))
 
 
-def apply(solver, p, with_field=True, with_agents=True):
-    """Feeds problem `p` to `solver` and initialises it."""
+def apply(solver, p, with_field=True, with_agents=True, initialize=True):
+    """Feeds problem `p` to `solver` and initialises it (with initialize=False the
+    solver stays uninitialised, holding no device memory, and the initial field is
+    the uniform initial conditions: a request for the simulation server)."""
     solver.set_mesh(p["dims"], p["bbmin"], p["bbmax"], p["voxel"])
     solver.set_substrates(p["dt"], p["D"], p["decay"], p["initial"])
     for axis, side, vals, conds in p["boundary"]:
@@ -174,6 +176,8 @@ def apply(solver, p, with_field=True, with_agents=True):
         solver.set_agents(a["positions"], a["secretion"], a["saturation"], a["uptake"], a["net_export"],
                           a["volumes"], a["is_active"], fraction_released=a["fraction_released"],
                           compute_internalized=p["compute_internalized"])
+    if not initialize:
+        return solver
     solver.initialize()
     if with_field and p.get("field") is not None:
         f = p["field"]
