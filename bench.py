@@ -291,6 +291,8 @@ def run_gb300(args, w):
             "cpu_baseline": cpu}
     if args.batch_domains > 0:
         line["batched"] = run_batched(args, local, ClockSampler)
+    if args.serve_duration > 0:
+        line["serve"] = run_serve(args, local)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -395,6 +397,85 @@ def run_batched(args, local, clock_sampler=None):
     return out
 
 
+def run_serve(args, local):
+    """The served request stream (Poisson arrivals of independent simulations of
+    random sizes and step counts; workloads.ServedStream) through the simulation
+    server: a feeder thread submits each request at its arrival time, the main
+    thread collects finished ones, reads their fields back (FP32, planar, into a
+    pinned buffer) and destroys them.  Reports time-to-result percentiles (submit ->
+    finished on the device, and -> field on the host) and aggregate VSS/s."""
+    import torch
+
+    import physicore_gb300 as pcg
+    from physicore_gb300 import workloads as W
+    stream = W.ServedStream(duration=args.serve_duration)
+    n = len(stream)
+    srv = pcg.Server(pcg.FP32, device=local, steps_per_tick=args.serve_tick, reserve_bytes=1 << 30)
+    max_elems = int(max(np.prod(stream.sides[i]) * stream.S[i] for i in range(n)))
+    host = torch.empty(max_elems, dtype=torch.float32, pin_memory=True).numpy()
+    submit_wall = np.zeros(n)
+    lag = np.zeros(n)
+    err = []
+
+    def feed():
+        t0 = time.perf_counter()
+        try:
+            for i in range(n):
+                delay = stream.arrivals[i] - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                lag[i] = max(0.0, -delay)
+                s = stream.request(pcg.Solver(pcg.FP32, device=local), i)
+                submit_wall[i] = time.perf_counter()
+                srv.submit(s, int(stream.steps[i]), i)
+        except Exception as e:  # surfaced by the main thread
+            err.append(e)
+
+    th = threading.Thread(target=feed, daemon=True)
+    t_start = time.perf_counter()
+    th.start()
+    lat_dev, lat_host, statuses, vss_done = [], [], {}, 0
+    t_first = t_last = None
+    got = 0
+    while got < n and not err:
+        for r in srv.poll(64, wait_ms=20):
+            got += 1
+            statuses[r["status"]] = statuses.get(r["status"], 0) + 1
+            s = r["solver"]
+            if r["status"] == "done":
+                i = r["tag"]
+                nx, ny, nz = (int(v) for v in stream.sides[i])
+                S = int(stream.S[i])
+                s.get_field(layout=pcg.LAYOUT_PLANAR, dtype=np.float32, out=host[: S * nx * ny * nz].reshape(S, nz, ny, nx))
+                lat_host.append(time.perf_counter() - submit_wall[i])
+                lat_dev.append(r["t_done"] - r["t_submit"])
+                vss_done += stream.vss(i)
+                t_first = r["t_submit"] if t_first is None else min(t_first, r["t_submit"])
+                t_last = r["t_done"] if t_last is None else max(t_last, r["t_done"])
+            s.close()
+        if time.perf_counter() - t_start > args.serve_duration * 20 + 120:
+            break
+    wall = time.perf_counter() - t_start
+    st = srv.stats()
+    srv.close()
+    if err:
+        raise err[0]
+    offered = sum(stream.vss(i) for i in range(n)) / args.serve_duration
+    q = lambda a, p: float(np.percentile(a, p)) if len(a) else None
+    return {"workload": f"served: Poisson arrivals at 200/s for {args.serve_duration:g} s ({n} requests), sides "
+                        "log-uniform [32,256] per axis, 1-8 substrates, 0-200,000 agents, steps log-uniform "
+                        "[10,1000], FP32",
+            "requests": n, "statuses": statuses, "offered_vss_per_s": offered,
+            "value": vss_done / (t_last - t_first) if t_last else None, "unit": UNIT,
+            "time_to_result_s": {"p50": q(lat_dev, 50), "p99": q(lat_dev, 99), "mean": float(np.mean(lat_dev))
+                                 if lat_dev else None, "measured": "submit -> last step finished on the device"},
+            "time_to_host_s": {"p50": q(lat_host, 50), "p99": q(lat_host, 99),
+                               "measured": "submit -> field (FP32, planar) in pinned host memory"},
+            "feeder_lag_s": {"p50": q(lag, 50), "max": float(lag.max()) if n else None},
+            "server": {k: st[k] for k in ("ticks", "rebuilds", "steps", "admitted", "refused", "failed")},
+            "steps_per_tick": args.serve_tick, "wall_s": round(wall, 2)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -408,12 +489,19 @@ def main():
     ap.add_argument("--batch-domains", type=int, default=256, help="domains of the batched workload (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=200)
     ap.add_argument("--only-batched", action="store_true", help="run only the batched workload")
+    ap.add_argument("--serve-duration", type=float, default=10.0, help="seconds of request arrivals (0: skip)")
+    ap.add_argument("--serve-tick", type=int, default=8, help="steps between admission points")
+    ap.add_argument("--only-serve", action="store_true", help="run only the served request stream")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     w = dict(WORKLOAD, n=args.n)
     if args.impl == "reference":
         run_reference(args, w)
+    elif args.only_serve:
+        import torch
+        torch.cuda.set_device(dist_env()[2])
+        print(json.dumps(run_serve(args, dist_env()[2])), flush=True)
     elif args.only_batched:
         import torch
         torch.cuda.set_device(dist_env()[2])

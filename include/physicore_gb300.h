@@ -209,6 +209,10 @@ int pcg_batch_destroy(pcg_batch* batch);
 /* `iterations` steps of every domain (solver::solve; a context whose positional
  * data are marked for recomputation rebuilds its ballot on each of them). */
 int pcg_batch_solve(pcg_batch* batch, uint64_t iterations);
+/* `iterations` steps in which domain d takes part in the first budgets[d] only
+ * (0: it sits this call out); lets requests of different lengths share launches
+ * and finish inside one call. */
+int pcg_batch_solve_budgets(pcg_batch* batch, uint64_t iterations, const uint64_t* budgets);
 int pcg_batch_synchronize(pcg_batch* batch);
 int pcg_batch_get_stream(pcg_batch* batch, void** stream);
 /* Replays the step from a CUDA graph (default 1) or launches it directly. */

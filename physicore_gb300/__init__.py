@@ -76,6 +76,7 @@ SIGNATURES = {
     "pcg_batch_create": [_P, _P, _u64],
     "pcg_batch_destroy": [_P],
     "pcg_batch_solve": [_P, _u64],
+    "pcg_batch_solve_budgets": [_P, _u64, _P],
     "pcg_batch_synchronize": [_P],
     "pcg_batch_get_stream": [_P, _P],
     "pcg_batch_set_graph": [_P, _i32],
@@ -362,8 +363,15 @@ class Batch:
         except Exception:
             pass
 
-    def solve(self, iterations=1):
-        self._check(self._L.pcg_batch_solve(self._h, iterations))
+    def solve(self, iterations=1, budgets=None):
+        """`iterations` steps; with budgets, domain d takes part in the first budgets[d] only."""
+        if budgets is None:
+            self._check(self._L.pcg_batch_solve(self._h, iterations))
+        else:
+            b = np.ascontiguousarray(budgets, dtype=np.uint64)
+            if b.size != len(self.solvers):
+                raise ValueError("one budget per domain")
+            self._check(self._L.pcg_batch_solve_budgets(self._h, iterations, b.ctypes.data))
 
     def synchronize(self):
         self._check(self._L.pcg_batch_synchronize(self._h))

@@ -105,6 +105,7 @@ struct BatchArgs
 	uint32_t* counter;        // tile counter of this launch (zeroed at the start of every step)
 	uint32_t* err;            // [0] DEV_ERR_* bits, [1] lowest failing domain
 	const uint8_t* recompute; // per domain: rebuild the ballot this step
+	uint32_t* steps_left;     // per domain: steps still to run in this call (0: the domain sits out)
 };
 
 __device__ __forceinline__ uint32_t find_entry(const WorkList& l, uint64_t u)
@@ -275,6 +276,11 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 			break;
 		const uint32_t k = find_entry(b.list, t);
 		const uint32_t di = __ldg(b.list.dom + k);
+		if (b.steps_left[di] == 0)
+		{
+			__syncthreads(); // everyone has read the ticket before thread 0 draws the next
+			continue;
+		}
 		const BatchDomain& D = b.doms[di];
 		const uint32_t R = D.x_rows, S = D.S, n = D.n[0];
 		const uint64_t r0 = (t - __ldg(b.list.base + k)) * R;
@@ -353,6 +359,11 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 			break;
 		const uint32_t k = find_entry(b.list, t);
 		const uint32_t di = __ldg(b.list.dom + k);
+		if (b.steps_left[di] == 0)
+		{
+			phase ^= 1; // no tile was loaded: keep the barrier's parity
+			continue;
+		}
 		const BatchDomain& D = b.doms[di];
 		const uint64_t lt = t - __ldg(b.list.base + k);
 		const int x0 = (int)((lt % D.yz_xblocks) * kLanes);
@@ -426,7 +437,7 @@ __global__ void batch_faces_kernel(BatchArgs b)
 	{
 		const uint64_t u = wu + (threadIdx.x & 31);
 		const uint32_t k = warp_entry(b.list, u);
-		if (u < b.list.total)
+		if (u < b.list.total && b.steps_left[__ldg(b.list.dom + k)])
 			fielddev::face_item<T>(b.doms[__ldg(b.list.dom + k)].faces, u - __ldg(b.list.base + k));
 	}
 }
@@ -440,7 +451,7 @@ __global__ void batch_interior_kernel(BatchArgs b)
 	{
 		const uint64_t u = wu + (threadIdx.x & 31);
 		const uint32_t k = warp_entry(b.list, u);
-		if (u >= b.list.total)
+		if (u >= b.list.total || !b.steps_left[__ldg(b.list.dom + k)])
 			continue;
 		const BatchDomain& D = b.doms[__ldg(b.list.dom + k)];
 		const uint64_t i = u - __ldg(b.list.base + k);
@@ -459,6 +470,8 @@ __global__ void batch_bulk_kernel(BatchArgs b)
 	for (uint64_t u = warp; u < b.list.total; u += nwarps)
 	{
 		const uint32_t k = warp_entry(b.list, u);
+		if (!b.steps_left[__ldg(b.list.dom + k)])
+			continue;
 		const BatchDomain& D = b.doms[__ldg(b.list.dom + k)];
 		const uint64_t r = u - __ldg(b.list.base + k);
 		const T* sp = static_cast<const T*>(D.bulk[0]);
@@ -486,7 +499,7 @@ __global__ void batch_clear_counts_kernel(BatchArgs b)
 	{
 		const uint32_t k = warp_entry(b.list, u);
 		const uint32_t di = __ldg(b.list.dom + k);
-		if (!b.recompute[di])
+		if (!b.recompute[di] || !b.steps_left[di])
 			continue;
 		const BatchDomain& D = b.doms[di];
 		const uint64_t v0 = (u - __ldg(b.list.base + k)) * kClearChunk;
@@ -505,7 +518,7 @@ __global__ void batch_cells_locate_kernel(BatchArgs b)
 	if (u >= b.list.total)
 		return;
 	const uint32_t di = __ldg(b.list.dom + k);
-	if (!b.recompute[di])
+	if (!b.recompute[di] || !b.steps_left[di])
 		return;
 	const CellArgs& a = b.doms[di].cells;
 	const uint64_t i = u - __ldg(b.list.base + k);
@@ -525,7 +538,7 @@ __global__ void batch_cells_ballot_kernel(BatchArgs b)
 	if (u < b.list.total)
 	{
 		di = __ldg(b.list.dom + k);
-		if (b.recompute[di])
+		if (b.recompute[di] && b.steps_left[di])
 		{
 			i = u - __ldg(b.list.base + k);
 			v = b.doms[di].cells.vox[i];
@@ -555,7 +568,7 @@ __global__ void batch_cells_reduce_kernel(BatchArgs b)
 	if (u < b.list.total)
 	{
 		di = __ldg(b.list.dom + k);
-		if (b.recompute[di])
+		if (b.recompute[di] && b.steps_left[di])
 		{
 			const CellArgs& a = b.doms[di].cells;
 			const uint64_t i = u - __ldg(b.list.base + k);
@@ -573,7 +586,7 @@ __global__ void batch_cells_apply_kernel(BatchArgs b)
 {
 	const uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	const uint32_t k = warp_entry(b.list, u);
-	if (u >= b.list.total)
+	if (u >= b.list.total || !b.steps_left[__ldg(b.list.dom + k)])
 		return;
 	agent_apply<T>(b.doms[__ldg(b.list.dom + k)].cells, u - __ldg(b.list.base + k));
 }
@@ -583,11 +596,19 @@ __global__ void batch_cells_internalize_kernel(BatchArgs b)
 {
 	const uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	const uint32_t k = warp_entry(b.list, u);
-	if (u >= b.list.total)
+	if (u >= b.list.total || !b.steps_left[__ldg(b.list.dom + k)])
 		return;
 	const CellArgs& a = b.doms[__ldg(b.list.dom + k)].cells;
 	if (a.internalized)
 		agent_internalize<T>(a, u - __ldg(b.list.base + k));
+}
+
+// End of a step: one step fewer for every domain still running.
+__global__ void batch_count_step_kernel(uint32_t* steps_left, uint32_t count)
+{
+	for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < count; d += gridDim.x * blockDim.x)
+		if (steps_left[d])
+			steps_left[d]--;
 }
 
 // ------------------------------------------------------------------ host side
@@ -703,7 +724,8 @@ struct pcg_batch
 	std::vector<pcg::BatchDomain> h_doms;
 	std::vector<CUtensorMap> h_tmaps;
 	std::vector<pcg::AxisConfig> cfg[3];
-	DeviceBuffer d_doms, d_tmaps, d_lists, d_counters, d_err, d_recompute;
+	DeviceBuffer d_doms, d_tmaps, d_lists, d_counters, d_err, d_recompute, d_steps_left;
+	std::vector<uint32_t> h_steps_left;
 	pcg::WorkList lists[pcg::L_COUNT] {};
 	uint64_t smem[3] = { 0, 0, 0 };
 	unsigned grid[3] = { 0, 0, 0 };
@@ -743,21 +765,24 @@ namespace {
 
 void free_buf(DeviceBuffer& b) { dfree(b); }
 
-int balloc(DeviceBuffer& b, size_t bytes)
+// Batch buffers come from the stream-ordered allocator on the batch's stream (all
+// their users run on it), so regrouping batches never synchronises the device.
+int balloc(DeviceBuffer& b, size_t bytes, cudaStream_t stream)
 {
 	if (b.ptr && b.bytes >= bytes)
 		return PCG_OK;
 	dfree(b);
 	if (!bytes)
 		return PCG_OK;
-	cudaError_t e = cudaMalloc(&b.ptr, bytes);
+	cudaError_t e = cudaMallocAsync(&b.ptr, bytes, stream);
 	if (e != cudaSuccess)
 	{
 		b.ptr = nullptr;
 		cudaGetLastError();
-		return fail(PCG_ERR_NOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes for a batch failed");
+		return fail(PCG_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes for a batch failed");
 	}
 	b.bytes = bytes;
+	b.stream = stream;
 	return PCG_OK;
 }
 
@@ -881,7 +906,7 @@ int upload_lists(DeviceBuffer& buf, const std::vector<HostList>& hl, WorkList* o
 	size_t bytes = 0;
 	for (const auto& h : hl)
 		bytes += round_up(h.base.size() * 8, 256) + round_up(std::max<size_t>(h.dom.size(), 1) * 4, 256);
-	int rc = balloc(buf, bytes);
+	int rc = balloc(buf, bytes, stream);
 	if (rc)
 		return rc;
 	std::vector<unsigned char> host(bytes, 0);
@@ -923,7 +948,8 @@ int upload_domains(pcg_batch* b)
 	for (size_t d = 0; d < N; d++)
 		b->h_doms[d] = describe_domain(b, d);
 	int rc;
-	if ((rc = balloc(b->d_doms, N * sizeof(BatchDomain))) || (rc = balloc(b->d_tmaps, N * 2 * sizeof(CUtensorMap))))
+	if ((rc = balloc(b->d_doms, N * sizeof(BatchDomain), b->stream)) ||
+		(rc = balloc(b->d_tmaps, N * 2 * sizeof(CUtensorMap), b->stream)))
 		return rc;
 	PCG_CUDA_TRY(cudaMemcpyAsync(b->d_doms.ptr, b->h_doms.data(), N * sizeof(BatchDomain), cudaMemcpyHostToDevice,
 								 b->stream));
@@ -1129,6 +1155,7 @@ BatchArgs args_for(pcg_batch* b, int list, int counter)
 	a.counter = static_cast<uint32_t*>(b->d_counters.ptr) + counter;
 	a.err = static_cast<uint32_t*>(b->d_err.ptr);
 	a.recompute = static_cast<const uint8_t*>(b->d_recompute.ptr);
+	a.steps_left = static_cast<uint32_t*>(b->d_steps_left.ptr);
 	return a;
 }
 
@@ -1222,6 +1249,9 @@ int launch_step(pcg_batch* b)
 			PCG_CUDA_TRY(cudaGetLastError());
 		}
 	}
+	const uint32_t N = (uint32_t)b->ctx.size();
+	batch_count_step_kernel<<<(N + 255) / 256, 256, 0, b->stream>>>(static_cast<uint32_t*>(b->d_steps_left.ptr), N);
+	PCG_CUDA_TRY(cudaGetLastError());
 	return PCG_OK;
 }
 
@@ -1493,7 +1523,7 @@ int autotune_t(pcg_batch* b)
 	for (size_t d = 0; d < N; d++)
 		off[d + 1] = off[d] + round_up(C(b, d)->rows * C(b, d)->pitch * b->wsize, 256);
 	DeviceBuffer save;
-	if ((rc = balloc(save, off[N])))
+	if ((rc = balloc(save, off[N], b->stream)))
 		return fail(PCG_ERR_NOMEM, "autotune needs a copy of the batch's fields and could not allocate it");
 	for (size_t d = 0; d < N; d++)
 		cudaMemcpyAsync(static_cast<char*>(save.ptr) + off[d], C(b, d)->field.ptr,
@@ -1649,11 +1679,15 @@ int pcg_batch_create(pcg_batch** out, pcg_context* const* contexts, uint64_t cou
 		c.assign(count, pcg::AxisConfig {});
 	b->h_recompute.assign(count, 0);
 	int rc;
-	if ((rc = pcg::balloc(b->d_counters, 16 * sizeof(uint32_t))) || (rc = pcg::balloc(b->d_err, 2 * sizeof(uint32_t))) ||
-		(rc = pcg::balloc(b->d_recompute, count)))
+	if ((rc = pcg::balloc(b->d_counters, 16 * sizeof(uint32_t), b->stream)) ||
+		(rc = pcg::balloc(b->d_err, 2 * sizeof(uint32_t), b->stream)) ||
+		(rc = pcg::balloc(b->d_recompute, count, b->stream)) ||
+		(rc = pcg::balloc(b->d_steps_left, count * sizeof(uint32_t), b->stream)))
 		return bail(rc);
+	b->h_steps_left.assign(count, 0);
 	const uint32_t reset[2] = { 0, 0xffffffffu };
-	if (cudaMemcpy(b->d_err.ptr, reset, sizeof(reset), cudaMemcpyHostToDevice) != cudaSuccess)
+	if (cudaMemcpyAsync(b->d_err.ptr, reset, sizeof(reset), cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
+		cudaStreamSynchronize(b->stream) != cudaSuccess)
 		return bail(fail(PCG_ERR_CUDA, "could not clear the batch error word"));
 	if ((rc = pcg::refresh(b)))
 		return bail(rc);
@@ -1672,7 +1706,8 @@ int pcg_batch_destroy(pcg_batch* b)
 	pcg::collect(b);
 	for (cudaEvent_t e : b->event_pool)
 		cudaEventDestroy(e);
-	DeviceBuffer* bufs[] = { &b->d_doms, &b->d_tmaps, &b->d_lists, &b->d_counters, &b->d_err, &b->d_recompute };
+	DeviceBuffer* bufs[] = { &b->d_doms,	 &b->d_tmaps,	  &b->d_lists,		&b->d_counters,
+							 &b->d_err, &b->d_recompute, &b->d_steps_left };
 	for (DeviceBuffer* x : bufs)
 		pcg::free_buf(*x);
 	if (b->ev_sync)
@@ -1685,13 +1720,25 @@ int pcg_batch_destroy(pcg_batch* b)
 
 int pcg_batch_solve(pcg_batch* b, uint64_t iterations)
 {
+	return pcg_batch_solve_budgets(b, iterations, nullptr);
+}
+
+int pcg_batch_solve_budgets(pcg_batch* b, uint64_t iterations, const uint64_t* budgets)
+{
 	BATCH_CHECK(b);
 	if (iterations == 0)
 		return PCG_OK;
+	if (iterations >= 0xffffffffull)
+		return fail(PCG_ERR_UNSUPPORTED, "at most 2^32-2 iterations per call");
 	pcg::DeviceGuard g(b->device);
 	int rc;
 	if ((rc = pcg::refresh(b)) || (rc = pcg::sync_in(b)) || (rc = pcg::upload_recompute(b)))
 		return rc;
+	for (size_t d = 0; d < b->ctx.size(); d++)
+		b->h_steps_left[d] = (uint32_t)(budgets ? std::min(budgets[d], iterations) : iterations);
+	PCG_CUDA_TRY(cudaMemcpyAsync(b->d_steps_left.ptr, b->h_steps_left.data(), b->ctx.size() * sizeof(uint32_t),
+								 cudaMemcpyHostToDevice, b->stream));
+	// pageable source: the copy is staged before the call returns, so the next call may rewrite it
 	const bool graph = b->use_graph && !b->timing;
 	if (graph && !b->exec && (rc = pcg::capture(b)))
 		return rc;
@@ -1713,7 +1760,8 @@ int pcg_batch_solve(pcg_batch* b, uint64_t iterations)
 			return rc;
 	}
 	for (size_t d = 0; d < b->ctx.size(); d++)
-		static_cast<Context*>(b->ctx[d])->recompute_cells = false;
+		if (!budgets || budgets[d] > 0)
+			static_cast<Context*>(b->ctx[d])->recompute_cells = false;
 	return pcg::sync_out(b);
 }
 

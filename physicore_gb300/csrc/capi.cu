@@ -35,31 +35,49 @@ const char* kernel_name(int id)
 	return (id >= 0 && id < K_COUNT) ? names[id] : "?";
 }
 
+// Context buffers come from the stream-ordered allocator on the context's own
+// stream, which lives as long as the context; freeing them (a replaced buffer, or
+// pcg_destroy) then never synchronises the device, so a process that creates and
+// destroys many contexts while others run (a server) does not stall them.
 int dalloc(Context* c, DeviceBuffer& b, size_t bytes)
 {
-	(void)c;
 	if (b.ptr && b.bytes >= bytes)
 		return PCG_OK;
-	dfree(b);
+	if (b.ptr)
+	{
+		cudaStreamSynchronize(c->stream); // earlier work may still read the old buffer
+		dfree(b);
+	}
 	if (bytes == 0)
 		return PCG_OK;
-	cudaError_t e = cudaMalloc(&b.ptr, bytes);
+	cudaStream_t s = c->own_stream;
+	cudaError_t e = s ? cudaMallocAsync(&b.ptr, bytes, s) : cudaMalloc(&b.ptr, bytes);
 	if (e != cudaSuccess)
 	{
 		b.ptr = nullptr;
 		cudaGetLastError();
-		return fail(PCG_ERR_NOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
+		return fail(PCG_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed: " +
+									   cudaGetErrorString(e));
 	}
 	b.bytes = bytes;
+	b.stream = s;
+	if (s)
+		cudaStreamSynchronize(s); // usable from any stream and by synchronous copies from here on
 	return PCG_OK;
 }
 
 void dfree(DeviceBuffer& b)
 {
 	if (b.ptr)
-		cudaFree(b.ptr);
+	{
+		if (b.stream)
+			cudaFreeAsync(b.ptr, b.stream);
+		else
+			cudaFree(b.ptr);
+	}
 	b.ptr = nullptr;
 	b.bytes = 0;
+	b.stream = nullptr;
 }
 
 static cudaEvent_t get_event(Context* c)
@@ -130,6 +148,8 @@ std::string device_error_text(uint32_t word)
 
 static int check_device(Context* c)
 {
+	if (!c->err.ptr)
+		return PCG_OK; // nothing has run on the device yet
 	cudaError_t e = cudaStreamSynchronize(c->stream);
 	if (e != cudaSuccess)
 		return fail(PCG_ERR_CUDA, std::string("stream synchronise: ") + cudaGetErrorString(e));
@@ -396,10 +416,45 @@ int upload_agents(Context* c, uint64_t A, const double* positions, const double*
 				  const double* uptake, const double* net_export, const double* volumes, const uint8_t* is_active,
 				  const double* internalized, const double* fraction_released, bool compute_internalized);
 
+// The context's own stream and device words, created on first use.
+int ensure_device_state(Context* c)
+{
+	if (!c->own_stream)
+	{
+		if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+		{
+			c->own_stream = nullptr;
+			cudaGetLastError();
+			return fail(PCG_ERR_CUDA, "cudaStreamCreate failed");
+		}
+		if (!c->stream)
+			c->stream = c->own_stream;
+	}
+	if (!c->err.ptr)
+	{
+		int rc = dalloc(c, c->err, sizeof(uint32_t) * 4);
+		if (!rc)
+			rc = dalloc(c, c->flags, sizeof(uint32_t) * 4);
+		if (!rc)
+			rc = dalloc(c, c->tickets, sizeof(uint32_t) * 4);
+		if (rc)
+			return rc;
+		PCG_CUDA_TRY(cudaMemsetAsync(c->err.ptr, 0, sizeof(uint32_t) * 4, c->stream));
+		PCG_CUDA_TRY(cudaMemsetAsync(c->flags.ptr, 0, sizeof(uint32_t) * 4, c->stream));
+	}
+	return PCG_OK;
+}
+
 static int do_initialize(Context* c)
 {
 	if (c->initialized)
 		return PCG_OK;
+	{
+		DeviceGuard g(c->device);
+		const int rc0 = ensure_device_state(c);
+		if (rc0)
+			return rc0;
+	}
 	if (!c->mesh_set || c->S == 0)
 		return fail(PCG_ERR_INVALID, "mesh and substrates must be set before initialize");
 	int rc;
@@ -574,24 +629,8 @@ int pcg_create(pcg_context** out, int precision, int device)
 	c->precision = precision;
 	c->wsize = precision == PCG_FP32 ? 4 : 8;
 	cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
-	if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
-	{
-		delete c;
-		return fail(PCG_ERR_CUDA, "cudaStreamCreate failed");
-	}
-	c->stream = c->own_stream;
-	int rc = pcg::dalloc(c, c->err, sizeof(uint32_t) * 4);
-	if (!rc)
-		rc = pcg::dalloc(c, c->flags, sizeof(uint32_t) * 4);
-	if (rc == PCG_OK)
-		rc = pcg::dalloc(c, c->tickets, sizeof(uint32_t) * 4);
-	if (rc)
-	{
-		pcg_destroy(c);
-		return rc;
-	}
-	cudaMemset(c->err.ptr, 0, sizeof(uint32_t) * 4);
-	cudaMemset(c->flags.ptr, 0, sizeof(uint32_t) * 4);
+	// the stream and the device words are created on first use (initialize), so
+	// that a context being configured holds no device resources at all
 	*out = c;
 	return PCG_OK;
 }
@@ -625,13 +664,17 @@ int pcg_destroy(pcg_context* c)
 int pcg_set_stream(pcg_context* c, void* stream)
 {
 	CTX_CHECK(c);
-	c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+	c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream; // may be created later
 	return PCG_OK;
 }
 
 int pcg_get_stream(pcg_context* c, void** stream)
 {
 	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	const int rc = pcg::ensure_device_state(c);
+	if (rc)
+		return rc;
 	*stream = c->stream;
 	return PCG_OK;
 }

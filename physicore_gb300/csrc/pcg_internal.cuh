@@ -122,10 +122,13 @@ struct SweepArgs
 
 // ------------------------------------------------------------------ context
 
+// Device memory from the stream-ordered allocator: allocated and freed on `stream`
+// (a stream that outlives the buffer), so that freeing never waits for the device.
 struct DeviceBuffer
 {
 	void* ptr = nullptr;
 	size_t bytes = 0;
+	cudaStream_t stream = nullptr;
 };
 
 struct Context;

@@ -82,11 +82,16 @@ struct GpuBackend
 		}
 		return rc;
 	}
-	int step(uint64_t k)
+	int step_begin(uint64_t k, const std::vector<uint64_t>& budgets)
 	{
-		int rc = pcg_batch_solve(batch, k);
-		if (!rc)
-			rc = pcg_batch_synchronize(batch);
+		const int rc = pcg_batch_solve_budgets(batch, k, budgets.data());
+		if (rc)
+			err = pcg_last_error();
+		return rc;
+	}
+	int step_end()
+	{
+		const int rc = pcg_batch_synchronize(batch);
 		if (rc)
 			err = pcg_last_error();
 		return rc;

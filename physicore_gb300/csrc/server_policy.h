@@ -8,16 +8,20 @@
 //   uint64_t total_bytes();                memory the server may ever use
 //   int admit(void* ctx);                  allocate and upload (PCG_OK, PCG_ERR_NOMEM, other codes)
 //   int rebuild(const std::vector<void*>&) regroup the active set into one batch
-//   int step(uint64_t k);                  k steps of every active simulation
+//   int step_begin(uint64_t k, const std::vector<uint64_t>& budgets)
+//                                          start k steps, simulation i taking part in the first budgets[i]
+//   int step_end();                        wait for them
 //   std::string last_error();
 // so the same code runs against the GPU (server.cu) and against a fake backend in
 // the CPU tests (admission refusals, allocation failures, malformed requests,
 // cancellations and step faults are all injected on the host).
 //
-// One tick: admit queued requests in arrival order while the active set has room
-// and the next request's device bytes plus a reserve fit in free memory; regroup
-// the batch when the active set changed; step every active simulation by
-// min(steps_per_tick, the smallest remaining count); retire the finished ones.
+// One tick: regroup the batch if the active set changed; start steps_per_tick steps
+// in which each active simulation takes part in min(steps_per_tick, its remaining
+// steps); while they run, admit queued requests in arrival order while the active
+// set has room and the next request's device bytes plus a reserve fit in free
+// memory (admission overlaps the device work; admitted requests join at the next
+// regroup); then wait for the steps and retire the finished simulations.
 // A request that does not fit now waits (memory is freed as active requests
 // finish and as callers destroy returned ones); it is refused only when it could
 // never fit (its bytes plus the reserve exceed total_bytes) or when its allocation
@@ -128,47 +132,62 @@ public:
 	// One scheduling step; returns false when there is nothing to do.
 	bool tick(double now)
 	{
-		admit(now);
-		if (active_.empty())
-			return false;
-		stats_.ticks++;
-		if (dirty_)
+		const size_t stepped = active_.size();
+		std::vector<uint64_t> budgets;
+		if (stepped)
 		{
-			std::vector<void*> ctxs;
+			stats_.ticks++;
+			if (dirty_)
+			{
+				std::vector<void*> ctxs;
+				for (const Request& r : active_)
+					ctxs.push_back(r.ctx);
+				const int rc = be_.rebuild(ctxs);
+				stats_.rebuilds++;
+				if (rc)
+				{
+					fail_active(rc, be_.last_error(), now);
+					return true;
+				}
+				dirty_ = false;
+			}
+			const uint64_t k = opt_.steps_per_tick;
 			for (const Request& r : active_)
-				ctxs.push_back(r.ctx);
-			const int rc = be_.rebuild(ctxs);
-			stats_.rebuilds++;
+				budgets.push_back(std::min(k, r.remaining));
+			const int rc = be_.step_begin(k, budgets);
 			if (rc)
 			{
 				fail_active(rc, be_.last_error(), now);
 				return true;
 			}
-			dirty_ = false;
 		}
-		uint64_t k = opt_.steps_per_tick;
-		for (const Request& r : active_)
-			k = std::min(k, r.remaining);
-		const int rc = be_.step(k);
+		const size_t admitted = admit(now); // overlaps the steps just started
+		if (!stepped)
+			return admitted > 0;
+		const int rc = be_.step_end();
 		if (rc)
 		{
 			fail_active(rc, be_.last_error(), now);
 			return true;
 		}
-		stats_.steps += k;
+		stats_.steps += opt_.steps_per_tick;
 		std::vector<Request> still;
-		for (Request& r : active_)
+		for (size_t i = 0; i < active_.size(); i++)
 		{
-			r.remaining -= k;
-			stats_.vss += r.vss_per_step * k;
-			if (r.remaining == 0)
+			Request& r = active_[i];
+			if (i < stepped)
 			{
-				stats_.active_bytes -= r.bytes;
-				dirty_ = true;
-				finish(r, Status::Done, 0, "", now);
+				r.remaining -= budgets[i];
+				stats_.vss += r.vss_per_step * budgets[i];
+				if (r.remaining == 0)
+				{
+					stats_.active_bytes -= r.bytes;
+					dirty_ = true;
+					finish(r, Status::Done, 0, "", now);
+					continue;
+				}
 			}
-			else
-				still.push_back(std::move(r));
+			still.push_back(std::move(r));
 		}
 		active_.swap(still);
 		return true;
@@ -208,8 +227,9 @@ public:
 	const Stats& stats() const { return stats_; }
 
 private:
-	void admit(double now)
+	size_t admit(double now)
 	{
+		size_t admitted = 0;
 		while (!queue_.empty() && active_.size() < opt_.max_active)
 		{
 			Request& r = queue_.front();
@@ -225,13 +245,13 @@ private:
 				continue;
 			}
 			if (r.bytes + opt_.reserve_bytes > be_.free_bytes())
-				return; // wait for memory to be freed
+				return admitted; // wait for memory to be freed
 			const int rc = be_.admit(r.ctx);
 			if (rc == 3 /* PCG_ERR_NOMEM */)
 			{
 				// memory went elsewhere meanwhile: retry later, unless nothing of ours holds any
 				if (!active_.empty() || ++r.attempts < kMaxAttempts)
-					return;
+					return admitted;
 			}
 			Request x = std::move(r);
 			queue_.pop_front();
@@ -245,7 +265,9 @@ private:
 			stats_.active_bytes += x.bytes;
 			active_.push_back(std::move(x));
 			dirty_ = true;
+			admitted++;
 		}
+		return admitted;
 	}
 
 	void fail_active(int rc, const std::string& msg, double now)

@@ -235,3 +235,55 @@ def batched_uneven(seed=3, count=256, **kw):
     together: about 1.8 GB of FP32 for 256 domains)."""
     for i, (sides, S, A) in enumerate(batched_sizes(seed, count, **kw)):
         yield _domain(_rng((seed, i)), f"batched_{i}", sides, S, A)
+
+
+class ServedStream:
+    """The served request stream: Poisson arrivals at `rate` per second for
+    `duration` seconds; each request a 3-D domain with sides log-uniform in
+    [32, 256] voxels per axis, 1-8 substrates, D and decay as large_320, initial
+    conditions U[0,1], 0-200,000 uniform agents (internalized tracking on) and a
+    step count log-uniform in [10, 1000].  Agent rates come from pools shared by all
+    requests of a substrate count (synthetic inputs; only positions are drawn per
+    request), so that building a request costs little host time."""
+
+    def __init__(self, seed=4, rate=200.0, duration=10.0, side_lo=32, side_hi=256, S_hi=8, agents_hi=200_000,
+                 steps_lo=10, steps_hi=1000):
+        rng = _rng(seed)
+        n = int(rng.poisson(rate * duration))
+        self.arrivals = np.sort(rng.uniform(0.0, duration, n))
+        self.sides = np.rint(log_uniform(rng, side_lo, side_hi, (n, 3))).astype(np.int64)
+        self.S = rng.integers(1, S_hi + 1, n)
+        self.A = rng.integers(0, agents_hi + 1, n)
+        self.steps = np.rint(log_uniform(rng, steps_lo, steps_hi, n)).astype(np.int64)
+        self.D = [log_uniform(rng, 10.0, 1e5, int(S)) for S in self.S]
+        self.decay = [log_uniform(rng, 1e-4, 1.0, int(S)) for S in self.S]
+        self.initial = [rng.random(int(S)) for S in self.S]
+        self.seeds = rng.integers(0, 2 ** 31, n)
+        self._unit = rng.random((agents_hi, 3))
+        self._pools = {}
+        for S in range(1, S_hi + 1):
+            blk = agents_block(rng, agents_hi, S, np.zeros((agents_hi, 3)))
+            self._pools[S] = {k: np.ascontiguousarray(blk[k]) for k in
+                              ("secretion", "saturation", "uptake", "net_export", "volumes", "is_active",
+                               "fraction_released")}
+
+    def __len__(self):
+        return len(self.arrivals)
+
+    def vss(self, i):
+        return int(np.prod(self.sides[i])) * int(self.S[i]) * int(self.steps[i])
+
+    def request(self, solver, i):
+        """Configures `solver` (not initialised) as request i."""
+        nx, ny, nz = (int(v) for v in self.sides[i])
+        S, A = int(self.S[i]), int(self.A[i])
+        ext = np.array([nx, ny, nz], dtype=np.float64) * VOXEL
+        solver.set_mesh(3, (0, 0, 0), tuple(int(v) for v in ext), (VOXEL,) * 3)
+        solver.set_substrates(0.01, self.D[i], self.decay[i], self.initial[i])
+        if A:
+            pool = self._pools[S]
+            pos = np.minimum(self._unit[:A] * ext, np.nextafter(ext, 0.0))
+            solver.set_agents(pos, pool["secretion"][:A], pool["saturation"][:A], pool["uptake"][:A],
+                              pool["net_export"][:A], pool["volumes"][:A], pool["is_active"][:A],
+                              fraction_released=pool["fraction_released"][:A], compute_internalized=True)
+        return solver

@@ -60,6 +60,7 @@ struct FakeBackend
 	{
 		rebuilds++;
 		batch = std::set<void*>(ctxs.begin(), ctxs.end());
+		order = ctxs;
 		for (void* c : ctxs)
 			if (!resident.count(c))
 			{
@@ -68,7 +69,8 @@ struct FakeBackend
 			}
 		return 0;
 	}
-	int step(uint64_t k)
+	std::vector<void*> order; // batch members in rebuild order
+	int step_begin(uint64_t, const std::vector<uint64_t>& budgets)
 	{
 		if (fail_next_step)
 		{
@@ -76,10 +78,11 @@ struct FakeBackend
 			err = "device fault";
 			return 4;
 		}
-		for (void* c : batch)
-			stepped[c] += k;
+		for (size_t i = 0; i < order.size(); i++)
+			stepped[order[i]] += budgets[i];
 		return 0;
 	}
+	int step_end() { return 0; }
 	std::string last_error() const { return err; }
 	void release(void* c) // the caller destroys a returned context
 	{
@@ -137,11 +140,15 @@ void continuous_batching()
 	Scheduler<FakeBackend> s(be, o);
 	s.submit(req(be, 1, 10, 100), 0);
 	s.submit(req(be, 2, 3, 100), 0);
-	s.tick(0); // both admitted, stepped by min(4, 3) = 3; request 2 done
+	s.tick(0); // both admitted (nothing was running yet)
+	EXPECT(s.active() == 2 && s.take_finished().empty());
+	s.tick(1); // 4 steps for 1, 3 for 2 (its budget): 2 is done inside the tick
 	auto f = s.take_finished();
-	EXPECT(f.size() == 1 && f[0].tag == 2 && f[0].status == Status::Done);
-	be.release(f[0].ctx);
-	s.submit(req(be, 3, 2, 100), 1); // arrives while 1 runs: joins the next tick
+	EXPECT(f.size() == 1 && !f.empty() && f[0].tag == 2 && f[0].status == Status::Done);
+	if (!f.empty())
+		be.release(f[0].ctx);
+	EXPECT(be.stepped[ctx(1)] == 4 && be.stepped[ctx(2)] == 3);
+	s.submit(req(be, 3, 2, 100), 1); // arrives while 1 runs: admitted during the next tick
 	auto done = run(s, be);
 	EXPECT(be.stepped[ctx(1)] == 10 && be.stepped[ctx(2)] == 3 && be.stepped[ctx(3)] == 2);
 	EXPECT(find(done, 1) && find(done, 1)->status == Status::Done);
@@ -162,12 +169,14 @@ void admission_waits_for_memory()
 	s.submit(req(be, 2, 5, 200), 0); // does not fit beside 1: waits, is not refused
 	s.tick(0);
 	EXPECT(s.active() == 1 && s.queued() == 1);
-	s.tick(1); // 1 finishes; its memory stays held until the caller releases it
+	s.tick(1); // 5 of 10 steps
+	s.tick(2); // 1 finishes; its memory stays held until the caller releases it
 	auto f = s.take_finished();
-	EXPECT(f.size() == 1 && f[0].tag == 1);
-	s.tick(2);
+	EXPECT(f.size() == 1 && !f.empty() && f[0].tag == 1);
+	s.tick(3);
 	EXPECT(s.active() == 0 && s.queued() == 1 && s.stats().refused == 0); // still waiting
-	be.release(f[0].ctx);
+	if (!f.empty())
+		be.release(f[0].ctx);
 	auto done = run(s, be);
 	EXPECT(find(done, 2) && find(done, 2)->status == Status::Done);
 	EXPECT(find(done, 2)->t_admit >= 0);
@@ -213,7 +222,8 @@ void cancellation()
 	Scheduler<FakeBackend> s(be, o);
 	s.submit(req(be, 1, 100, 10), 0);
 	s.submit(req(be, 2, 100, 10), 0);
-	s.tick(0);
+	s.tick(0); // admitted
+	s.tick(1); // 2 steps each
 	EXPECT(s.cancel(1, 1));  // active
 	EXPECT(!s.cancel(7, 1)); // unknown
 	s.submit(req(be, 3, 100, 10), 1);
@@ -236,9 +246,11 @@ void step_fault_fails_the_active_set()
 	s.submit(req(be, 1, 50, 10), 0);
 	s.submit(req(be, 2, 50, 10), 0);
 	be.fail_next_step = true;
-	s.tick(0);
+	s.tick(0); // admitted
+	s.tick(1); // the step fails
 	auto f = s.take_finished();
-	EXPECT(f.size() == 2 && f[0].status == Status::Failed && f[0].code == 4 && f[0].error == "device fault");
+	EXPECT(f.size() == 2 && !f.empty() && f[0].status == Status::Failed && f[0].code == 4 &&
+		   f[0].error == "device fault");
 	EXPECT(s.idle() && s.stats().active_bytes == 0);
 }
 

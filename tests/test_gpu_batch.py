@@ -107,6 +107,27 @@ def test_batch_yz_chunks(pcg, oracle_mod, chunk):
     _verify(problems, _run(pcg, oracle_mod, problems, 1, configure=cfg), 1)
 
 
+@pytest.mark.parametrize("graph", [True, False], ids=["graph", "direct"])
+def test_batch_step_budgets(pcg, oracle_mod, graph):
+    """Domains take part in only the first budgets[d] steps of a call: each matches
+    the oracle after exactly that many steps (0: untouched)."""
+    problems = _problems(range(10))
+    budgets = [0, 1, 5, 2, 7, 7, 3, 0, 6, 4]
+    batched = [W.apply(pcg.Solver(1), p) for p in problems]
+    b = pcg.Batch(batched)
+    b.set_graph(graph)
+    b.solve(7, budgets=budgets)
+    b.synchronize()
+    for p, g, n in zip(problems, batched, budgets):
+        o = W.apply(oracle_mod.OracleSolver(threads=2), p)
+        if n:
+            o.solve(n)
+        e = rel_err(g.get_field(), o.get_field())
+        assert e <= FP64_RTOL, f"{p['name']} budget {n}: {e:.3e}"
+        if g.A and n:
+            assert np.array_equal(g.get_counts(), o.get_counts()), p["name"]
+
+
 def test_batch_direct_launches(pcg, oracle_mod):
     problems = _problems(range(16, 24))
     _verify(problems, _run(pcg, oracle_mod, problems, 0, graph=False), 0)
