@@ -334,7 +334,8 @@ def run_batched(args, local, clock_sampler=None):
 
     b = pcg.Batch(solvers)
     t0 = time.perf_counter()
-    b.autotune()
+    if not args.no_batch_autotune:
+        b.autotune()
     b.synchronize()
     tune_s = time.perf_counter() - t0
     bs = torch.cuda.ExternalStream(b.stream())
@@ -434,7 +435,7 @@ def run_serve(args, local):
     th = threading.Thread(target=feed, daemon=True)
     t_start = time.perf_counter()
     th.start()
-    lat_dev, lat_host, statuses, vss_done = [], [], {}, 0
+    lat_dev, lat_host, statuses, vss_done, agent_steps = [], [], {}, 0, 0
     t_first = t_last = None
     got = 0
     while got < n and not err:
@@ -450,6 +451,7 @@ def run_serve(args, local):
                 lat_host.append(time.perf_counter() - submit_wall[i])
                 lat_dev.append(r["t_done"] - r["t_submit"])
                 vss_done += stream.vss(i)
+                agent_steps += int(stream.A[i]) * int(stream.steps[i])
                 t_first = r["t_submit"] if t_first is None else min(t_first, r["t_submit"])
                 t_last = r["t_done"] if t_last is None else max(t_last, r["t_done"])
             s.close()
@@ -467,6 +469,7 @@ def run_serve(args, local):
                         "[10,1000], FP32",
             "requests": n, "statuses": statuses, "offered_vss_per_s": offered,
             "value": vss_done / (t_last - t_first) if t_last else None, "unit": UNIT,
+            "agent_steps_per_s": agent_steps / (t_last - t_first) if t_last else None,
             "time_to_result_s": {"p50": q(lat_dev, 50), "p99": q(lat_dev, 99), "mean": float(np.mean(lat_dev))
                                  if lat_dev else None, "measured": "submit -> last step finished on the device"},
             "time_to_host_s": {"p50": q(lat_host, 50), "p99": q(lat_host, 99),
@@ -488,6 +491,7 @@ def main():
     ap.add_argument("--n", type=int, default=WORKLOAD["n"], help="grid side (default: the 320^3 workload)")
     ap.add_argument("--batch-domains", type=int, default=256, help="domains of the batched workload (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=200)
+    ap.add_argument("--no-batch-autotune", action="store_true", help="keep the default line mappings")
     ap.add_argument("--only-batched", action="store_true", help="run only the batched workload")
     ap.add_argument("--serve-duration", type=float, default=10.0, help="seconds of request arrivals (0: skip)")
     ap.add_argument("--serve-tick", type=int, default=8, help="steps between admission points")

@@ -61,6 +61,7 @@ enum : uint32_t
 constexpr uint32_t kMaxChunks = 64;        // y/z boxes per line (TMA operations per tile)
 constexpr uint64_t kClearChunk = 4096;     // voxels of the ballot counts cleared per warp item
 constexpr uint64_t kXSmemDefault = 32768;  // default shared-memory budget of an x tile
+constexpr double kTuneShare = 0.01;        // buckets below this share of an axis keep the defaults
 
 struct BatchDomain
 {
@@ -636,6 +637,7 @@ struct AxisConfig
 struct TuneRecord
 {
 	int axis;
+	double share; // of the axis' voxel-substrates
 	uint64_t n_bucket, S, domains;
 	AxisConfig best;
 	double best_us;
@@ -684,8 +686,9 @@ AxisConfig default_config(const Context* c, int axis)
 	AxisConfig a;
 	if (axis == 0)
 	{
-		a.mode = kMapRow;
-		a.rows = x_rows_cap(c, kMapRow, kXSmemDefault);
+		// measured on uneven batches: substrate-per-thread beats row-per-thread for every S
+		a.mode = c->S <= kLanes ? kMapSubstrate : kMapRow;
+		a.rows = x_rows_cap(c, a.mode, kXSmemDefault);
 		return a;
 	}
 	uint32_t R, nc;
@@ -1435,6 +1438,8 @@ int time_axis(pcg_batch* b, int axis, const std::vector<size_t>& subset, double*
 	}
 	BatchArgs a = args_for(b, axis, axis);
 	a.list = wl;
+	// every domain takes part in the timed launches
+	cudaMemsetAsync(b->d_steps_left.ptr, 0x01, b->ctx.size() * sizeof(uint32_t), b->stream);
 	cudaEvent_t e0, e1;
 	cudaEventCreate(&e0);
 	cudaEventCreate(&e1);
@@ -1473,15 +1478,11 @@ std::vector<AxisConfig> candidates(const Context* c, int axis)
 	};
 	if (axis == 0)
 	{
-		for (uint64_t budget : { (uint64_t)16384, (uint64_t)32768, (uint64_t)57344 })
+		if (c->S <= kLanes)
+			for (uint64_t budget : { (uint64_t)16384, (uint64_t)32768, (uint64_t)57344 })
+				add({ kMapSubstrate, x_rows_cap(c, kMapSubstrate, budget) });
+		for (uint64_t budget : { (uint64_t)32768, (uint64_t)57344 })
 			add({ kMapRow, x_rows_cap(c, kMapRow, budget) });
-		if (c->S > 1 && c->S <= 16)
-		{
-			const uint32_t cap = x_rows_cap(c, kMapSubstrate, 57344);
-			add({ kMapSubstrate, cap });
-			if (cap > 1)
-				add({ kMapSubstrate, std::max<uint32_t>(1, cap / 2) });
-		}
 		return out;
 	}
 	const uint64_t n = c->n[axis];
@@ -1528,10 +1529,38 @@ int autotune_t(pcg_batch* b)
 	for (size_t d = 0; d < N; d++)
 		cudaMemcpyAsync(static_cast<char*>(save.ptr) + off[d], C(b, d)->field.ptr,
 						C(b, d)->rows * C(b, d)->pitch * b->wsize, cudaMemcpyDeviceToDevice, b->stream);
+	// In context: a candidate is timed on the whole axis launch (every domain of the
+	// batch, the other buckets at their current choice), so that what is measured
+	// is the bucket's effect on the launch the batch will run, not the latency of a
+	// tiny launch.  Buckets are tuned in decreasing order of work; those below
+	// kTuneShare of the axis keep the default mapping (their effect is below the
+	// timing noise) and are not cached.
 	for (int axis = 0; axis < 3 && !rc; axis++)
+	{
+		if (todo[axis].empty())
+			continue;
+		std::vector<size_t> axis_doms;
+		double axis_work = 0;
+		for (size_t d = 0; d < N; d++)
+			if (axis < C(b, d)->dims)
+			{
+				axis_doms.push_back(d);
+				axis_work += (double)C(b, d)->V * (double)C(b, d)->S;
+			}
+		std::vector<std::pair<double, uint64_t>> order;
 		for (auto& kv : todo[axis])
 		{
-			const std::vector<size_t>& dom = kv.second;
+			double w = 0;
+			for (size_t d : kv.second)
+				w += (double)C(b, d)->V * (double)C(b, d)->S;
+			order.push_back({ -w, kv.first });
+		}
+		std::sort(order.begin(), order.end());
+		for (const auto& ow : order)
+		{
+			const std::vector<size_t>& dom = todo[axis][ow.second];
+			if (-ow.first < kTuneShare * axis_work)
+				continue;
 			Context* c0 = C(b, dom[0]);
 			TuneRecord rec {};
 			rec.axis = axis;
@@ -1539,7 +1568,7 @@ int autotune_t(pcg_batch* b)
 			rec.S = axis == 0 ? c0->S : 0;
 			rec.domains = dom.size();
 			rec.best_us = 1e300;
-			const std::vector<AxisConfig> saved = b->cfg[axis];
+			rec.share = -ow.first / axis_work;
 			for (const AxisConfig& cand : candidates(c0, axis))
 			{
 				for (size_t d : dom)
@@ -1555,7 +1584,7 @@ int autotune_t(pcg_batch* b)
 				if (rc || (rc = upload_domains(b)))
 					break;
 				double us = 0;
-				if ((rc = time_axis<T>(b, axis, dom, &us)))
+				if ((rc = time_axis<T>(b, axis, axis_doms, &us)))
 					break;
 				rec.tried.push_back({ cand, us });
 				if (us < rec.best_us)
@@ -1564,15 +1593,27 @@ int autotune_t(pcg_batch* b)
 					rec.best = cand;
 				}
 			}
-			b->cfg[axis] = saved;
+			if (rc)
+				break;
+			for (size_t d : dom) // keep the winner while the next buckets are timed
+			{
+				AxisConfig cf = rec.best;
+				Context* c = C(b, d);
+				cf.rows = axis == 0 ? std::min(cf.rows, x_rows_cap(c, cf.mode, kMaxSmemBytes - 16))
+									: fit_chunk(c->n[axis], cf.rows);
+				b->cfg[axis][d] = cf;
+				if (axis > 0 && (rc = encode_maps(b, d)))
+					break;
+			}
 			if (rc)
 				break;
 			{
 				std::lock_guard<std::mutex> lk(g_tune_mu);
-				g_tuned[kv.first] = rec.best;
+				g_tuned[ow.second] = rec.best;
 			}
 			b->tuned.push_back(rec);
 		}
+	}
 	for (size_t d = 0; d < N; d++)
 		cudaMemcpyAsync(C(b, d)->field.ptr, static_cast<char*>(save.ptr) + off[d],
 						C(b, d)->rows * C(b, d)->pitch * b->wsize, cudaMemcpyDeviceToDevice, b->stream);
@@ -1604,7 +1645,8 @@ std::string describe(pcg_batch* b)
 					   "\", \"rows_per_tile\": " + std::to_string(a.rows) + "}";
 			return std::string("{\"mapping\": \"column-per-lane\", \"box_points\": ") + std::to_string(a.rows) + "}";
 		};
-		s += "{\"axis\": " + std::to_string(r.axis) + ", \"line_bucket\": " + std::to_string(r.n_bucket) +
+		s += "{\"axis\": " + std::to_string(r.axis) + ", \"share\": " + std::to_string(r.share) +
+			 ", \"line_bucket\": " + std::to_string(r.n_bucket) +
 			 ", \"substrates\": " + std::to_string(r.S) + ", \"domains\": " + std::to_string(r.domains) +
 			 ", \"choice\": " + cfg_txt(r.best) + ", \"us\": " + std::to_string(r.best_us) + ", \"tried\": [";
 		for (size_t i = 0; i < r.tried.size(); i++)
