@@ -462,6 +462,24 @@ def run_serve(args, local):
     srv.close()
     if err:
         raise err[0]
+    # plain: a sample of the same requests, one after another through pcg_solve
+    # (create, solve all steps, read the field, destroy), on the same device
+    sample = list(range(0, n, max(1, n // args.serve_plain_sample)))[: args.serve_plain_sample]
+    cs = torch.cuda.Stream()
+    t0 = time.perf_counter()
+    vss_plain = 0
+    for i in sample:
+        s = stream.request(pcg.Solver(pcg.FP32, device=local), i)
+        s.set_stream(cs.cuda_stream)
+        s.initialize()
+        s.solve(int(stream.steps[i]))
+        nx, ny, nz = (int(v) for v in stream.sides[i])
+        S = int(stream.S[i])
+        s.get_field(layout=pcg.LAYOUT_PLANAR, dtype=np.float32, out=host[: S * nx * ny * nz].reshape(S, nz, ny, nx))
+        s.set_stream(None)
+        s.close()
+        vss_plain += stream.vss(i)
+    plain_s = time.perf_counter() - t0
     offered = sum(stream.vss(i) for i in range(n)) / args.serve_duration
     q = lambda a, p: float(np.percentile(a, p)) if len(a) else None
     return {"workload": f"served: Poisson arrivals at 200/s for {args.serve_duration:g} s ({n} requests), sides "
@@ -470,6 +488,10 @@ def run_serve(args, local):
             "requests": n, "statuses": statuses, "offered_vss_per_s": offered,
             "value": vss_done / (t_last - t_first) if t_last else None, "unit": UNIT,
             "agent_steps_per_s": agent_steps / (t_last - t_first) if t_last else None,
+            "plain": {"value": vss_plain / plain_s, "requests": len(sample),
+                      "path": "the same requests (an even sample) one after another: pcg_create, pcg_solve(steps), "
+                              "pcg_get_field, pcg_destroy"},
+            "speedup_vs_plain": (vss_done / (t_last - t_first)) / (vss_plain / plain_s) if t_last else None,
             "time_to_result_s": {"p50": q(lat_dev, 50), "p99": q(lat_dev, 99), "mean": float(np.mean(lat_dev))
                                  if lat_dev else None, "measured": "submit -> last step finished on the device"},
             "time_to_host_s": {"p50": q(lat_host, 50), "p99": q(lat_host, 99),
@@ -496,6 +518,7 @@ def main():
     ap.add_argument("--serve-duration", type=float, default=10.0, help="seconds of request arrivals (0: skip)")
     ap.add_argument("--serve-tick", type=int, default=8, help="steps between admission points")
     ap.add_argument("--only-serve", action="store_true", help="run only the served request stream")
+    ap.add_argument("--serve-plain-sample", type=int, default=100, help="requests timed one after another")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

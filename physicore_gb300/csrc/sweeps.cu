@@ -205,7 +205,9 @@ __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 // S elements apart in shared memory, with the compressed coefficients of s (most
 // points need no coefficient load).  Row pitches are chosen so that the lanes of
 // a warp touch distinct banks.
-template <typename T>
+// ST = S when it is a compile-time constant (stride-S shared-memory accesses with
+// immediate offsets), 0 for the run-time path.
+template <typename T, int ST>
 __global__ void __launch_bounds__(kLanes) sweep_x_sub_kernel(SweepArgs a)
 {
 	extern __shared__ __align__(128) unsigned char smem[];
@@ -213,7 +215,7 @@ __global__ void __launch_bounds__(kLanes) sweep_x_sub_kernel(SweepArgs a)
 	uint32_t& ticket = *reinterpret_cast<uint32_t*>(smem + 8);
 	T* tile = reinterpret_cast<T*>(smem + 16);
 	const uint32_t tid = threadIdx.x;
-	const uint32_t R = a.rows_per_tile, S = a.S, n = a.n;
+	const uint32_t R = a.rows_per_tile, S = ST ? (uint32_t)ST : a.S, n = a.n;
 	const uint32_t r_local = tid / S, s = tid % S;
 	const uint32_t row_bytes = (uint32_t)round_up(a.row_len * sizeof(T), 16);
 	const LineCoef<T> L = line_coef<T>(static_cast<const T*>(a.coef) + a.comp_off, S, a.head, n, s);
@@ -246,7 +248,7 @@ __global__ void __launch_bounds__(kLanes) sweep_x_sub_kernel(SweepArgs a)
 			break;
 		}
 		if (r_local < nrows)
-			solve_line<T, 0>(tile + r_local * a.smem_pitch + s, n, S, L);
+			solve_line<T, ST>(tile + r_local * a.smem_pitch + s, n, S, L);
 		dev::fence_proxy_async_smem();
 		__syncthreads();
 		if (tid < nrows)
@@ -352,7 +354,16 @@ int run_sweep_x(Context* c)
 	a.tiles = (c->rows + p.rows_per_tile - 1) / p.rows_per_tile;
 	const double bytes = 2.0 * (double)(c->V * c->S) * (double)sizeof(T);
 	if (sub)
-		return launch_persistent(c, sweep_x_sub_kernel<T>, a, p, K_SWEEP_X, bytes);
+		switch (c->S)
+		{
+		case 3: return launch_persistent(c, sweep_x_sub_kernel<T, 3>, a, p, K_SWEEP_X, bytes);
+		case 4: return launch_persistent(c, sweep_x_sub_kernel<T, 4>, a, p, K_SWEEP_X, bytes);
+		case 5: return launch_persistent(c, sweep_x_sub_kernel<T, 5>, a, p, K_SWEEP_X, bytes);
+		case 6: return launch_persistent(c, sweep_x_sub_kernel<T, 6>, a, p, K_SWEEP_X, bytes);
+		case 7: return launch_persistent(c, sweep_x_sub_kernel<T, 7>, a, p, K_SWEEP_X, bytes);
+		case 8: return launch_persistent(c, sweep_x_sub_kernel<T, 8>, a, p, K_SWEEP_X, bytes);
+		default: return launch_persistent(c, sweep_x_sub_kernel<T, 0>, a, p, K_SWEEP_X, bytes);
+		}
 	switch (c->S)
 	{
 	case 1: return launch_persistent(c, sweep_x_kernel<T, 1>, a, p, K_SWEEP_X, bytes);
