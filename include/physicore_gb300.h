@@ -323,7 +323,7 @@ int pcg_server_get_stats(pcg_server* server, pcg_server_stats* stats);
  *    synchronises that stream to report device faults (PCG_ERR_DEVICE).
  *  - Scratch comes from one fixed 16 MiB array in device memory that every GPU
  *    loading this library holds until the process exits; a problem that needs
- *    more (about 8 bytes per voxel plus 8 + 24*substrates bytes per agent) is
+ *    more (about 8 bytes per voxel plus 13 + 24*substrates bytes per agent) is
  *    rejected with PCG_ERR_UNSUPPORTED.  The first call on a device looks up the
  *    array's device address, so make that first call before any stream capture.
  *  - All calls share the array: calls that overlap on the GPU (other streams,

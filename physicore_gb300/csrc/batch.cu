@@ -524,7 +524,7 @@ __global__ void batch_cells_locate_kernel(BatchArgs b)
 	const CellArgs& a = b.doms[di].cells;
 	const uint64_t i = u - __ldg(b.list.base + k);
 	if (i == 0)
-		a.flags[0] = 0;
+		a.flags[0] = a.flags[1] = 0;
 	agent_locate<T>(a, i);
 }
 
@@ -563,23 +563,24 @@ template <typename T>
 __global__ void batch_cells_reduce_kernel(BatchArgs b)
 {
 	const uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-	bool conflict = false;
+	uint8_t role = kRoleNone;
 	uint32_t di = 0;
+	uint64_t i = 0;
 	const uint32_t k = warp_entry(b.list, u);
 	if (u < b.list.total)
 	{
 		di = __ldg(b.list.dom + k);
 		if (b.recompute[di] && b.steps_left[di])
 		{
-			const CellArgs& a = b.doms[di].cells;
-			const uint64_t i = u - __ldg(b.list.base + k);
-			const uint32_t v = a.vox[i];
-			conflict = v != kNoAgent && agent_reduce<T>(a, i, v);
+			i = u - __ldg(b.list.base + k);
+			role = agent_reduce<T>(b.doms[di].cells, i);
 		}
 	}
+	const bool conflict = role == kRoleLoser;
 	const uint32_t group = __match_any_sync(0xffffffffu, conflict ? di : 0xffffffffu);
 	if (conflict && (threadIdx.x & 31) == (uint32_t)(__ffs(group) - 1))
 		atomicOr(b.doms[di].cells.flags, 1u);
+	list_shared(b.doms[di].cells, i, role == kRoleWinner || role == kRoleLoser, di);
 }
 
 template <typename T>
@@ -600,8 +601,10 @@ __global__ void batch_cells_internalize_kernel(BatchArgs b)
 	if (u >= b.list.total || !b.steps_left[__ldg(b.list.dom + k)])
 		return;
 	const CellArgs& a = b.doms[__ldg(b.list.dom + k)].cells;
-	if (a.internalized)
-		agent_internalize<T>(a, u - __ldg(b.list.base + k));
+	// the first flags[1] agent slots of a domain take its list of agents in shared voxels
+	const uint64_t j = u - __ldg(b.list.base + k);
+	if (a.internalized && j < __ldg(a.flags + 1))
+		agent_internalize<T>(a, __ldg(a.shared + j));
 }
 
 // End of a step: one step fewer for every domain still running.
@@ -1082,9 +1085,9 @@ int build_t(pcg_batch* b)
 		{
 			b->rebuild_bytes[d] = { 4.0 * V, A * (8.0 * c->dims + 1 + 5 * S * 8 + 8 + 6 * S * w + 4), A * 12,
 									A * (8 + 6 * S * w) };
-			b->step_bytes[K_CELLS_APPLY] += A * (8 + 5 * S * w + (c->compute_internalized ? 16 * S : 0));
+			b->step_bytes[K_CELLS_APPLY] += A * (5 + 5 * S * w + (c->compute_internalized ? 16 * S : 0));
 			if (c->compute_internalized)
-				b->step_bytes[K_CELLS_INTERNALIZE] += A * (8 + 4 * S * w + 16 * S);
+				b->step_bytes[K_CELLS_INTERNALIZE] += 4; // agents sharing a voxel not counted
 		}
 	}
 	b->built = true;

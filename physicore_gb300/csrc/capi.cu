@@ -518,6 +518,10 @@ static int alloc_agents(Context* c, uint64_t A)
 		return rc;
 	if ((rc = dalloc(c, c->a_vox, std::max<uint64_t>(A, 1) * sizeof(uint32_t))))
 		return rc;
+	if ((rc = dalloc(c, c->a_role, std::max<uint64_t>(A, 1))))
+		return rc;
+	if ((rc = dalloc(c, c->a_shared, std::max<uint64_t>(A, 1) * sizeof(uint32_t))))
+		return rc;
 	DeviceBuffer* rs[] = { &c->a_num, &c->a_den, &c->a_fac, &c->a_rnum, &c->a_rden, &c->a_rfac };
 	for (DeviceBuffer* b : rs)
 		if ((rc = dalloc(c, *b, std::max<uint64_t>(A * S, 1) * w)))
@@ -587,7 +591,7 @@ uint64_t estimate_device_bytes(const Context* c)
 	else if (c->bulk_mode == PCG_BULK_PER_VOXEL)
 		b += 3 * rows * pitch * w;
 	if (A)
-		b += A * (c->dims * 8 + 6 * S * 8 + 8 + 1 + 8 + 6 * S * w) + V * 8;
+		b += A * (c->dims * 8 + 6 * S * 8 + 8 + 1 + 8 + 5 + 6 * S * w) + V * 8;
 	return b;
 }
 
@@ -650,7 +654,7 @@ int pcg_destroy(pcg_context* c)
 								 &c->a_sec,		 &c->a_sat,		&c->a_upt,		&c->a_net,		 &c->a_vol,
 								 &c->a_active,	 &c->a_internal, &c->a_frac,	&c->a_foff,		 &c->a_num,
 								 &c->a_den,		 &c->a_fac,		&c->a_rnum,		&c->a_rden,		 &c->a_rfac,
-								 &c->owner,		 &c->counts };
+								 &c->owner,		 &c->counts,	&c->a_role,		&c->a_shared };
 	for (auto* b : all)
 		pcg::dfree(*b);
 	for (cudaEvent_t e : c->event_pool)

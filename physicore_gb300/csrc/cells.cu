@@ -38,7 +38,7 @@ __global__ void cells_locate_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	if (i == 0)
-		a.flags[0] = 0;
+		a.flags[0] = a.flags[1] = 0;
 	if (i < a.A)
 		agent_locate<T>(a, i);
 }
@@ -55,10 +55,10 @@ template <typename T>
 __global__ void cells_reduce_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-	const uint32_t key = i < a.A ? a.vox[i] : kNoAgent;
-	const bool conflict = key != kNoAgent && agent_reduce<T>(a, i, key);
-	if (__any_sync(0xffffffffu, conflict) && (threadIdx.x & 31) == 0)
+	const uint8_t role = i < a.A ? agent_reduce<T>(a, i) : kRoleNone;
+	if (__any_sync(0xffffffffu, role == kRoleLoser) && (threadIdx.x & 31) == 0)
 		atomicOr(a.flags, 1u);
+	list_shared(a, i, role == kRoleWinner || role == kRoleLoser, 0);
 }
 
 template <typename T>
@@ -69,12 +69,13 @@ __global__ void cells_apply_kernel(CellArgs a)
 		agent_apply<T>(a, i);
 }
 
+// Over the list of agents in shared voxels (empty when there was no conflict).
 template <typename T>
 __global__ void cells_internalize_kernel(CellArgs a)
 {
-	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-	if (i < a.A)
-		agent_internalize<T>(a, i);
+	const uint32_t count = __ldg(a.flags + 1);
+	for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < count; j += (uint64_t)gridDim.x * blockDim.x)
+		agent_internalize<T>(a, __ldg(a.shared + j));
 }
 
 // release_internal (cell_solver.cpp:274-289) for one agent
@@ -134,6 +135,8 @@ CellArgs make_cell_args(const Context* c)
 	a.rfac = c->a_rfac.ptr;
 	a.owner = static_cast<uint32_t*>(c->owner.ptr);
 	a.counts = static_cast<uint32_t*>(c->counts.ptr);
+	a.role = static_cast<uint8_t*>(c->a_role.ptr);
+	a.shared = static_cast<uint32_t*>(c->a_shared.ptr);
 	a.flags = static_cast<uint32_t*>(c->flags.ptr);
 	a.err = static_cast<uint32_t*>(c->err.ptr);
 	a.field = c->field.ptr;
@@ -169,16 +172,18 @@ static int run_cells(Context* c, bool recompute)
 		launch_end(c, K_CELLS_REDUCE, ev);
 		PCG_CUDA_TRY(cudaGetLastError());
 	}
-	// per active agent: voxel index, offset, reduced terms, density read+write
-	launch_begin(c, K_CELLS_APPLY, A * (8 + 3 * S * w + 2 * S * w + (c->compute_internalized ? 16 * S : 0)), &ev);
+	// per agent: role, offset, summed (or own) terms, density read+write
+	launch_begin(c, K_CELLS_APPLY, A * (5 + 3 * S * w + 2 * S * w + (c->compute_internalized ? 16 * S : 0)), &ev);
 	cells_apply_kernel<T><<<grid, block, 0, c->stream>>>(a);
 	launch_end(c, K_CELLS_APPLY, ev);
 	PCG_CUDA_TRY(cudaGetLastError());
 	if (c->compute_internalized)
 	{
-		// after a conflict: own terms, density read, internalized read+write
-		launch_begin(c, K_CELLS_INTERNALIZE, A * (8 + 3 * S * w + S * w + 16 * S), &ev);
-		cells_internalize_kernel<T><<<grid, block, 0, c->stream>>>(a);
+		// the agents that share a voxel (a few percent at 1e6 agents in 320^3 voxels)
+		// read their own terms and density and rewrite their internalized amounts:
+		// not counted, only the list length is
+		launch_begin(c, K_CELLS_INTERNALIZE, 4, &ev);
+		cells_internalize_kernel<T><<<std::min<unsigned>(grid, 8 * std::max(c->sm_count, 1)), block, 0, c->stream>>>(a);
 		launch_end(c, K_CELLS_INTERNALIZE, ev);
 		PCG_CUDA_TRY(cudaGetLastError());
 	}
@@ -228,6 +233,8 @@ int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream)
 	a.rfac = b.rfac;
 	a.owner = b.owner;
 	a.counts = b.counts;
+	a.role = b.role;
+	a.shared = b.shared;
 	a.flags = b.flags;
 	a.err = b.err;
 	a.field = b.field;

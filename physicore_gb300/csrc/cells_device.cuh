@@ -18,6 +18,15 @@ namespace cellsdev {
 constexpr uint32_t kNoAgent = 0xffffffffu;
 constexpr int kSubBatch = 8; // substrates whose loads are issued together
 
+// Ballot role of an agent, recorded by agent_reduce whenever the ballot is rebuilt.
+enum : uint8_t
+{
+	kRoleNone = 0,   // inactive or outside the grid
+	kRoleAlone = 1,  // the only agent of its voxel
+	kRoleWinner = 2, // winner of a voxel that holds several agents
+	kRoleLoser = 3,  // any other agent of such a voxel (a ballot conflict)
+};
+
 struct CellArgs
 {
 	int dims;
@@ -35,7 +44,9 @@ struct CellArgs
 	void *num, *den, *fac, *rnum, *rden, *rfac;
 	uint32_t* owner;
 	uint32_t* counts;
-	uint32_t* flags; // [0] conflict
+	uint8_t* role;    // [A] ballot role
+	uint32_t* shared; // [A] agents of voxels that hold several, flags[1] of them
+	uint32_t* flags;  // [0] conflict, [1] entries of `shared`
 	uint32_t* err;
 	void* field;
 	int internalized;
@@ -112,13 +123,28 @@ __device__ __forceinline__ void warp_ballot(const CellArgs* a, uint64_t i, uint3
 	}
 }
 
-// Sums into the winner's row (cell_solver.cpp:102-127); returns true when agent i
-// is not its voxel's winner (a ballot conflict).
+// Sums into the winner's row (cell_solver.cpp:102-127) and records agent i's
+// role, which it returns (kRoleLoser: a ballot conflict).  An agent alone in its
+// voxel adds nothing: its sums would be its own terms (0 + x, exactly), which
+// agent_apply reads in their place.
 template <typename T>
-__device__ __forceinline__ bool agent_reduce(const CellArgs& a, uint64_t i, uint32_t v)
+__device__ __forceinline__ uint8_t agent_reduce(const CellArgs& a, uint64_t i)
 {
+	const uint32_t v = a.vox[i];
+	if (v == kNoAgent)
+	{
+		a.role[i] = kRoleNone;
+		return kRoleNone;
+	}
 	const uint32_t w = a.owner[v];
 	const bool conflict = w != (uint32_t)i;
+	if (!conflict && a.counts[v] == 1)
+	{
+		a.role[i] = kRoleAlone;
+		return kRoleAlone;
+	}
+	const uint8_t role = conflict ? kRoleLoser : kRoleWinner;
+	a.role[i] = role;
 	const T* num = static_cast<const T*>(a.num);
 	const T* den = static_cast<const T*>(a.den);
 	const T* fac = static_cast<const T*>(a.fac);
@@ -133,25 +159,65 @@ __device__ __forceinline__ bool agent_reduce(const CellArgs& a, uint64_t i, uint
 		atomicAdd(rden + kw, conflict ? den[k] : den[k] + T(1));
 		atomicAdd(rfac + kw, fac[k]);
 	}
-	return conflict;
+	return role;
+}
+
+// Appends agent i to the list of agents in shared voxels, one atomic per group of
+// lanes with the same `key` (the lanes of one domain).  All lanes of the warp call it.
+__device__ __forceinline__ void list_shared(const CellArgs& a, uint64_t i, bool shared, uint32_t key)
+{
+	const uint32_t group = __match_any_sync(0xffffffffu, shared ? key : 0xffffffffu);
+	if (!shared)
+		return;
+	const uint32_t lane = threadIdx.x & 31, leader = __ffs(group) - 1;
+	uint32_t base = 0;
+	if (lane == leader)
+		base = atomicAdd(a.flags + 1, (uint32_t)__popc(group));
+	base = __shfl_sync(group, base, leader);
+	a.shared[base + __popc(group & ((1u << lane) - 1))] = (uint32_t)i;
+}
+
+// Change of an internalized amount.  The FP64 build evaluates the reference's
+// expressions in FP64 in its order: fused Vv (D - D') (cell_solver.cpp:166-185),
+// after a conflict -Vv (num - D' den + fac) (cell_solver.cpp:132-143).  The FP32
+// build evaluates them in FP32 (the product inside one fma) and only the
+// accumulation into the FP64 amount in FP64: double-precision arithmetic runs at a
+// small fraction of the single-precision rate on this GPU.
+__device__ __forceinline__ double fused_delta(double Vv, double D, double Dn) { return Vv * (D - Dn); }
+__device__ __forceinline__ double fused_delta(double Vv, float D, float Dn) { return (double)((float)Vv * (D - Dn)); }
+__device__ __forceinline__ double conflict_delta(double Vv, double n, double Dn, double d, double f)
+{
+	return -(Vv * (n - Dn * d + f));
+}
+__device__ __forceinline__ double conflict_delta(double Vv, float n, float Dn, float d, float f)
+{
+	return (double)(-(float)Vv * (fmaf(-Dn, d, n) + f));
 }
 
 // compute_result (cell_solver.cpp:187-227) for agent i.  All loads of a batch of
 // substrates are issued before any store, so an agent's accesses overlap.
+//
+// The winner of a voxel writes its new density from the voxel's sums: for an
+// agent alone in its voxel these are its own terms (num, 1 + den, fac, with the
+// 1 added in T as the ballot does).  Internalized amounts: when no voxel holds two
+// agents, the reference's fused update I += Vv (D - D'); otherwise every agent's
+// I -= Vv (num - D' den + fac) from the final density of its voxel
+// (cell_solver.cpp:229-243).  An agent alone in its voxel has just written that
+// final density itself, so it applies the update here, from the same values, and
+// agent_internalize takes only the agents of shared voxels.
 template <typename T>
 __device__ __forceinline__ void agent_apply(const CellArgs& a, uint64_t i)
 {
-	const uint32_t key = a.vox[i];
-	if (key == kNoAgent)
+	const uint8_t role = a.role[i];
+	if (role == kRoleNone || role == kRoleLoser)
 		return;
-	const uint32_t off = a.foff[i];
-	const bool fused = a.internalized && *(volatile uint32_t*)a.flags == 0;
-	if (!fused && a.owner[key] != (uint32_t)i)
-		return;
-	T* __restrict__ D = static_cast<T*>(a.field) + off;
-	const T* __restrict__ rn = static_cast<const T*>(a.rnum) + i * a.S;
-	const T* __restrict__ rd = static_cast<const T*>(a.rden) + i * a.S;
-	const T* __restrict__ rf = static_cast<const T*>(a.rfac) + i * a.S;
+	const bool alone = role == kRoleAlone;
+	const bool track = alone && a.internalized;
+	const bool fused = track && __ldg(a.flags) == 0;
+	T* __restrict__ D = static_cast<T*>(a.field) + a.foff[i];
+	const T* __restrict__ rn = static_cast<const T*>(alone ? a.num : a.rnum) + i * a.S;
+	const T* __restrict__ rd = static_cast<const T*>(alone ? a.den : a.rden) + i * a.S;
+	const T* __restrict__ rf = static_cast<const T*>(alone ? a.fac : a.rfac) + i * a.S;
 	double* __restrict__ I = a.internal + i * a.S;
 	for (uint32_t s0 = 0; s0 < a.S; s0 += kSubBatch)
 	{
@@ -165,27 +231,28 @@ __device__ __forceinline__ void agent_apply(const CellArgs& a, uint64_t i)
 				n_[q] = rn[s0 + q];
 				d_[q] = rd[s0 + q];
 				f_[q] = rf[s0 + q];
-				if (fused)
+				if (track)
 					iv[q] = I[s0 + q];
 			}
 #pragma unroll
 		for (int q = 0; q < kSubBatch; q++)
 			if (s0 + q < a.S)
 			{
-				const T next = (dv[q] + n_[q]) / d_[q] + f_[q];
+				const T next = (dv[q] + n_[q]) / (alone ? d_[q] + T(1) : d_[q]) + f_[q];
 				D[s0 + q] = next;
 				if (fused)
-					I[s0 + q] = iv[q] + a.Vv * ((double)dv[q] - (double)next);
+					I[s0 + q] = iv[q] + fused_delta(a.Vv, dv[q], next);
+				else if (track)
+					I[s0 + q] = iv[q] + conflict_delta(a.Vv, n_[q], next, d_[q], f_[q]);
 			}
 	}
 }
 
-// compute_internalized after a conflict (cell_solver.cpp:229-243) for agent i.
+// compute_internalized after a conflict (cell_solver.cpp:229-243) for agent i of
+// a voxel that holds several agents (an entry of the shared list).
 template <typename T>
 __device__ __forceinline__ void agent_internalize(const CellArgs& a, uint64_t i)
 {
-	if (*(volatile uint32_t*)a.flags == 0 || a.vox[i] == kNoAgent)
-		return;
 	const T* __restrict__ D = static_cast<const T*>(a.field) + a.foff[i];
 	const T* __restrict__ nu = static_cast<const T*>(a.num) + i * a.S;
 	const T* __restrict__ de = static_cast<const T*>(a.den) + i * a.S;
@@ -208,7 +275,7 @@ __device__ __forceinline__ void agent_internalize(const CellArgs& a, uint64_t i)
 #pragma unroll
 		for (int q = 0; q < kSubBatch; q++)
 			if (s0 + q < a.S)
-				I[s0 + q] = iv[q] - a.Vv * ((double)n_[q] - (double)dv[q] * (double)d_[q] + (double)f_[q]);
+				I[s0 + q] = iv[q] + conflict_delta(a.Vv, n_[q], dv[q], d_[q], f_[q]);
 	}
 }
 

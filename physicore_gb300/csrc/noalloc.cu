@@ -14,8 +14,9 @@
 
 namespace {
 
-// 16 MiB of scratch: 8 bytes per voxel (ballot slot + count) plus 8 + 24*S bytes
-// per agent (voxel index, field offset, six FP32 terms per substrate) plus 32.
+// 16 MiB of scratch: 8 bytes per voxel (ballot slot + count) plus 13 + 24*S bytes
+// per agent (voxel index, field offset, shared-voxel list entry, ballot role, six
+// FP32 terms per substrate).
 constexpr size_t kScratchBytes = size_t(16) << 20;
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
@@ -74,7 +75,7 @@ extern "C" int pcg_cells_noalloc(float* field, uint64_t pitch, int dims, const i
 	if (agents == 0)
 		return PCG_OK;
 
-	// scratch layout: flags | err | owner[V] | counts[V] | vox[A] | foff[A] | 6 x terms[A*S]
+	// scratch layout: flags | err | owner[V] | counts[V] | vox[A] | foff[A] | shared[A] | role[A] | 6 x terms[A*S]
 	const size_t terms = agents * substrates * sizeof(float);
 	size_t off = 0;
 	const size_t o_flags = off;
@@ -89,6 +90,10 @@ extern "C" int pcg_cells_noalloc(float* field, uint64_t pitch, int dims, const i
 	off = align256(off + agents * 4);
 	const size_t o_foff = off;
 	off = align256(off + agents * 4);
+	const size_t o_shared = off;
+	off = align256(off + agents * 4);
+	const size_t o_role = off;
+	off = align256(off + agents);
 	size_t o_terms[6];
 	for (int k = 0; k < 6; k++)
 	{
@@ -99,7 +104,7 @@ extern "C" int pcg_cells_noalloc(float* field, uint64_t pitch, int dims, const i
 		return fail(PCG_ERR_UNSUPPORTED,
 					"pcg_cells_noalloc: the mesh and agents need " + std::to_string(off) +
 						" bytes of scratch, more than the fixed " + std::to_string(kScratchBytes) +
-						" (about 8 bytes per voxel + (8 + 24*S) bytes per agent)");
+						" (about 8 bytes per voxel + (13 + 24*S) bytes per agent)");
 
 	int device = 0;
 	cudaError_t e = cudaGetDevice(&device);
@@ -138,6 +143,8 @@ extern "C" int pcg_cells_noalloc(float* field, uint64_t pitch, int dims, const i
 	b.counts = reinterpret_cast<uint32_t*>(base + o_counts);
 	b.vox = reinterpret_cast<uint32_t*>(base + o_vox);
 	b.foff = reinterpret_cast<uint32_t*>(base + o_foff);
+	b.shared = reinterpret_cast<uint32_t*>(base + o_shared);
+	b.role = base + o_role;
 	float** t[6] = { &b.num, &b.den, &b.fac, &b.rnum, &b.rden, &b.rfac };
 	for (int k = 0; k < 6; k++)
 		*t[k] = reinterpret_cast<float*>(base + o_terms[k]);

@@ -227,6 +227,8 @@ struct Context
 	// cell scratch
 	DeviceBuffer a_vox;                   // uint32 [A]: linear voxel index (x + nx*(y + ny*z)), or ~0
 	DeviceBuffer a_foff;                  // uint32 [A]: field offset of the voxel's first substrate
+	DeviceBuffer a_role;                  // uint8 [A]: ballot role (cells_device.cuh)
+	DeviceBuffer a_shared;                // uint32 [A]: agents of voxels that hold several
 	DeviceBuffer a_num, a_den, a_fac;     // real [A*S]
 	DeviceBuffer a_rnum, a_rden, a_rfac;  // real [A*S]
 	DeviceBuffer owner;                   // uint32 [V]: winning agent per voxel
@@ -284,8 +286,9 @@ struct CellStepBuffers
 	double* internal;
 	int internalized;
 	float* field;
-	// scratch: vox/foff [A], owner/counts [V], flags/err [4] each, terms [A*S] each
-	uint32_t *vox, *foff, *owner, *counts, *flags, *err;
+	// scratch: vox/foff/shared/role [A], owner/counts [V], flags/err [4] each, terms [A*S] each
+	uint32_t *vox, *foff, *shared, *owner, *counts, *flags, *err;
+	uint8_t* role;
 	float *num, *den, *fac, *rnum, *rden, *rfac;
 };
 int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream);
