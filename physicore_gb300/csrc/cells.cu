@@ -141,6 +141,7 @@ CellArgs make_cell_args(const Context* c)
 	a.err = static_cast<uint32_t*>(c->err.ptr);
 	a.field = c->field.ptr;
 	a.internalized = c->compute_internalized ? 1 : 0;
+	a.vec = rows_vectorizable(a, c->wsize);
 	return a;
 }
 
@@ -239,6 +240,7 @@ int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream)
 	a.err = b.err;
 	a.field = b.field;
 	a.internalized = b.internalized;
+	a.vec = rows_vectorizable(a, sizeof(float));
 	const uint64_t V = b.n[0] * b.n[1] * b.n[2];
 	const unsigned block = 256;
 	const unsigned grid = (unsigned)((b.A + block - 1) / block);

@@ -50,10 +50,20 @@ struct CellArgs
 	uint32_t* err;
 	void* field;
 	int internalized;
+	int vec; // rows of S values start on 16-byte boundaries and S is a multiple of 16 / sizeof(T)
 };
 
 // Cell arguments of a context's own buffers (cells.cu).
 CellArgs make_cell_args(const Context* c);
+
+// Whether the rows of S values of `a` (field, terms, internalized) all start on
+// 16-byte boundaries, for 16-byte accesses.
+inline int rows_vectorizable(const CellArgs& a, size_t wsize)
+{
+	auto al = [](const void* p) { return p == nullptr || reinterpret_cast<uintptr_t>(p) % 16 == 0; };
+	return a.S % (16 / wsize) == 0 && (a.pitch * wsize) % 16 == 0 && al(a.field) && al(a.internal) && al(a.num) &&
+		   al(a.den) && al(a.fac) && al(a.rnum) && al(a.rden) && al(a.rfac);
+}
 
 // cartesian_mesh::voxel_position (mesh.cpp:37-61) in FP64; false when outside the grid.
 __device__ __forceinline__ bool locate(const CellArgs& a, uint64_t i, uint64_t idx[3])
@@ -194,7 +204,67 @@ __device__ __forceinline__ double conflict_delta(double Vv, float n, float Dn, f
 	return (double)(-(float)Vv * (fmaf(-Dn, d, n) + f));
 }
 
-// compute_result (cell_solver.cpp:187-227) for agent i.  All loads of a batch of
+// Accesses to values s0 .. s0 + kSubBatch - 1 (those below S) of an agent's row.
+// With `vec` they are 16-byte accesses: the rows of a warp's agents are scattered,
+// so an access costs an L1 wavefront per lane whatever its width, and 16-byte ones
+// need a quarter (FP32) or half (FP64) as many.
+template <typename T>
+__device__ __forceinline__ void row_load(const T* __restrict__ p, uint32_t s0, uint32_t S, bool vec, T (&v)[kSubBatch])
+{
+	constexpr int L = 16 / sizeof(T);
+	if (vec)
+	{
+#pragma unroll
+		for (int q = 0; q < kSubBatch; q += L)
+			if (s0 + q < S)
+			{
+				union
+				{
+					uint4 u;
+					T t[L];
+				} x;
+				x.u = *reinterpret_cast<const uint4*>(p + s0 + q);
+#pragma unroll
+				for (int r = 0; r < L; r++)
+					v[q + r] = x.t[r];
+			}
+		return;
+	}
+#pragma unroll
+	for (int q = 0; q < kSubBatch; q++)
+		if (s0 + q < S)
+			v[q] = p[s0 + q];
+}
+
+template <typename T>
+__device__ __forceinline__ void row_store(T* __restrict__ p, uint32_t s0, uint32_t S, bool vec, const T (&v)[kSubBatch])
+{
+	constexpr int L = 16 / sizeof(T);
+	if (vec)
+	{
+#pragma unroll
+		for (int q = 0; q < kSubBatch; q += L)
+			if (s0 + q < S)
+			{
+				union
+				{
+					uint4 u;
+					T t[L];
+				} x;
+#pragma unroll
+				for (int r = 0; r < L; r++)
+					x.t[r] = v[q + r];
+				*reinterpret_cast<uint4*>(p + s0 + q) = x.u;
+			}
+		return;
+	}
+#pragma unroll
+	for (int q = 0; q < kSubBatch; q++)
+		if (s0 + q < S)
+			p[s0 + q] = v[q];
+}
+
+// compute_result (cell_solver.cpp:188-244) for agent i.  All loads of a batch of
 // substrates are issued before any store, so an agent's accesses overlap.
 //
 // The winner of a voxel writes its new density from the voxel's sums: for an
@@ -209,73 +279,71 @@ template <typename T>
 __device__ __forceinline__ void agent_apply(const CellArgs& a, uint64_t i)
 {
 	const uint8_t role = a.role[i];
+	const uint32_t off = a.foff[i];
 	if (role == kRoleNone || role == kRoleLoser)
 		return;
 	const bool alone = role == kRoleAlone;
 	const bool track = alone && a.internalized;
 	const bool fused = track && __ldg(a.flags) == 0;
-	T* __restrict__ D = static_cast<T*>(a.field) + a.foff[i];
-	const T* __restrict__ rn = static_cast<const T*>(alone ? a.num : a.rnum) + i * a.S;
-	const T* __restrict__ rd = static_cast<const T*>(alone ? a.den : a.rden) + i * a.S;
-	const T* __restrict__ rf = static_cast<const T*>(alone ? a.fac : a.rfac) + i * a.S;
-	double* __restrict__ I = a.internal + i * a.S;
-	for (uint32_t s0 = 0; s0 < a.S; s0 += kSubBatch)
+	const bool vec = a.vec;
+	const uint32_t S = (uint32_t)a.S;
+	T* __restrict__ D = static_cast<T*>(a.field) + off;
+	const T* __restrict__ rn = static_cast<const T*>(alone ? a.num : a.rnum) + i * S;
+	const T* __restrict__ rd = static_cast<const T*>(alone ? a.den : a.rden) + i * S;
+	const T* __restrict__ rf = static_cast<const T*>(alone ? a.fac : a.rfac) + i * S;
+	double* __restrict__ I = a.internal + i * S;
+	for (uint32_t s0 = 0; s0 < S; s0 += kSubBatch)
 	{
-		T dv[kSubBatch], n_[kSubBatch], d_[kSubBatch], f_[kSubBatch];
+		T dv[kSubBatch], n_[kSubBatch], d_[kSubBatch], f_[kSubBatch], nx[kSubBatch];
 		double iv[kSubBatch];
+		row_load(D, s0, S, vec, dv);
+		row_load(rn, s0, S, vec, n_);
+		row_load(rd, s0, S, vec, d_);
+		row_load(rf, s0, S, vec, f_);
+		if (track)
+			row_load(I, s0, S, vec, iv);
 #pragma unroll
 		for (int q = 0; q < kSubBatch; q++)
-			if (s0 + q < a.S)
+			if (s0 + q < S)
 			{
-				dv[q] = D[s0 + q];
-				n_[q] = rn[s0 + q];
-				d_[q] = rd[s0 + q];
-				f_[q] = rf[s0 + q];
-				if (track)
-					iv[q] = I[s0 + q];
-			}
-#pragma unroll
-		for (int q = 0; q < kSubBatch; q++)
-			if (s0 + q < a.S)
-			{
-				const T next = (dv[q] + n_[q]) / (alone ? d_[q] + T(1) : d_[q]) + f_[q];
-				D[s0 + q] = next;
+				nx[q] = (dv[q] + n_[q]) / (alone ? d_[q] + T(1) : d_[q]) + f_[q];
 				if (fused)
-					I[s0 + q] = iv[q] + fused_delta(a.Vv, dv[q], next);
+					iv[q] += fused_delta(a.Vv, dv[q], nx[q]);
 				else if (track)
-					I[s0 + q] = iv[q] + conflict_delta(a.Vv, n_[q], next, d_[q], f_[q]);
+					iv[q] += conflict_delta(a.Vv, n_[q], nx[q], d_[q], f_[q]);
 			}
+		row_store(D, s0, S, vec, nx);
+		if (track)
+			row_store(I, s0, S, vec, iv);
 	}
 }
 
-// compute_internalized after a conflict (cell_solver.cpp:229-243) for agent i of
+// compute_internalized after a conflict (cell_solver.cpp:132-143) for agent i of
 // a voxel that holds several agents (an entry of the shared list).
 template <typename T>
 __device__ __forceinline__ void agent_internalize(const CellArgs& a, uint64_t i)
 {
+	const bool vec = a.vec;
+	const uint32_t S = (uint32_t)a.S;
 	const T* __restrict__ D = static_cast<const T*>(a.field) + a.foff[i];
-	const T* __restrict__ nu = static_cast<const T*>(a.num) + i * a.S;
-	const T* __restrict__ de = static_cast<const T*>(a.den) + i * a.S;
-	const T* __restrict__ fa = static_cast<const T*>(a.fac) + i * a.S;
-	double* __restrict__ I = a.internal + i * a.S;
-	for (uint32_t s0 = 0; s0 < a.S; s0 += kSubBatch)
+	const T* __restrict__ nu = static_cast<const T*>(a.num) + i * S;
+	const T* __restrict__ de = static_cast<const T*>(a.den) + i * S;
+	const T* __restrict__ fa = static_cast<const T*>(a.fac) + i * S;
+	double* __restrict__ I = a.internal + i * S;
+	for (uint32_t s0 = 0; s0 < S; s0 += kSubBatch)
 	{
 		T dv[kSubBatch], n_[kSubBatch], d_[kSubBatch], f_[kSubBatch];
 		double iv[kSubBatch];
+		row_load(D, s0, S, vec, dv);
+		row_load(nu, s0, S, vec, n_);
+		row_load(de, s0, S, vec, d_);
+		row_load(fa, s0, S, vec, f_);
+		row_load(I, s0, S, vec, iv);
 #pragma unroll
 		for (int q = 0; q < kSubBatch; q++)
-			if (s0 + q < a.S)
-			{
-				dv[q] = D[s0 + q];
-				n_[q] = nu[s0 + q];
-				d_[q] = de[s0 + q];
-				f_[q] = fa[s0 + q];
-				iv[q] = I[s0 + q];
-			}
-#pragma unroll
-		for (int q = 0; q < kSubBatch; q++)
-			if (s0 + q < a.S)
-				I[s0 + q] = iv[q] + conflict_delta(a.Vv, n_[q], dv[q], d_[q], f_[q]);
+			if (s0 + q < S)
+				iv[q] += conflict_delta(a.Vv, n_[q], dv[q], d_[q], f_[q]);
+		row_store(I, s0, S, vec, iv);
 	}
 }
 
