@@ -953,6 +953,19 @@ int pcg_release_internalized(pcg_context* c, uint64_t agent)
 	return pcg::launch_release(c, agent);
 }
 
+// The device address of a host buffer mapped into the device's address space
+// (memory from cudaHostAlloc, or registered with cudaHostRegister), else null.
+static void* mapped_host_pointer(const void* host)
+{
+	cudaPointerAttributes at {};
+	if (cudaPointerGetAttributes(&at, host) != cudaSuccess)
+	{
+		cudaGetLastError();
+		return nullptr;
+	}
+	return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int pcg_get_field(pcg_context* c, void* host, int layout, int dtype)
 {
 	CTX_CHECK(c);
@@ -966,6 +979,14 @@ int pcg_get_field(pcg_context* c, void* host, int layout, int dtype)
 	if (rc)
 		return rc;
 	const size_t hw = dtype == PCG_DTYPE_F32 ? 4 : 8;
+	if (void* mapped = mapped_host_pointer(host))
+	{
+		// pinned and mapped: the layout kernel writes the host buffer over the host
+		// link directly, without a staging copy
+		if ((rc = pcg::launch_to_host_layout(c, mapped, layout, dtype)))
+			return rc;
+		return pcg::check_device(c);
+	}
 	if (layout == PCG_LAYOUT_INTERLEAVED && hw == c->wsize)
 	{
 		// the device rows are the host rows plus padding: one strided copy, no kernel
@@ -995,6 +1016,12 @@ int pcg_set_field(pcg_context* c, const void* host, int layout, int dtype)
 	if (rc)
 		return rc;
 	const size_t hw = dtype == PCG_DTYPE_F32 ? 4 : 8;
+	if (const void* mapped = mapped_host_pointer(host))
+	{
+		if ((rc = pcg::launch_from_host_layout(c, mapped, layout, dtype)))
+			return rc;
+		return pcg::check_device(c);
+	}
 	if (layout == PCG_LAYOUT_INTERLEAVED && hw == c->wsize)
 	{
 		PCG_CUDA_TRY(cudaMemcpy2DAsync(c->field.ptr, c->pitch * hw, host, c->row_len * hw, c->row_len * hw, c->rows,

@@ -106,12 +106,27 @@ __device__ __forceinline__ void agent_locate(const CellArgs& a, uint64_t i)
 	T* rden = static_cast<T*>(a.rden);
 	T* rfac = static_cast<T*>(a.rfac);
 	const double vol = a.vol[i];
+	// FP32 build: the agent's dt Vc / Vv and dt / Vv once, products per substrate;
+	// within a few FP64 ulps of the reference's left-to-right quotients before the
+	// rounding to FP32, and without the divisions (double precision runs at a small
+	// fraction of the single-precision rate on this GPU).  FP64 build: the
+	// reference's expressions.
+	const double fv = a.dt * vol / a.Vv, ft = a.dt / a.Vv;
 	for (uint64_t s = 0; s < a.S; s++)
 	{
 		const uint64_t k = i * a.S + s;
-		num[k] = (T)(a.sec[k] * a.sat[k] * a.dt * vol / a.Vv);
-		den[k] = (T)((a.upt[k] + a.sec[k]) * a.dt * vol / a.Vv);
-		fac[k] = (T)(a.net[k] * a.dt / a.Vv);
+		if constexpr (sizeof(T) == 4)
+		{
+			num[k] = (T)(a.sec[k] * a.sat[k] * fv);
+			den[k] = (T)((a.upt[k] + a.sec[k]) * fv);
+			fac[k] = (T)(a.net[k] * ft);
+		}
+		else
+		{
+			num[k] = (T)(a.sec[k] * a.sat[k] * a.dt * vol / a.Vv);
+			den[k] = (T)((a.upt[k] + a.sec[k]) * a.dt * vol / a.Vv);
+			fac[k] = (T)(a.net[k] * a.dt / a.Vv);
+		}
 		rnum[k] = T(0);
 		rden[k] = T(0);
 		rfac[k] = T(0);

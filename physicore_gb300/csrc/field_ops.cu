@@ -76,50 +76,53 @@ __global__ void fill_kernel(T* field, const T* init, uint64_t row_len, uint64_t 
 	}
 }
 
-// device field -> dense host-order buffer of element type OUT; planar or interleaved
-template <typename T, typename OUT, bool INTERLEAVED>
-__global__ void pack_kernel(const T* field, OUT* dst, uint64_t nx, uint64_t pitch, uint64_t rows, uint64_t S)
+// Device field <-> dense host-order buffer of element type OUT/IN.
+// Interleaved host layout [v][s]: element order equals the device row order, so
+// consecutive threads read consecutive device values.
+template <typename T, typename OUT>
+__global__ void pack_interleaved_kernel(const T* field, OUT* dst, uint64_t nx, uint64_t pitch, uint64_t rows,
+										uint64_t S)
 {
-	const uint64_t V = nx * rows;
-	const uint64_t total = V * S;
+	const uint64_t row_len = nx * S, total = row_len * rows;
 	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
 		 i += (uint64_t)gridDim.x * blockDim.x)
+		dst[i] = (OUT)field[(i / row_len) * pitch + i % row_len];
+}
+
+// Planar host layout [s][v]: a thread per voxel reads the voxel's S adjacent
+// values once and writes one value into each substrate's plane (coalesced across
+// the warp for every s).
+template <typename T, typename OUT>
+__global__ void pack_planar_kernel(const T* field, OUT* dst, uint64_t nx, uint64_t pitch, uint64_t rows, uint32_t S)
+{
+	const uint64_t V = nx * rows;
+	for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x)
 	{
-		uint64_t s, v;
-		if (INTERLEAVED)
-		{
-			s = i % S;
-			v = i / S;
-		}
-		else
-		{
-			s = i / V;
-			v = i % V;
-		}
-		dst[i] = (OUT)field[(v / nx) * pitch + (v % nx) * S + s];
+		const T* src = field + (v / nx) * pitch + (v % nx) * S;
+		for (uint32_t s = 0; s < S; s++)
+			dst[s * V + v] = (OUT)src[s];
 	}
 }
 
-template <typename T, typename IN, bool INTERLEAVED>
-__global__ void unpack_kernel(T* field, const IN* src, uint64_t nx, uint64_t pitch, uint64_t rows, uint64_t S)
+template <typename T, typename IN>
+__global__ void unpack_interleaved_kernel(T* field, const IN* src, uint64_t nx, uint64_t pitch, uint64_t rows,
+										  uint64_t S)
 {
-	const uint64_t V = nx * rows;
-	const uint64_t total = V * S;
+	const uint64_t row_len = nx * S, total = row_len * rows;
 	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
 		 i += (uint64_t)gridDim.x * blockDim.x)
+		field[(i / row_len) * pitch + i % row_len] = (T)src[i];
+}
+
+template <typename T, typename IN>
+__global__ void unpack_planar_kernel(T* field, const IN* src, uint64_t nx, uint64_t pitch, uint64_t rows, uint32_t S)
+{
+	const uint64_t V = nx * rows;
+	for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x)
 	{
-		uint64_t s, v;
-		if (INTERLEAVED)
-		{
-			s = i % S;
-			v = i / S;
-		}
-		else
-		{
-			s = i / V;
-			v = i % V;
-		}
-		field[(v / nx) * pitch + (v % nx) * S + s] = (T)src[i];
+		T* out = field + (v / nx) * pitch + (v % nx) * S;
+		for (uint32_t s = 0; s < S; s++)
+			out[s] = (T)src[s * V + v];
 	}
 }
 
@@ -233,11 +236,11 @@ static int run_pack(Context* c, void* dst, int layout)
 	cudaEvent_t ev;
 	launch_begin(c, K_LAYOUT, (double)(total * (sizeof(T) + sizeof(H))), &ev);
 	if (layout == PCG_LAYOUT_INTERLEAVED)
-		pack_kernel<T, H, true><<<grid_for(c, total, 256), 256, 0, c->stream>>>(
+		pack_interleaved_kernel<T, H><<<grid_for(c, total, 256), 256, 0, c->stream>>>(
 			static_cast<const T*>(c->field.ptr), static_cast<H*>(dst), c->n[0], c->pitch, c->rows, c->S);
 	else
-		pack_kernel<T, H, false><<<grid_for(c, total, 256), 256, 0, c->stream>>>(
-			static_cast<const T*>(c->field.ptr), static_cast<H*>(dst), c->n[0], c->pitch, c->rows, c->S);
+		pack_planar_kernel<T, H><<<grid_for(c, c->V, 256), 256, 0, c->stream>>>(
+			static_cast<const T*>(c->field.ptr), static_cast<H*>(dst), c->n[0], c->pitch, c->rows, (uint32_t)c->S);
 	launch_end(c, K_LAYOUT, ev);
 	PCG_CUDA_TRY(cudaGetLastError());
 	return PCG_OK;
@@ -250,11 +253,11 @@ static int run_unpack(Context* c, const void* src, int layout)
 	cudaEvent_t ev;
 	launch_begin(c, K_LAYOUT, (double)(total * (sizeof(T) + sizeof(H))), &ev);
 	if (layout == PCG_LAYOUT_INTERLEAVED)
-		unpack_kernel<T, H, true><<<grid_for(c, total, 256), 256, 0, c->stream>>>(
+		unpack_interleaved_kernel<T, H><<<grid_for(c, total, 256), 256, 0, c->stream>>>(
 			static_cast<T*>(c->field.ptr), static_cast<const H*>(src), c->n[0], c->pitch, c->rows, c->S);
 	else
-		unpack_kernel<T, H, false><<<grid_for(c, total, 256), 256, 0, c->stream>>>(
-			static_cast<T*>(c->field.ptr), static_cast<const H*>(src), c->n[0], c->pitch, c->rows, c->S);
+		unpack_planar_kernel<T, H><<<grid_for(c, c->V, 256), 256, 0, c->stream>>>(
+			static_cast<T*>(c->field.ptr), static_cast<const H*>(src), c->n[0], c->pitch, c->rows, (uint32_t)c->S);
 	launch_end(c, K_LAYOUT, ev);
 	PCG_CUDA_TRY(cudaGetLastError());
 	return PCG_OK;

@@ -126,6 +126,34 @@ def test_layouts_round_trip(pcg):
         assert g.get_density(s, x, y, z) == f[z, y, x, s]
 
 
+def test_layouts_pinned_host_buffers(pcg):
+    """Pinned (device-mapped) host buffers take the direct path (the layout kernel
+    reads or writes host memory); results equal the staged copies of pageable ones."""
+    torch = pytest.importorskip("torch")
+    for prec in (pcg.FP64, pcg.FP32):
+        p = W.random_small(11)
+        g = W.apply(pcg.Solver(prec), p)
+        g.solve(2)
+        for layout in (pcg.LAYOUT_INTERLEAVED, pcg.LAYOUT_PLANAR):
+            for dt in (np.float32, np.float64):
+                ref = g.get_field(layout=layout, dtype=dt)
+                pinned = torch.empty(ref.shape, dtype=torch.float32 if dt == np.float32 else torch.float64,
+                                     pin_memory=True).numpy()
+                pinned[...] = -1
+                g.get_field(layout=layout, dtype=dt, out=pinned)
+                assert np.array_equal(pinned, ref), (prec, layout, dt)
+        f = g.get_field()
+        for layout in (pcg.LAYOUT_INTERLEAVED, pcg.LAYOUT_PLANAR):
+            src = f if layout == pcg.LAYOUT_INTERLEAVED else np.ascontiguousarray(np.moveaxis(f, -1, 0))
+            pinned = torch.empty(src.shape, dtype=torch.float64, pin_memory=True).numpy()
+            pinned[...] = src * 0.5
+            g.set_field(pinned, layout=layout)
+            back = g.get_field()
+            expect = (f * 0.5).astype(np.float32).astype(np.float64) if prec == pcg.FP32 else f * 0.5
+            assert np.array_equal(back, expect), (prec, layout)
+            g.set_field(f)
+
+
 def test_mass_identity_pure_diffusion(pcg):
     """Without Dirichlet, bulk or agents each sweep scales the mass of substrate s by
     exactly 1/(1 + decay*dt/dims) (column sums of the ADI matrix)."""
