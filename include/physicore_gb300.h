@@ -157,6 +157,16 @@ int pcg_release_internalized(pcg_context* ctx, uint64_t agent);
  * (transfer_to_host, data_manager.cpp:35-59; get_substrate_density,
  * openmp_solver.cpp:42-56).  Synchronises the stream. */
 int pcg_get_field(pcg_context* ctx, void* host, int layout, int dtype);
+/* pcg_get_field without waiting: the field is converted on the device, in stream
+ * order after the work already enqueued, into one of two staging buffers, and
+ * copied to `host` on a copy stream of the context's own, so the copy overlaps the
+ * steps enqueued next.  `host` must be pinned (cudaHostAlloc / cudaHostRegister;
+ * pageable memory is read back synchronously) and left alone until
+ * pcg_wait_field(ticket) returns.  Reserves 2 x V x S x element bytes of device
+ * memory at first use. */
+int pcg_get_field_async(pcg_context* ctx, void* host, int layout, int dtype, uint64_t* ticket);
+/* Waits until the readback `ticket` (and every earlier one) is in host memory. */
+int pcg_wait_field(pcg_context* ctx, uint64_t ticket);
 /* Overwrites the field from `host` (transfer_to_device of the densities). */
 int pcg_set_field(pcg_context* ctx, const void* host, int layout, int dtype);
 /* One density, synchronising (the const get_substrate_density). */

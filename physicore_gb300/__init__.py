@@ -61,6 +61,8 @@ SIGNATURES = {
     "pcg_recompute_positional_data": [_P],
     "pcg_release_internalized": [_P, _u64],
     "pcg_get_field": [_P, _P, _i32, _i32],
+    "pcg_get_field_async": [_P, _P, _i32, _i32, _P],
+    "pcg_wait_field": [_P, _u64],
     "pcg_set_field": [_P, _P, _i32, _i32],
     "pcg_get_density": [_P, _u64, _u64, _u64, _u64, _P],
     "pcg_get_internalized": [_P, _P],
@@ -265,6 +267,23 @@ class Solver:
             out = np.empty(shape, dtype=dt)
         self._check(self._L.pcg_get_field(self._h, _ptr(out), layout, code))
         return out
+
+    def get_field_async(self, out, layout=LAYOUT_INTERLEAVED):
+        """Starts reading the field into `out` (a C-contiguous float32/float64 array
+        of the layout's shape, ideally pinned memory) and returns a ticket for
+        wait_field; `out` must stay alive and unread until then."""
+        dt = np.dtype(out.dtype)
+        code = DTYPE_F64 if dt == np.float64 else DTYPE_F32 if dt == np.float32 else None
+        nx, ny, nz = self.grid
+        shape = (nz, ny, nx, self.S) if layout == LAYOUT_INTERLEAVED else (self.S, nz, ny, nx)
+        if code is None or tuple(out.shape) != shape or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"out must be a C-contiguous float32/float64 array of shape {shape}")
+        t = ctypes.c_uint64()
+        self._check(self._L.pcg_get_field_async(self._h, _ptr(out), layout, code, ctypes.byref(t)))
+        return t.value
+
+    def wait_field(self, ticket):
+        self._check(self._L.pcg_wait_field(self._h, ticket))
 
     def set_field(self, field, layout=LAYOUT_INTERLEAVED):
         f = np.ascontiguousarray(field)

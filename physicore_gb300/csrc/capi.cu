@@ -568,6 +568,7 @@ int upload_agents(Context* c, uint64_t A, const double* positions, const double*
 		PCG_CUDA_TRY(cudaStreamSynchronize(c->stream)); // the caller may free its arrays on return
 	}
 	c->recompute_cells = true;
+	c->terms_dirty = true;
 	return PCG_OK;
 }
 
@@ -646,6 +647,8 @@ int pcg_destroy(pcg_context* c)
 	pcg::DeviceGuard g(c->device);
 	if (c->stream)
 		cudaStreamSynchronize(c->stream);
+	if (c->rb_stream)
+		cudaStreamSynchronize(c->rb_stream);
 	pcg::collect_timings(c);
 	pcg::DeviceBuffer* all[] = { &c->field,		 &c->coef[0],	&c->coef[1],	&c->coef[2],	 &c->a_vox,
 								 &c->err,		&c->flags,		 &c->mass,		&c->tickets,
@@ -654,11 +657,21 @@ int pcg_destroy(pcg_context* c)
 								 &c->a_sec,		 &c->a_sat,		&c->a_upt,		&c->a_net,		 &c->a_vol,
 								 &c->a_active,	 &c->a_internal, &c->a_frac,	&c->a_foff,		 &c->a_num,
 								 &c->a_den,		 &c->a_fac,		&c->a_rnum,		&c->a_rden,		 &c->a_rfac,
-								 &c->owner,		 &c->counts,	&c->a_role,		&c->a_shared };
+								 &c->owner,		 &c->counts,	&c->a_role,		&c->a_shared,	 &c->rb_staging[0],
+								 &c->rb_staging[1] };
 	for (auto* b : all)
 		pcg::dfree(*b);
 	for (cudaEvent_t e : c->event_pool)
 		cudaEventDestroy(e);
+	for (int j = 0; j < 2; j++)
+	{
+		if (c->rb_packed[j])
+			cudaEventDestroy(c->rb_packed[j]);
+		if (c->rb_done[j])
+			cudaEventDestroy(c->rb_done[j]);
+	}
+	if (c->rb_stream)
+		cudaStreamDestroy(c->rb_stream);
 	if (c->own_stream)
 		cudaStreamDestroy(c->own_stream);
 	delete c;
@@ -1001,6 +1014,79 @@ int pcg_get_field(pcg_context* c, void* host, int layout, int dtype)
 		return rc;
 	PCG_CUDA_TRY(cudaMemcpyAsync(host, c->staging.ptr, bytes, cudaMemcpyDeviceToHost, c->stream));
 	return pcg::check_device(c);
+}
+
+int pcg_get_field_async(pcg_context* c, void* host, int layout, int dtype, uint64_t* ticket)
+{
+	CTX_CHECK(c);
+	if (!host || !ticket)
+		return fail(PCG_ERR_INVALID, "null host buffer or ticket");
+	if ((layout != PCG_LAYOUT_INTERLEAVED && layout != PCG_LAYOUT_PLANAR) ||
+		(dtype != PCG_DTYPE_F32 && dtype != PCG_DTYPE_F64))
+		return fail(PCG_ERR_INVALID, "bad layout or dtype");
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::do_initialize(c);
+	if (rc)
+		return rc;
+	if (!mapped_host_pointer(host))
+	{
+		// pageable memory: a copy to it would block anyway
+		*ticket = c->rb_issued++;
+		return pcg_get_field(c, host, layout, dtype);
+	}
+	if (!c->rb_stream)
+	{
+		PCG_CUDA_TRY(cudaStreamCreateWithFlags(&c->rb_stream, cudaStreamNonBlocking));
+		for (int j = 0; j < 2; j++)
+		{
+			PCG_CUDA_TRY(cudaEventCreateWithFlags(&c->rb_packed[j], cudaEventDisableTiming));
+			PCG_CUDA_TRY(cudaEventCreateWithFlags(&c->rb_done[j], cudaEventDisableTiming));
+		}
+	}
+	const int j = (int)(c->rb_issued % 2);
+	const size_t bytes = c->V * c->S * (dtype == PCG_DTYPE_F32 ? 4 : 8);
+	if (c->rb_staging[j].bytes < bytes)
+	{
+		if (c->rb_pending[j])
+			PCG_CUDA_TRY(cudaEventSynchronize(c->rb_done[j])); // its last copy still reads it
+		if ((rc = pcg::dalloc(c, c->rb_staging[j], bytes)))
+			return rc;
+	}
+	// the slot's previous copy to the host must have read the buffer before it is
+	// overwritten; the main stream waits for it on the device, not the host
+	if (c->rb_pending[j])
+		PCG_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->rb_done[j], 0));
+	if ((rc = pcg::launch_to_host_layout(c, c->rb_staging[j].ptr, layout, dtype)))
+		return rc;
+	PCG_CUDA_TRY(cudaEventRecord(c->rb_packed[j], c->stream));
+	PCG_CUDA_TRY(cudaStreamWaitEvent(c->rb_stream, c->rb_packed[j], 0));
+	PCG_CUDA_TRY(cudaMemcpyAsync(host, c->rb_staging[j].ptr, bytes, cudaMemcpyDeviceToHost, c->rb_stream));
+	PCG_CUDA_TRY(cudaEventRecord(c->rb_done[j], c->rb_stream));
+	c->rb_pending[j] = true;
+	*ticket = c->rb_issued++;
+	return PCG_OK;
+}
+
+int pcg_wait_field(pcg_context* c, uint64_t ticket)
+{
+	CTX_CHECK(c);
+	if (ticket >= c->rb_issued)
+		return fail(PCG_ERR_INVALID, "no readback with this ticket was started");
+	pcg::DeviceGuard g(c->device);
+	const int j = (int)(ticket % 2);
+	// the slot's event belongs to this readback or to a later one in the same
+	// copy stream, which completes after it: either way the slot is idle after it
+	if (c->rb_pending[j])
+	{
+		cudaError_t e = cudaEventSynchronize(c->rb_done[j]);
+		if (e != cudaSuccess)
+			return fail(PCG_ERR_CUDA, std::string("readback: ") + cudaGetErrorString(e));
+		c->rb_pending[j] = false;
+	}
+	// no device error-word read here: a copy from the device would queue behind the
+	// readbacks still running and wait for them; kernel errors surface at the next
+	// call that synchronises the context's stream
+	return PCG_OK;
 }
 
 int pcg_set_field(pcg_context* c, const void* host, int layout, int dtype)

@@ -142,6 +142,7 @@ CellArgs make_cell_args(const Context* c)
 	a.field = c->field.ptr;
 	a.internalized = c->compute_internalized ? 1 : 0;
 	a.vec = rows_vectorizable(a, c->wsize);
+	a.terms = 1;
 	return a;
 }
 
@@ -160,8 +161,13 @@ static int run_cells(Context* c, bool recompute)
 	if (recompute)
 	{
 		PCG_CUDA_TRY(cudaMemsetAsync(c->counts.ptr, 0, c->V * sizeof(uint32_t), c->stream));
-		launch_begin(c, K_CELLS_LOCATE, A * (8.0 * c->dims + 1 + 5 * S * 8 + 8 + 6 * S * w + 4), &ev);
+		// positions, activity, voxel index/offset, ballot slot, cleared sums; the terms
+		// (rates, volume in; three FP32/FP64 rows out) only after new agent data
+		a.terms = c->terms_dirty ? 1 : 0;
+		launch_begin(c, K_CELLS_LOCATE,
+					 A * (8.0 * c->dims + 1 + 8 + 4 + 3 * S * w + (a.terms ? 5 * S * 8 + 8 + 3 * S * w : 0)), &ev);
 		cells_locate_kernel<T><<<grid, block, 0, c->stream>>>(a);
+		c->terms_dirty = false;
 		launch_end(c, K_CELLS_LOCATE, ev);
 		PCG_CUDA_TRY(cudaGetLastError());
 		launch_begin(c, K_CELLS_BALLOT, A * (4 + 8), &ev);
@@ -241,6 +247,7 @@ int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream)
 	a.field = b.field;
 	a.internalized = b.internalized;
 	a.vec = rows_vectorizable(a, sizeof(float));
+	a.terms = 1;
 	const uint64_t V = b.n[0] * b.n[1] * b.n[2];
 	const unsigned block = 256;
 	const unsigned grid = (unsigned)((b.A + block - 1) / block);

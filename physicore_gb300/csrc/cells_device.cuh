@@ -50,7 +50,8 @@ struct CellArgs
 	uint32_t* err;
 	void* field;
 	int internalized;
-	int vec; // rows of S values start on 16-byte boundaries and S is a multiple of 16 / sizeof(T)
+	int vec;   // rows of S values start on 16-byte boundaries and S is a multiple of 16 / sizeof(T)
+	int terms; // recompute the agent terms (their rates or volumes changed), not only positions
 };
 
 // Cell arguments of a context's own buffers (cells.cu).
@@ -80,9 +81,42 @@ __device__ __forceinline__ bool locate(const CellArgs& a, uint64_t i, uint64_t i
 }
 
 // compute_intermediates + clear_ballots (cell_solver.cpp:22-77) for agent i < A.
+// The terms depend on the agent's rates and volume only: a recompute after the
+// agents moved keeps them (a.terms == 0), with the same values the reference
+// recomputes.  With a.terms they are computed for inactive agents too, so that an
+// agent activated later finds its terms.
 template <typename T>
 __device__ __forceinline__ void agent_locate(const CellArgs& a, uint64_t i)
 {
+	T* num = static_cast<T*>(a.num);
+	T* den = static_cast<T*>(a.den);
+	T* fac = static_cast<T*>(a.fac);
+	if (a.terms)
+	{
+		const double vol = a.vol[i];
+		// FP32 build: the agent's dt Vc / Vv and dt / Vv once, products per
+		// substrate; within a few FP64 ulps of the reference's left-to-right
+		// quotients before the rounding to FP32, and without the divisions (double
+		// precision runs at a small fraction of the single-precision rate on this
+		// GPU).  FP64 build: the reference's expressions.
+		const double fv = a.dt * vol / a.Vv, ft = a.dt / a.Vv;
+		for (uint64_t s = 0; s < a.S; s++)
+		{
+			const uint64_t k = i * a.S + s;
+			if constexpr (sizeof(T) == 4)
+			{
+				num[k] = (T)(a.sec[k] * a.sat[k] * fv);
+				den[k] = (T)((a.upt[k] + a.sec[k]) * fv);
+				fac[k] = (T)(a.net[k] * ft);
+			}
+			else
+			{
+				num[k] = (T)(a.sec[k] * a.sat[k] * a.dt * vol / a.Vv);
+				den[k] = (T)((a.upt[k] + a.sec[k]) * a.dt * vol / a.Vv);
+				fac[k] = (T)(a.net[k] * a.dt / a.Vv);
+			}
+		}
+	}
 	uint64_t idx[3];
 	if (!a.active[i])
 	{
@@ -99,34 +133,12 @@ __device__ __forceinline__ void agent_locate(const CellArgs& a, uint64_t i)
 	a.vox[i] = v;
 	a.foff[i] = (uint32_t)((idx[2] * a.n[1] + idx[1]) * a.pitch + idx[0] * a.S);
 	a.owner[v] = kNoAgent;
-	T* num = static_cast<T*>(a.num);
-	T* den = static_cast<T*>(a.den);
-	T* fac = static_cast<T*>(a.fac);
 	T* rnum = static_cast<T*>(a.rnum);
 	T* rden = static_cast<T*>(a.rden);
 	T* rfac = static_cast<T*>(a.rfac);
-	const double vol = a.vol[i];
-	// FP32 build: the agent's dt Vc / Vv and dt / Vv once, products per substrate;
-	// within a few FP64 ulps of the reference's left-to-right quotients before the
-	// rounding to FP32, and without the divisions (double precision runs at a small
-	// fraction of the single-precision rate on this GPU).  FP64 build: the
-	// reference's expressions.
-	const double fv = a.dt * vol / a.Vv, ft = a.dt / a.Vv;
 	for (uint64_t s = 0; s < a.S; s++)
 	{
 		const uint64_t k = i * a.S + s;
-		if constexpr (sizeof(T) == 4)
-		{
-			num[k] = (T)(a.sec[k] * a.sat[k] * fv);
-			den[k] = (T)((a.upt[k] + a.sec[k]) * fv);
-			fac[k] = (T)(a.net[k] * ft);
-		}
-		else
-		{
-			num[k] = (T)(a.sec[k] * a.sat[k] * a.dt * vol / a.Vv);
-			den[k] = (T)((a.upt[k] + a.sec[k]) * a.dt * vol / a.Vv);
-			fac[k] = (T)(a.net[k] * a.dt / a.Vv);
-		}
 		rnum[k] = T(0);
 		rden[k] = T(0);
 		rfac[k] = T(0);

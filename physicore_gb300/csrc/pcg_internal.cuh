@@ -173,6 +173,7 @@ struct Context
 	// device state
 	bool initialized = false;
 	bool recompute_cells = true;
+	bool terms_dirty = true; // agent rates or volumes uploaded since the agent terms were computed
 	// bumped by every call that may reallocate a device buffer or change a
 	// parameter; batches compare it with the value they captured
 	uint64_t generation = 0;
@@ -189,9 +190,16 @@ struct Context
 	uint32_t coef_head[3] = { 0, 0, 0 };     // head points per substrate of the compressed tables
 	DeviceBuffer err;      // uint32 device error word
 	DeviceBuffer tickets;  // uint32 [4]: tile counters of the persistent sweeps
-	DeviceBuffer flags;    // uint32 [4]: [0] ballot conflict
+	DeviceBuffer flags;    // uint32 [4]: [0] ballot conflict, [1] agents in shared voxels
 	DeviceBuffer mass;     // double [S]
 	DeviceBuffer staging;  // layout conversion
+	// asynchronous field readback: two staging buffers used in turn, copied to the
+	// host on a stream of their own; readback k uses slot k % 2
+	DeviceBuffer rb_staging[2];
+	cudaStream_t rb_stream = nullptr;
+	cudaEvent_t rb_packed[2] = { nullptr, nullptr }, rb_done[2] = { nullptr, nullptr };
+	bool rb_pending[2] = { false, false };
+	uint64_t rb_issued = 0;
 
 	// Dirichlet
 	uint64_t K = 0;

@@ -154,6 +154,36 @@ def test_layouts_pinned_host_buffers(pcg):
             g.set_field(f)
 
 
+def test_field_readback_async(pcg):
+    """Readbacks overlapped with the following steps (two staging slots in turn)
+    deliver each step's field; a twin solver without agents (deterministic) gives
+    the expected fields.  Pageable buffers fall back to a synchronous readback."""
+    torch = pytest.importorskip("torch")
+    p = W.random_small(12)
+    p["agents"] = None
+    g = W.apply(pcg.Solver(pcg.FP32), p)
+    twin = W.apply(pcg.Solver(pcg.FP32), p)
+    nx, ny, nz = g.grid
+    shape = (g.S, nz, ny, nx)
+    bufs = [torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
+    expect, tickets = [], []
+    for k in range(6):
+        g.solve(1)
+        twin.solve(1)
+        expect.append(twin.get_field(layout=pcg.LAYOUT_PLANAR, dtype=np.float32))
+        tickets.append(g.get_field_async(bufs[k % 2], layout=pcg.LAYOUT_PLANAR))
+        if k:  # the previous step's field, read while this step's readback runs
+            g.wait_field(tickets[k - 1])
+            assert np.array_equal(bufs[(k - 1) % 2], expect[k - 1]), k - 1
+    g.wait_field(tickets[-1])
+    assert np.array_equal(bufs[5 % 2], expect[5])
+    out = np.empty(shape, np.float32)
+    g.wait_field(g.get_field_async(out, layout=pcg.LAYOUT_PLANAR))
+    assert np.array_equal(out, expect[5])
+    with pytest.raises(pcg.PcgError):
+        g.wait_field(10 ** 6)
+
+
 def test_mass_identity_pure_diffusion(pcg):
     """Without Dirichlet, bulk or agents each sweep scales the mass of substrate s by
     exactly 1/(1 + decay*dt/dims) (column sums of the ADI matrix)."""
