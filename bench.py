@@ -412,13 +412,47 @@ def run_batched(args, local, clock_sampler=None):
     return out
 
 
+class PinnedArena:
+    """First-fit extents of one pinned float32 buffer, shared by a producer that
+    takes slices and a consumer that gives them back."""
+
+    def __init__(self, torch, elems):
+        self.buf = torch.empty(elems, dtype=torch.float32, pin_memory=True).numpy()
+        self.free = [(0, elems)]  # sorted (offset, length)
+        self.cv = threading.Condition()
+
+    def take(self, n):
+        """Offset of n free elements, or None when no free extent is that long."""
+        with self.cv:
+            for k, (o, l) in enumerate(self.free):
+                if l >= n:
+                    self.free[k:k + 1] = [(o + n, l - n)] if l > n else []
+                    return o
+            return None
+
+    def give(self, off, n):
+        with self.cv:
+            self.free.append((off, n))
+            self.free.sort()
+            merged = []
+            for o, l in self.free:
+                if merged and merged[-1][0] + merged[-1][1] == o:
+                    merged[-1] = (merged[-1][0], merged[-1][1] + l)
+                else:
+                    merged.append((o, l))
+            self.free = merged
+            self.cv.notify_all()
+
+
 def run_serve(args, local):
     """The served request stream (Poisson arrivals of independent simulations of
     random sizes and step counts; workloads.ServedStream) through the simulation
-    server: a feeder thread submits each request at its arrival time, the main
-    thread collects finished ones, reads their fields back (FP32, planar, into a
-    pinned buffer) and destroys them.  Reports time-to-result percentiles (submit ->
-    finished on the device, and -> field on the host) and aggregate VSS/s."""
+    server: a feeder thread submits each request at its arrival time with a slice
+    of a pinned host arena for its field, which the server fills (FP32, planar)
+    before returning the request; the main thread collects finished ones, frees
+    their slices and destroys them.  Reports time-to-result percentiles (submit ->
+    field in host memory, on the server's clock and on the collector's) and
+    aggregate VSS/s."""
     import torch
 
     import physicore_gb300 as pcg
@@ -426,10 +460,15 @@ def run_serve(args, local):
     stream = W.ServedStream(duration=args.serve_duration)
     n = len(stream)
     srv = pcg.Server(pcg.FP32, device=local, steps_per_tick=args.serve_tick, reserve_bytes=1 << 30)
-    max_elems = int(max(np.prod(stream.sides[i]) * stream.S[i] for i in range(n)))
-    host = torch.empty(max_elems, dtype=torch.float32, pin_memory=True).numpy()
+    elems = [int(np.prod(stream.sides[i]) * stream.S[i]) for i in range(n)]
+    # pinned slices for the fields of requests in flight; beyond 16 GB of them (a
+    # backlog under overload) a request gets a pageable buffer instead
+    arena = PinnedArena(torch, min(sum(elems), 4 << 30))
+    host = arena.buf
     submit_wall = np.zeros(n)
     lag = np.zeros(n)
+    slices = {}
+    pageable = [0]
     err = []
 
     def feed():
@@ -439,10 +478,16 @@ def run_serve(args, local):
                 delay = stream.arrivals[i] - (time.perf_counter() - t0)
                 if delay > 0:
                     time.sleep(delay)
-                lag[i] = max(0.0, -delay)
                 s = stream.request(pcg.Solver(pcg.FP32, device=local), i)
+                lag[i] = max(0.0, time.perf_counter() - t0 - stream.arrivals[i])
+                nx, ny, nz = (int(v) for v in stream.sides[i])
+                off = arena.take(elems[i])
+                slices[i] = off
+                pageable[0] += off is None
+                out = (host[off: off + elems[i]] if off is not None else np.empty(elems[i], np.float32))
                 submit_wall[i] = time.perf_counter()
-                srv.submit(s, int(stream.steps[i]), i)
+                srv.submit(s, int(stream.steps[i]), i, out=out.reshape(int(stream.S[i]), nz, ny, nx),
+                           layout=pcg.LAYOUT_PLANAR)
         except Exception as e:  # surfaced by the main thread
             err.append(e)
 
@@ -457,11 +502,11 @@ def run_serve(args, local):
             got += 1
             statuses[r["status"]] = statuses.get(r["status"], 0) + 1
             s = r["solver"]
+            i = r["tag"]
+            off = slices.pop(i)
+            if off is not None:
+                arena.give(off, elems[i])
             if r["status"] == "done":
-                i = r["tag"]
-                nx, ny, nz = (int(v) for v in stream.sides[i])
-                S = int(stream.S[i])
-                s.get_field(layout=pcg.LAYOUT_PLANAR, dtype=np.float32, out=host[: S * nx * ny * nz].reshape(S, nz, ny, nx))
                 lat_host.append(time.perf_counter() - submit_wall[i])
                 lat_dev.append(r["t_done"] - r["t_submit"])
                 vss_done += stream.vss(i)
@@ -507,11 +552,15 @@ def run_serve(args, local):
                               "pcg_get_field, pcg_destroy"},
             "speedup_vs_plain": (vss_done / (t_last - t_first)) / (vss_plain / plain_s) if t_last else None,
             "time_to_result_s": {"p50": q(lat_dev, 50), "p99": q(lat_dev, 99), "mean": float(np.mean(lat_dev))
-                                 if lat_dev else None, "measured": "submit -> last step finished on the device"},
+                                 if lat_dev else None,
+                                 "measured": "submit -> field (FP32, planar) in pinned host memory, server clock"},
             "time_to_host_s": {"p50": q(lat_host, 50), "p99": q(lat_host, 99),
-                               "measured": "submit -> field (FP32, planar) in pinned host memory"},
+                               "measured": "submit -> result collected by the caller (includes its polling)"},
             "feeder_lag_s": {"p50": q(lag, 50), "max": float(lag.max()) if n else None},
-            "server": {k: st[k] for k in ("ticks", "rebuilds", "steps", "admitted", "refused", "failed")},
+            "result_buffers": {"pinned": int(n - pageable[0]), "pageable": int(pageable[0])},
+            "server": {k: (round(st[k], 3) if isinstance(st[k], float) else st[k])
+                       for k in ("ticks", "rebuilds", "steps", "admitted", "refused", "failed", "rebuild_s", "step_s",
+                                 "admit_s")},
             "steps_per_tick": args.serve_tick, "wall_s": round(wall, 2)}
 
 

@@ -304,12 +304,23 @@ typedef struct pcg_server_stats
 	uint64_t active_bytes;   /* device bytes of the admitted set */
 	uint64_t queued, active, in_flight;
 	double uptime_s;
+	/* worker time regrouping the active set into a batch, starting and waiting
+	 * for steps, and admitting requests */
+	double rebuild_s, step_s, admit_s;
 } pcg_server_stats;
 
 int pcg_server_create(pcg_server** out, int precision, int device, const pcg_server_options* options);
 /* Stops the worker; contexts the server still holds are destroyed. */
 int pcg_server_destroy(pcg_server* server);
 int pcg_server_submit(pcg_server* server, pcg_context* request, uint64_t steps, uint64_t tag);
+/* pcg_server_submit, and when the request is done the server copies its field
+ * into `host` (layouts and types as pcg_get_field; pinned memory recommended)
+ * right after the steps in which it finished, before reporting it: the copies of
+ * finished requests then run while the device has no other work of the server,
+ * and the caller's thread issues no device work of its own.  `host` must stay
+ * valid until the request is returned by pcg_server_poll. */
+int pcg_server_submit_readback(pcg_server* server, pcg_context* request, uint64_t steps, uint64_t tag, void* host,
+							   int layout, int dtype);
 /* Cancels a queued or running request (it comes back with PCG_REQUEST_CANCELLED). */
 int pcg_server_cancel(pcg_server* server, uint64_t tag);
 /* Up to `cap` finished requests; waits up to wait_ms for the first. */

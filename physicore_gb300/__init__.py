@@ -92,6 +92,7 @@ SIGNATURES = {
     "pcg_server_create": [_P, _i32, _i32, _P],
     "pcg_server_destroy": [_P],
     "pcg_server_submit": [_P, _P, _u64, _u64],
+    "pcg_server_submit_readback": [_P, _P, _u64, _u64, _P, _i32, _i32],
     "pcg_server_cancel": [_P, _u64],
     "pcg_server_poll": [_P, _P, _u64, _P, _i32],
     "pcg_server_get_stats": [_P, _P],
@@ -453,7 +454,8 @@ class ServerResult(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "admitted", "completed", "cancelled", "refused",
                                                "failed", "ticks", "rebuilds", "steps", "vss", "active_bytes",
-                                               "queued", "active", "in_flight")] + [("uptime_s", ctypes.c_double)]
+                                               "queued", "active", "in_flight")] + [
+        (n, ctypes.c_double) for n in ("uptime_s", "rebuild_s", "step_s", "admit_s")]
 
 
 REQUEST_DONE, REQUEST_CANCELLED, REQUEST_REFUSED, REQUEST_FAILED = 0, 1, 2, 3
@@ -477,15 +479,30 @@ class Server:
         self._check(self._L.pcg_server_create(ctypes.byref(h), precision, device, ctypes.byref(opts)))
         self._h = h
         self._held = {}  # tag -> Solver owned by the server
+        self._outs = {}  # tag -> host buffer the server writes the field into
 
     def _check(self, rc):
         if rc != 0:
             raise PcgError(rc, self._L.pcg_last_error().decode())
 
-    def submit(self, solver: "Solver", steps: int, tag: int):
+    def submit(self, solver: "Solver", steps: int, tag: int, out=None, layout: int = LAYOUT_INTERLEAVED):
+        """Hands `solver` over for `steps` steps.  With `out` (a C-contiguous
+        float32/float64 array of the layout's shape, ideally pinned) the server
+        copies the final field into it before returning the request."""
         if tag in self._held:
             raise ValueError(f"tag {tag} is already in flight")
-        self._check(self._L.pcg_server_submit(self._h, solver.handle, steps, tag))
+        if out is None:
+            self._check(self._L.pcg_server_submit(self._h, solver.handle, steps, tag))
+        else:
+            nx, ny, nz = solver.grid
+            shape = (nz, ny, nx, solver.S) if layout == LAYOUT_INTERLEAVED else (solver.S, nz, ny, nx)
+            dt = np.dtype(out.dtype)
+            if dt not in (np.float32, np.float64) or tuple(out.shape) != shape or not out.flags["C_CONTIGUOUS"]:
+                raise ValueError(f"out must be a C-contiguous float32/float64 array of shape {shape}")
+            code = DTYPE_F32 if dt == np.float32 else DTYPE_F64
+            self._check(self._L.pcg_server_submit_readback(self._h, solver.handle, steps, tag, _ptr(out), layout,
+                                                           code))
+            self._outs[tag] = out  # kept alive until the request comes back
         self._held[tag] = solver
 
     def cancel(self, tag: int):
@@ -498,6 +515,7 @@ class Server:
         out = []
         for i in range(n.value):
             r = arr[i]
+            self._outs.pop(r.tag, None)
             out.append({"solver": self._held.pop(r.tag), "tag": r.tag, "steps": r.steps,
                         "status": REQUEST_STATUS.get(r.status, r.status), "code": r.code,
                         "t_submit": r.t_submit, "t_admit": r.t_admit, "t_done": r.t_done,

@@ -720,6 +720,8 @@ using pcg::DeviceBuffer;
 struct pcg_batch
 {
 	int device = 0;
+	uint32_t* h_words = nullptr; // pinned host words for reading the error words
+	cudaEvent_t ev_block = nullptr; // blocking-sync event for host waits on the stream
 	size_t wsize = 4;
 	int sm_count = 0;
 	std::vector<pcg_context*> ctx;
@@ -773,14 +775,14 @@ void free_buf(DeviceBuffer& b) { dfree(b); }
 
 // Batch buffers come from the stream-ordered allocator on the batch's stream (all
 // their users run on it), so regrouping batches never synchronises the device.
-int balloc(DeviceBuffer& b, size_t bytes, cudaStream_t stream)
+int balloc(DeviceBuffer& b, size_t bytes, cudaStream_t stream, int device)
 {
 	if (b.ptr && b.bytes >= bytes)
 		return PCG_OK;
 	dfree(b);
 	if (!bytes)
 		return PCG_OK;
-	cudaError_t e = cudaMallocAsync(&b.ptr, bytes, stream);
+	cudaError_t e = pool_alloc(&b.ptr, bytes, stream, device);
 	if (e != cudaSuccess)
 	{
 		b.ptr = nullptr;
@@ -793,6 +795,22 @@ int balloc(DeviceBuffer& b, size_t bytes, cudaStream_t stream)
 }
 
 Context* C(pcg_batch* b, size_t d) { return static_cast<Context*>(b->ctx[d]); }
+
+// Host wait for the batch stream, asleep (see stream_wait in capi.cu).
+cudaError_t batch_wait(pcg_batch* b)
+{
+	if (!b->ev_block)
+	{
+		cudaError_t e = cudaEventCreateWithFlags(&b->ev_block, cudaEventBlockingSync | cudaEventDisableTiming);
+		if (e != cudaSuccess)
+		{
+			b->ev_block = nullptr;
+			return e;
+		}
+	}
+	cudaError_t e = cudaEventRecord(b->ev_block, b->stream);
+	return e != cudaSuccess ? e : cudaEventSynchronize(b->ev_block);
+}
 
 // ---- descriptors
 
@@ -907,12 +925,13 @@ HostList build_list(pcg_batch* b, int id, const std::vector<size_t>& subset)
 }
 
 // Uploads host lists into one device buffer and fills the device-side views.
-int upload_lists(DeviceBuffer& buf, const std::vector<HostList>& hl, WorkList* out, cudaStream_t stream)
+int upload_lists(DeviceBuffer& buf, const std::vector<HostList>& hl, WorkList* out, cudaStream_t stream,
+				 int device)
 {
 	size_t bytes = 0;
 	for (const auto& h : hl)
 		bytes += round_up(h.base.size() * 8, 256) + round_up(std::max<size_t>(h.dom.size(), 1) * 4, 256);
-	int rc = balloc(buf, bytes, stream);
+	int rc = balloc(buf, bytes, stream, device);
 	if (rc)
 		return rc;
 	std::vector<unsigned char> host(bytes, 0);
@@ -954,14 +973,14 @@ int upload_domains(pcg_batch* b)
 	for (size_t d = 0; d < N; d++)
 		b->h_doms[d] = describe_domain(b, d);
 	int rc;
-	if ((rc = balloc(b->d_doms, N * sizeof(BatchDomain), b->stream)) ||
-		(rc = balloc(b->d_tmaps, N * 2 * sizeof(CUtensorMap), b->stream)))
+	if ((rc = balloc(b->d_doms, N * sizeof(BatchDomain), b->stream, b->device)) ||
+		(rc = balloc(b->d_tmaps, N * 2 * sizeof(CUtensorMap), b->stream, b->device)))
 		return rc;
 	PCG_CUDA_TRY(cudaMemcpyAsync(b->d_doms.ptr, b->h_doms.data(), N * sizeof(BatchDomain), cudaMemcpyHostToDevice,
 								 b->stream));
 	PCG_CUDA_TRY(cudaMemcpyAsync(b->d_tmaps.ptr, b->h_tmaps.data(), N * 2 * sizeof(CUtensorMap),
 								 cudaMemcpyHostToDevice, b->stream));
-	PCG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+	PCG_CUDA_TRY(pcg::batch_wait(b));
 	return PCG_OK;
 }
 
@@ -1054,7 +1073,7 @@ int build_t(pcg_batch* b)
 	std::vector<HostList> hl;
 	for (int id = 0; id < L_COUNT; id++)
 		hl.push_back(build_list(b, id, all));
-	if ((rc = upload_lists(b->d_lists, hl, b->lists, b->stream)))
+	if ((rc = upload_lists(b->d_lists, hl, b->lists, b->stream, b->device)))
 		return rc;
 	for (int axis = 0; axis < 3; axis++)
 	{
@@ -1395,7 +1414,7 @@ int upload_recompute(pcg_batch* b)
 	if (b->dev_recompute_valid && b->dev_recompute == b->h_recompute)
 		return PCG_OK;
 	PCG_CUDA_TRY(cudaMemcpyAsync(b->d_recompute.ptr, b->h_recompute.data(), N, cudaMemcpyHostToDevice, b->stream));
-	PCG_CUDA_TRY(cudaStreamSynchronize(b->stream)); // the host buffer is reused by the next call
+	PCG_CUDA_TRY(pcg::batch_wait(b)); // the host buffer is reused by the next call
 	b->dev_recompute = b->h_recompute;
 	b->dev_recompute_valid = true;
 	return PCG_OK;
@@ -1403,16 +1422,20 @@ int upload_recompute(pcg_batch* b)
 
 int check_batch(pcg_batch* b)
 {
-	cudaError_t e = cudaStreamSynchronize(b->stream);
+	cudaError_t e = pcg::batch_wait(b);
 	if (e != cudaSuccess)
 		return fail(PCG_ERR_CUDA, std::string("batch stream synchronise: ") + cudaGetErrorString(e));
 	collect(b);
-	uint32_t word[2] = { 0, 0 };
-	PCG_CUDA_TRY(cudaMemcpy(word, b->d_err.ptr, sizeof(word), cudaMemcpyDeviceToHost));
+	if (!b->h_words && !(b->h_words = pinned_words_get()))
+		return fail(PCG_ERR_NOMEM, "pinned host memory for the batch error words");
+	PCG_CUDA_TRY(cudaMemcpyAsync(b->h_words, b->d_err.ptr, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, b->stream));
+	PCG_CUDA_TRY(pcg::batch_wait(b));
+	const uint32_t word[2] = { b->h_words[0], b->h_words[1] };
 	if (word[0])
 	{
-		const uint32_t reset[2] = { 0, 0xffffffffu };
-		PCG_CUDA_TRY(cudaMemcpy(b->d_err.ptr, reset, sizeof(reset), cudaMemcpyHostToDevice));
+		uint32_t* d = static_cast<uint32_t*>(b->d_err.ptr);
+		PCG_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(uint32_t), b->stream));
+		PCG_CUDA_TRY(cudaMemsetAsync(d + 1, 0xff, sizeof(uint32_t), b->stream));
 		std::string msg = device_error_text(word[0]);
 		if (word[1] != 0xffffffffu)
 			msg += " (batch domain " + std::to_string(word[1]) + ")";
@@ -1430,7 +1453,7 @@ int time_axis(pcg_batch* b, int axis, const std::vector<size_t>& subset, double*
 	std::vector<HostList> hl { build_list(b, axis, subset) };
 	DeviceBuffer lbuf;
 	WorkList wl {};
-	if ((rc = upload_lists(lbuf, hl, &wl, b->stream)))
+	if ((rc = upload_lists(lbuf, hl, &wl, b->stream, b->device)))
 		return rc;
 	const uint64_t smem = sweep_smem<T>(b, axis, subset);
 	unsigned grid = 0;
@@ -1527,7 +1550,7 @@ int autotune_t(pcg_batch* b)
 	for (size_t d = 0; d < N; d++)
 		off[d + 1] = off[d] + round_up(C(b, d)->rows * C(b, d)->pitch * b->wsize, 256);
 	DeviceBuffer save;
-	if ((rc = balloc(save, off[N], b->stream)))
+	if ((rc = balloc(save, off[N], b->stream, b->device)))
 		return fail(PCG_ERR_NOMEM, "autotune needs a copy of the batch's fields and could not allocate it");
 	for (size_t d = 0; d < N; d++)
 		cudaMemcpyAsync(static_cast<char*>(save.ptr) + off[d], C(b, d)->field.ptr,
@@ -1620,7 +1643,7 @@ int autotune_t(pcg_batch* b)
 	for (size_t d = 0; d < N; d++)
 		cudaMemcpyAsync(C(b, d)->field.ptr, static_cast<char*>(save.ptr) + off[d],
 						C(b, d)->rows * C(b, d)->pitch * b->wsize, cudaMemcpyDeviceToDevice, b->stream);
-	cudaError_t e = cudaStreamSynchronize(b->stream);
+	cudaError_t e = pcg::batch_wait(b);
 	dfree(save);
 	std::copy(stats_before, stats_before + K_COUNT, b->stats);
 	b->launches = launches_before;
@@ -1724,15 +1747,15 @@ int pcg_batch_create(pcg_batch** out, pcg_context* const* contexts, uint64_t cou
 		c.assign(count, pcg::AxisConfig {});
 	b->h_recompute.assign(count, 0);
 	int rc;
-	if ((rc = pcg::balloc(b->d_counters, 16 * sizeof(uint32_t), b->stream)) ||
-		(rc = pcg::balloc(b->d_err, 2 * sizeof(uint32_t), b->stream)) ||
-		(rc = pcg::balloc(b->d_recompute, count, b->stream)) ||
-		(rc = pcg::balloc(b->d_steps_left, count * sizeof(uint32_t), b->stream)))
+	if ((rc = pcg::balloc(b->d_counters, 16 * sizeof(uint32_t), b->stream, b->device)) ||
+		(rc = pcg::balloc(b->d_err, 2 * sizeof(uint32_t), b->stream, b->device)) ||
+		(rc = pcg::balloc(b->d_recompute, count, b->stream, b->device)) ||
+		(rc = pcg::balloc(b->d_steps_left, count * sizeof(uint32_t), b->stream, b->device)))
 		return bail(rc);
 	b->h_steps_left.assign(count, 0);
 	const uint32_t reset[2] = { 0, 0xffffffffu };
 	if (cudaMemcpyAsync(b->d_err.ptr, reset, sizeof(reset), cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
-		cudaStreamSynchronize(b->stream) != cudaSuccess)
+		pcg::batch_wait(b) != cudaSuccess)
 		return bail(fail(PCG_ERR_CUDA, "could not clear the batch error word"));
 	if ((rc = pcg::refresh(b)))
 		return bail(rc);
@@ -1746,7 +1769,7 @@ int pcg_batch_destroy(pcg_batch* b)
 		return PCG_OK;
 	pcg::DeviceGuard g(b->device);
 	if (b->stream)
-		cudaStreamSynchronize(b->stream);
+		pcg::batch_wait(b);
 	pcg::drop_graph(b);
 	pcg::collect(b);
 	for (cudaEvent_t e : b->event_pool)
@@ -1759,6 +1782,9 @@ int pcg_batch_destroy(pcg_batch* b)
 		cudaEventDestroy(b->ev_sync);
 	if (b->stream)
 		cudaStreamDestroy(b->stream);
+	pcg::pinned_words_put(b->h_words);
+	if (b->ev_block)
+		cudaEventDestroy(b->ev_block);
 	delete b;
 	return PCG_OK;
 }
@@ -1886,7 +1912,7 @@ int pcg_batch_get_kernel_stats(pcg_batch* b, pcg_kernel_stat* stats, uint64_t ca
 {
 	BATCH_CHECK(b);
 	pcg::DeviceGuard g(b->device);
-	cudaStreamSynchronize(b->stream);
+	pcg::batch_wait(b);
 	pcg::collect(b);
 	if (count)
 		*count = pcg::K_COUNT;
@@ -1905,7 +1931,7 @@ int pcg_batch_reset_kernel_stats(pcg_batch* b)
 {
 	BATCH_CHECK(b);
 	pcg::DeviceGuard g(b->device);
-	cudaStreamSynchronize(b->stream);
+	pcg::batch_wait(b);
 	pcg::collect(b);
 	for (auto& s : b->stats)
 		s = pcg::KernelStat {};

@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 
 #include "pcg_internal.cuh"
@@ -35,23 +36,150 @@ const char* kernel_name(int id)
 	return (id >= 0 && id < K_COUNT) ? names[id] : "?";
 }
 
-// Context buffers come from the stream-ordered allocator on the context's own
-// stream, which lives as long as the context; freeing them (a replaced buffer, or
-// pcg_destroy) then never synchronises the device, so a process that creates and
-// destroys many contexts while others run (a server) does not stall them.
+// The library's stream-ordered memory pool on a device.  A block freed on one
+// stream is handed to an allocation on another only once that free has completed
+// on the device (no cross-stream dependency is inserted), so an allocation never
+// waits for other contexts' queued work; a server admitting requests while its
+// batched steps run is not held up by them.  Up to kPoolKeepBytes of freed blocks
+// stay in the pool for reuse (beyond that they go back to the device at the next
+// synchronisation); the pool's idle bytes count as free to a server's admission.
+constexpr uint64_t kPoolKeepBytes = 4ull << 30;
+static std::mutex g_pool_mu;
+static std::map<int, cudaMemPool_t> g_pools;
+
+static cudaMemPool_t library_pool(int device)
+{
+	std::lock_guard<std::mutex> lk(g_pool_mu);
+	auto it = g_pools.find(device);
+	if (it != g_pools.end())
+		return it->second;
+	cudaMemPoolProps props {};
+	props.allocType = cudaMemAllocationTypePinned;
+	props.handleTypes = cudaMemHandleTypeNone;
+	props.location.type = cudaMemLocationTypeDevice;
+	props.location.id = device;
+	cudaMemPool_t pool = nullptr;
+	if (cudaMemPoolCreate(&pool, &props) != cudaSuccess)
+	{
+		cudaGetLastError();
+		return nullptr;
+	}
+	int off = 0, on = 1;
+	uint64_t keep = kPoolKeepBytes;
+	cudaMemPoolSetAttribute(pool, cudaMemPoolReuseFollowEventDependencies, &off);
+	cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &off);
+	cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowOpportunistic, &on);
+	cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+	cudaGetLastError();
+	g_pools[device] = pool;
+	return pool;
+}
+
+cudaError_t pool_alloc(void** ptr, size_t bytes, cudaStream_t stream, int device)
+{
+	cudaMemPool_t pool = library_pool(device);
+	return pool ? cudaMallocFromPoolAsync(ptr, bytes, pool, stream) : cudaMallocAsync(ptr, bytes, stream);
+}
+
+uint64_t pool_idle_bytes(int device)
+{
+	cudaMemPool_t pool;
+	{
+		std::lock_guard<std::mutex> lk(g_pool_mu);
+		auto it = g_pools.find(device);
+		if (it == g_pools.end())
+			return 0;
+		pool = it->second;
+	}
+	uint64_t reserved = 0, used = 0;
+	if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) != cudaSuccess ||
+		cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) != cudaSuccess)
+	{
+		cudaGetLastError();
+		return 0;
+	}
+	return reserved > used ? reserved - used : 0;
+}
+
+static std::mutex g_words_mu;
+static std::vector<uint32_t*> g_free_words;
+
+uint32_t* pinned_words_get()
+{
+	std::lock_guard<std::mutex> lk(g_words_mu);
+	if (g_free_words.empty())
+	{
+		constexpr size_t kUnits = 1024; // 16 KB of pinned memory, four words a unit, never freed
+		uint32_t* blk = nullptr;
+		if (cudaHostAlloc(reinterpret_cast<void**>(&blk), kUnits * 4 * sizeof(uint32_t), cudaHostAllocDefault) !=
+			cudaSuccess)
+		{
+			cudaGetLastError();
+			return nullptr;
+		}
+		for (size_t u = 0; u < kUnits; u++)
+			g_free_words.push_back(blk + 4 * u);
+	}
+	uint32_t* w = g_free_words.back();
+	g_free_words.pop_back();
+	return w;
+}
+
+void pinned_words_put(uint32_t* w)
+{
+	if (!w)
+		return;
+	std::lock_guard<std::mutex> lk(g_words_mu);
+	g_free_words.push_back(w);
+}
+
+// Waits for the context's stream with the calling thread asleep (a blocking-sync
+// event) rather than spinning: a thread spinning in a stream synchronisation slows
+// the CUDA calls of other threads in the process -- a server's admissions and
+// steps -- while it waits, which can be milliseconds when the stream's kernels
+// queue behind other work on the SMs.
+cudaError_t stream_wait(Context* c)
+{
+	if (!c->ev_block)
+	{
+		cudaError_t e = cudaEventCreateWithFlags(&c->ev_block, cudaEventBlockingSync | cudaEventDisableTiming);
+		if (e != cudaSuccess)
+		{
+			c->ev_block = nullptr;
+			return e;
+		}
+	}
+	cudaError_t e = cudaEventRecord(c->ev_block, c->stream);
+	return e != cudaSuccess ? e : cudaEventSynchronize(c->ev_block);
+}
+
+// Context buffers come from the library's pool on the context's own stream, which
+// lives as long as the context; freeing them (a replaced buffer, or pcg_destroy)
+// then never synchronises the device, so a process that creates and destroys many
+// contexts while others run (a server) does not stall them.
 int dalloc(Context* c, DeviceBuffer& b, size_t bytes)
 {
 	if (b.ptr && b.bytes >= bytes)
 		return PCG_OK;
 	if (b.ptr)
 	{
-		cudaStreamSynchronize(c->stream); // earlier work may still read the old buffer
+		stream_wait(c); // earlier work may still read the old buffer
 		dfree(b);
 	}
 	if (bytes == 0)
 		return PCG_OK;
 	cudaStream_t s = c->own_stream;
-	cudaError_t e = s ? cudaMallocAsync(&b.ptr, bytes, s) : cudaMalloc(&b.ptr, bytes);
+	const size_t span = round_up(bytes, 256);
+	if (c->slab.ptr && span <= c->slab.bytes - c->slab_used)
+	{
+		b.ptr = static_cast<char*>(c->slab.ptr) + c->slab_used;
+		b.bytes = bytes;
+		b.stream = c->slab.stream;
+		b.carved = true;
+		c->slab_used += span;
+		return PCG_OK; // ordered like the slab's own allocation
+	}
+	cudaError_t e = s ? pool_alloc(&b.ptr, bytes, s, c->device) : cudaMalloc(&b.ptr, bytes);
 	if (e != cudaSuccess)
 	{
 		b.ptr = nullptr;
@@ -61,14 +189,17 @@ int dalloc(Context* c, DeviceBuffer& b, size_t bytes)
 	}
 	b.bytes = bytes;
 	b.stream = s;
-	if (s)
-		cudaStreamSynchronize(s); // usable from any stream and by synchronous copies from here on
+	// Work on the context's stream is ordered after the allocation when that stream
+	// is the own stream (the usual case, and always under a server; batches wait for
+	// it through events).  A caller-set stream is not: wait for the allocation.
+	if (s && s != c->stream)
+		cudaStreamSynchronize(s);
 	return PCG_OK;
 }
 
 void dfree(DeviceBuffer& b)
 {
-	if (b.ptr)
+	if (b.ptr && !b.carved)
 	{
 		if (b.stream)
 			cudaFreeAsync(b.ptr, b.stream);
@@ -78,6 +209,7 @@ void dfree(DeviceBuffer& b)
 	b.ptr = nullptr;
 	b.bytes = 0;
 	b.stream = nullptr;
+	b.carved = false;
 }
 
 static cudaEvent_t get_event(Context* c)
@@ -150,15 +282,21 @@ static int check_device(Context* c)
 {
 	if (!c->err.ptr)
 		return PCG_OK; // nothing has run on the device yet
-	cudaError_t e = cudaStreamSynchronize(c->stream);
+	if (!c->h_words && !(c->h_words = pinned_words_get()))
+		return fail(PCG_ERR_NOMEM, "pinned host memory for the device error word");
+	// The copy is queued only once the stream is idle: a copy waiting in a copy
+	// engine's queue for kernels (which may wait for other work to leave the SMs)
+	// holds up the copies other threads queue behind it.
+	cudaError_t e = stream_wait(c);
 	if (e != cudaSuccess)
 		return fail(PCG_ERR_CUDA, std::string("stream synchronise: ") + cudaGetErrorString(e));
+	PCG_CUDA_TRY(cudaMemcpyAsync(c->h_words, c->err.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+	PCG_CUDA_TRY(stream_wait(c));
 	collect_timings(c);
-	uint32_t word = 0;
-	PCG_CUDA_TRY(cudaMemcpy(&word, c->err.ptr, sizeof(word), cudaMemcpyDeviceToHost));
+	const uint32_t word = c->h_words[0];
 	if (word)
 	{
-		PCG_CUDA_TRY(cudaMemset(c->err.ptr, 0, sizeof(uint32_t)));
+		PCG_CUDA_TRY(cudaMemsetAsync(c->err.ptr, 0, sizeof(uint32_t), c->stream));
 		return fail(PCG_ERR_DEVICE, device_error_text(word));
 	}
 	return PCG_OK;
@@ -282,7 +420,7 @@ static int upload_coefficients(Context* c)
 			return rc;
 		PCG_CUDA_TRY(cudaMemcpyAsync(c->coef[axis].ptr, tab.data(), tab.size() * sizeof(T), cudaMemcpyHostToDevice,
 									 c->stream));
-		PCG_CUDA_TRY(cudaStreamSynchronize(c->stream)); // the host table dies at scope exit
+		PCG_CUDA_TRY(stream_wait(c)); // the host table dies at scope exit
 	}
 	return PCG_OK;
 }
@@ -340,7 +478,7 @@ static int upload_dirichlet(Context* c)
 									 c->stream));
 		PCG_CUDA_TRY(cudaMemcpyAsync(c->dir_conds.ptr, ic.data(), ic.size(), cudaMemcpyHostToDevice, c->stream));
 	}
-	PCG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+	PCG_CUDA_TRY(stream_wait(c));
 	return PCG_OK;
 }
 
@@ -370,7 +508,8 @@ static int upload_bulk(Context* c)
 		int rc = dalloc(c, c->bulk[k], cnt * sizeof(T));
 		if (rc)
 			return rc;
-		PCG_CUDA_TRY(cudaMemcpy(c->bulk[k].ptr, tab.data(), cnt * sizeof(T), cudaMemcpyHostToDevice));
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->bulk[k].ptr, tab.data(), cnt * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+		PCG_CUDA_TRY(stream_wait(c)); // the host table dies at scope exit
 	}
 	return PCG_OK;
 }
@@ -416,8 +555,10 @@ int upload_agents(Context* c, uint64_t A, const double* positions, const double*
 				  const double* uptake, const double* net_export, const double* volumes, const uint8_t* is_active,
 				  const double* internalized, const double* fraction_released, bool compute_internalized);
 
-// The context's own stream and device words, created on first use.
-int ensure_device_state(Context* c)
+// The context's own stream and device words, created on first use.  With
+// defer_clear the words are allocated but not yet cleared (no device work is
+// queued): initialisation clears them after its host-blocking uploads.
+int ensure_device_state(Context* c, bool defer_clear = false)
 {
 	if (!c->own_stream)
 	{
@@ -439,19 +580,42 @@ int ensure_device_state(Context* c)
 			rc = dalloc(c, c->tickets, sizeof(uint32_t) * 4);
 		if (rc)
 			return rc;
+		c->words_cleared = false;
+	}
+	if (!c->words_cleared && !defer_clear)
+	{
 		PCG_CUDA_TRY(cudaMemsetAsync(c->err.ptr, 0, sizeof(uint32_t) * 4, c->stream));
 		PCG_CUDA_TRY(cudaMemsetAsync(c->flags.ptr, 0, sizeof(uint32_t) * 4, c->stream));
+		c->words_cleared = true;
 	}
 	return PCG_OK;
 }
 
-static int do_initialize(Context* c)
+// The initial values as T in the mass buffer (S doubles hold S T's), for the fill.
+template <typename T>
+static int upload_initial_values(Context* c)
+{
+	std::vector<T> h(c->S);
+	for (uint64_t s = 0; s < c->S; s++)
+		h[s] = (T)c->init[s];
+	PCG_CUDA_TRY(cudaMemcpyAsync(c->mass.ptr, h.data(), c->S * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+	PCG_CUDA_TRY(stream_wait(c)); // the host vector dies at scope exit
+	return PCG_OK;
+}
+
+// Allocations and uploads first: the host waits for each upload while the
+// context's stream holds nothing else, so no wait depends on other work on the
+// device.  The kernels (word clearing, field fill, ballot counts) come last.  With
+// wait = false the call returns without waiting for them (a server admitting a
+// request while its batched steps occupy the device); the next batch step orders
+// them first, and a device error surfaces there.
+static int do_initialize(Context* c, bool wait = true)
 {
 	if (c->initialized)
 		return PCG_OK;
 	{
 		DeviceGuard g(c->device);
-		const int rc0 = ensure_device_state(c);
+		const int rc0 = ensure_device_state(c, true);
 		if (rc0)
 			return rc0;
 	}
@@ -460,13 +624,21 @@ static int do_initialize(Context* c)
 	int rc;
 	if ((rc = derive_layout(c)))
 		return rc;
+	if (!c->slab.ptr)
+	{
+		const size_t bytes = estimate_device_bytes(c) + (64 << 10); // + alignment of the pieces
+		if ((rc = dalloc(c, c->slab, bytes)))
+			return rc;
+		c->slab_used = 0;
+	}
 	if ((rc = dalloc(c, c->field, c->rows * c->pitch * c->wsize)))
 		return rc;
 	if ((rc = prepare_sweep_maps(c)))
 		return rc;
 	if ((rc = dalloc(c, c->mass, std::max<uint64_t>(c->S, 2) * sizeof(double))))
 		return rc;
-	if ((rc = launch_fill_initial(c)))
+	rc = c->wsize == 4 ? upload_initial_values<float>(c) : upload_initial_values<double>(c);
+	if (rc)
 		return rc;
 	rc = c->wsize == 4 ? upload_coefficients<float>(c) : upload_coefficients<double>(c);
 	if (rc)
@@ -486,17 +658,20 @@ static int do_initialize(Context* c)
 	{
 		const Context::HostAgents& h = *c->staged_agents;
 		rc = upload_agents(c, c->A, h.pos.data(), h.sec.data(), h.sat.data(), h.upt.data(), h.net.data(),
-						   h.vol.data(), h.active.data(), h.internal.data(), h.frac.data(), c->compute_internalized);
+						   h.vol.data(), h.active.data(), h.internal.empty() ? nullptr : h.internal.data(),
+						   h.frac.empty() ? nullptr : h.frac.data(), c->compute_internalized);
 		if (rc)
 			return rc;
 		c->staged_agents.reset();
 	}
+	if ((rc = ensure_device_state(c)) || (rc = launch_fill_initial(c)))
+		return rc;
 	c->initialized = true;
 	c->generation++;
-	return check_device(c);
+	return wait ? check_device(c) : PCG_OK;
 }
 
-int initialize_context(Context* c) { return do_initialize(c); }
+int initialize_context(Context* c, bool wait) { return do_initialize(c, wait); }
 int check_context(Context* c) { return check_device(c); }
 
 static int alloc_agents(Context* c, uint64_t A)
@@ -557,15 +732,16 @@ int upload_agents(Context* c, uint64_t A, const double* positions, const double*
 		if (internalized)
 			PCG_CUDA_TRY(cudaMemcpyAsync(c->a_internal.ptr, internalized, A * S * sizeof(double),
 										 cudaMemcpyHostToDevice, c->stream));
-		else
-			PCG_CUDA_TRY(cudaMemsetAsync(c->a_internal.ptr, 0, A * S * sizeof(double), c->stream));
 		if (fraction_released)
 			PCG_CUDA_TRY(cudaMemcpyAsync(c->a_frac.ptr, fraction_released, A * S * sizeof(double),
 										 cudaMemcpyHostToDevice, c->stream));
-		else
+		PCG_CUDA_TRY(stream_wait(c)); // the caller may free its arrays on return
+		// device-side clears after the host wait, which then waits for copies only
+		if (!internalized)
+			PCG_CUDA_TRY(cudaMemsetAsync(c->a_internal.ptr, 0, A * S * sizeof(double), c->stream));
+		if (!fraction_released)
 			PCG_CUDA_TRY(cudaMemsetAsync(c->a_frac.ptr, 0, A * S * sizeof(double), c->stream));
 		PCG_CUDA_TRY(cudaMemsetAsync(c->counts.ptr, 0, c->V * sizeof(uint32_t), c->stream));
-		PCG_CUDA_TRY(cudaStreamSynchronize(c->stream)); // the caller may free its arrays on return
 	}
 	c->recompute_cells = true;
 	c->terms_dirty = true;
@@ -646,7 +822,7 @@ int pcg_destroy(pcg_context* c)
 		return PCG_OK;
 	pcg::DeviceGuard g(c->device);
 	if (c->stream)
-		cudaStreamSynchronize(c->stream);
+		stream_wait(c);
 	if (c->rb_stream)
 		cudaStreamSynchronize(c->rb_stream);
 	pcg::collect_timings(c);
@@ -661,6 +837,7 @@ int pcg_destroy(pcg_context* c)
 								 &c->rb_staging[1] };
 	for (auto* b : all)
 		pcg::dfree(*b);
+	pcg::dfree(c->slab); // after the pieces carved from it
 	for (cudaEvent_t e : c->event_pool)
 		cudaEventDestroy(e);
 	for (int j = 0; j < 2; j++)
@@ -674,6 +851,9 @@ int pcg_destroy(pcg_context* c)
 		cudaStreamDestroy(c->rb_stream);
 	if (c->own_stream)
 		cudaStreamDestroy(c->own_stream);
+	pcg::pinned_words_put(c->h_words);
+	if (c->ev_block)
+		cudaEventDestroy(c->ev_block);
 	delete c;
 	return PCG_OK;
 }
@@ -850,10 +1030,10 @@ int pcg_set_agents(pcg_context* c, uint64_t A, const double* positions, const do
 		h->net.assign(net_export, net_export + A * S);
 		h->vol.assign(volumes, volumes + A);
 		h->active.assign(is_active, is_active + A);
-		h->internal = internalized ? std::vector<double>(internalized, internalized + A * S)
-								   : std::vector<double>(A * S, 0.0);
-		h->frac = fraction_released ? std::vector<double>(fraction_released, fraction_released + A * S)
-									: std::vector<double>(A * S, 0.0);
+		if (internalized)
+			h->internal.assign(internalized, internalized + A * S);
+		if (fraction_released)
+			h->frac.assign(fraction_released, fraction_released + A * S);
 		c->staged_agents = std::move(h);
 		c->A = A;
 		c->compute_internalized = compute_internalized != 0;
@@ -884,7 +1064,7 @@ int pcg_update_agents(pcg_context* c, const double* positions, const uint8_t* is
 									 cudaMemcpyHostToDevice, c->stream));
 	if (is_active)
 		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_active.ptr, is_active, c->A, cudaMemcpyHostToDevice, c->stream));
-	PCG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+	PCG_CUDA_TRY(stream_wait(c));
 	return PCG_OK;
 }
 
@@ -901,7 +1081,7 @@ int pcg_set_internalized(pcg_context* c, const double* internalized)
 	pcg::DeviceGuard g(c->device);
 	PCG_CUDA_TRY(cudaMemcpyAsync(c->a_internal.ptr, internalized, c->A * c->S * sizeof(double),
 								 cudaMemcpyHostToDevice, c->stream));
-	PCG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+	PCG_CUDA_TRY(stream_wait(c));
 	return PCG_OK;
 }
 
@@ -967,7 +1147,8 @@ int pcg_release_internalized(pcg_context* c, uint64_t agent)
 }
 
 // The device address of a host buffer mapped into the device's address space
-// (memory from cudaHostAlloc, or registered with cudaHostRegister), else null.
+// (memory from cudaHostAlloc, or registered with cudaHostRegister: pinned), else
+// null (pageable memory).
 static void* mapped_host_pointer(const void* host)
 {
 	cudaPointerAttributes at {};
@@ -991,18 +1172,16 @@ int pcg_get_field(pcg_context* c, void* host, int layout, int dtype)
 	int rc = pcg::do_initialize(c);
 	if (rc)
 		return rc;
+	// Conversion on the device into a staging buffer, then one copy by the copy
+	// engine.  (A kernel writing mapped host memory directly saves the staging pass,
+	// about 6 % at the host link's rate, but holds SMs for the whole transfer,
+	// which stalls other work on the device: a server's batched steps.)
 	const size_t hw = dtype == PCG_DTYPE_F32 ? 4 : 8;
-	if (void* mapped = mapped_host_pointer(host))
-	{
-		// pinned and mapped: the layout kernel writes the host buffer over the host
-		// link directly, without a staging copy
-		if ((rc = pcg::launch_to_host_layout(c, mapped, layout, dtype)))
-			return rc;
-		return pcg::check_device(c);
-	}
 	if (layout == PCG_LAYOUT_INTERLEAVED && hw == c->wsize)
 	{
-		// the device rows are the host rows plus padding: one strided copy, no kernel
+		// the device rows are the host rows plus padding: one strided copy, no
+		// kernel; queued once the stream is idle (see check_device)
+		PCG_CUDA_TRY(stream_wait(c));
 		PCG_CUDA_TRY(cudaMemcpy2DAsync(host, c->row_len * hw, c->field.ptr, c->pitch * hw, c->row_len * hw, c->rows,
 									   cudaMemcpyDeviceToHost, c->stream));
 		return pcg::check_device(c);
@@ -1012,6 +1191,8 @@ int pcg_get_field(pcg_context* c, void* host, int layout, int dtype)
 		return rc;
 	if ((rc = pcg::launch_to_host_layout(c, c->staging.ptr, layout, dtype)))
 		return rc;
+	// the copy is queued once the conversion is done (see check_device)
+	PCG_CUDA_TRY(stream_wait(c));
 	PCG_CUDA_TRY(cudaMemcpyAsync(host, c->staging.ptr, bytes, cudaMemcpyDeviceToHost, c->stream));
 	return pcg::check_device(c);
 }
@@ -1102,12 +1283,6 @@ int pcg_set_field(pcg_context* c, const void* host, int layout, int dtype)
 	if (rc)
 		return rc;
 	const size_t hw = dtype == PCG_DTYPE_F32 ? 4 : 8;
-	if (const void* mapped = mapped_host_pointer(host))
-	{
-		if ((rc = pcg::launch_from_host_layout(c, mapped, layout, dtype)))
-			return rc;
-		return pcg::check_device(c);
-	}
 	if (layout == PCG_LAYOUT_INTERLEAVED && hw == c->wsize)
 	{
 		PCG_CUDA_TRY(cudaMemcpy2DAsync(c->field.ptr, c->pitch * hw, host, c->row_len * hw, c->row_len * hw, c->rows,
@@ -1151,7 +1326,11 @@ int pcg_get_internalized(pcg_context* c, double* host)
 	CTX_CHECK(c);
 	if (c->staged_agents)
 	{
-		std::copy(c->staged_agents->internal.begin(), c->staged_agents->internal.end(), host);
+		const std::vector<double>& I = c->staged_agents->internal;
+		if (I.empty())
+			std::fill(host, host + c->A * c->S, 0.0);
+		else
+			std::copy(I.begin(), I.end(), host);
 		return PCG_OK;
 	}
 	pcg::DeviceGuard g(c->device);
@@ -1236,7 +1415,7 @@ int pcg_get_kernel_stats(pcg_context* c, pcg_kernel_stat* stats, uint64_t cap, u
 {
 	CTX_CHECK(c);
 	pcg::DeviceGuard g(c->device);
-	cudaStreamSynchronize(c->stream);
+	stream_wait(c);
 	pcg::collect_timings(c);
 	*count = pcg::K_COUNT;
 	for (uint64_t k = 0; k < cap && k < (uint64_t)pcg::K_COUNT; k++)
@@ -1254,7 +1433,7 @@ int pcg_reset_kernel_stats(pcg_context* c)
 {
 	CTX_CHECK(c);
 	pcg::DeviceGuard g(c->device);
-	cudaStreamSynchronize(c->stream);
+	stream_wait(c);
 	pcg::collect_timings(c);
 	for (auto& s : c->stats)
 		s = pcg::KernelStat {};

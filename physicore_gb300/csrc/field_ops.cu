@@ -212,11 +212,6 @@ int launch_mass(Context* c, double* out) { return c->wsize == 4 ? run_mass<float
 template <typename T>
 static int run_fill(Context* c)
 {
-	// initial conditions as T, staged through the mass buffer (S doubles >= S T's)
-	std::vector<T> h(c->S);
-	for (uint64_t s = 0; s < c->S; s++)
-		h[s] = (T)c->init[s];
-	PCG_CUDA_TRY(cudaMemcpyAsync(c->mass.ptr, h.data(), c->S * sizeof(T), cudaMemcpyHostToDevice, c->stream));
 	cudaEvent_t ev;
 	launch_begin(c, K_LAYOUT, (double)(c->rows * c->pitch * sizeof(T)), &ev);
 	fill_kernel<T><<<grid_for(c, c->rows * c->pitch, 256), 256, 0, c->stream>>>(

@@ -129,11 +129,25 @@ struct DeviceBuffer
 	void* ptr = nullptr;
 	size_t bytes = 0;
 	cudaStream_t stream = nullptr;
+	bool carved = false; // a piece of its context's slab: released with the slab
 };
 
 struct Context;
 
 int dalloc(Context* c, DeviceBuffer& b, size_t bytes);
+// Stream-ordered allocation from the library's pool on `device` (capi.cu), and the
+// bytes that pool holds free for reuse.
+cudaError_t pool_alloc(void** ptr, size_t bytes, cudaStream_t stream, int device);
+uint64_t pool_idle_bytes(int device);
+// Four pinned host words (capi.cu) for small device-to-host reads (error words):
+// a copy into pinned memory is a plain DMA, whereas a synchronous copy into
+// pageable memory goes through driver staging shared by every thread and, queued
+// behind other copies, stalls the transfers of all of them.  Null when pinned
+// memory cannot be had.
+uint32_t* pinned_words_get();
+void pinned_words_put(uint32_t* w);
+// Host wait for the context's stream, asleep rather than spinning (capi.cu).
+cudaError_t stream_wait(Context* c);
 void dfree(DeviceBuffer& b);
 
 struct KernelStat
@@ -174,6 +188,7 @@ struct Context
 	bool initialized = false;
 	bool recompute_cells = true;
 	bool terms_dirty = true; // agent rates or volumes uploaded since the agent terms were computed
+	bool words_cleared = false; // err/flags words zeroed on the device
 	// bumped by every call that may reallocate a device buffer or change a
 	// parameter; batches compare it with the value they captured
 	uint64_t generation = 0;
@@ -188,7 +203,14 @@ struct Context
 	uint64_t coef_elems[3] = { 0, 0, 0 };
 	uint64_t coef_comp_off[3] = { 0, 0, 0 }; // compressed tables (head rows, constants)
 	uint32_t coef_head[3] = { 0, 0, 0 };     // head points per substrate of the compressed tables
+	// One allocation at initialisation sized by estimate_device_bytes, from which
+	// the context's buffers are carved in turn (dozens of pool allocations per
+	// context cost milliseconds once many contexts come and go, as under a server)
+	DeviceBuffer slab;
+	size_t slab_used = 0;
 	DeviceBuffer err;      // uint32 device error word
+	uint32_t* h_words = nullptr; // pinned host words for reading it
+	cudaEvent_t ev_block = nullptr; // blocking-sync event for host waits on the stream
 	DeviceBuffer tickets;  // uint32 [4]: tile counters of the persistent sweeps
 	DeviceBuffer flags;    // uint32 [4]: [0] ballot conflict, [1] agents in shared voxels
 	DeviceBuffer mass;     // double [S]
@@ -227,7 +249,8 @@ struct Context
 	// initialize, so that an uninitialised context holds no device memory.
 	struct HostAgents
 	{
-		std::vector<double> pos, sec, sat, upt, net, vol, internal, frac;
+		std::vector<double> pos, sec, sat, upt, net, vol;
+		std::vector<double> internal, frac; // empty: all zero (cleared on the device, nothing copied)
 		std::vector<uint8_t> active;
 	};
 	std::unique_ptr<HostAgents> staged_agents;
@@ -275,7 +298,7 @@ int launch_release(Context* c, uint64_t agent);
 int launch_mass(Context* c, double* dev_out);
 int launch_to_host_layout(Context* c, void* dst, int layout, int dtype);
 int launch_from_host_layout(Context* c, const void* src, int layout, int dtype);
-int launch_fill_initial(Context* c);
+int launch_fill_initial(Context* c); // from the initial values already in c->mass (as T)
 
 // One FP32 cell secretion/uptake pass (ballot rebuilt) over caller-owned device
 // buffers, with the scratch arrays supplied by the caller as well; used by the
@@ -305,7 +328,7 @@ int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream);
 uint64_t estimate_device_bytes(const Context* c);
 
 // context lifecycle (capi.cu)
-int initialize_context(Context* c);  // allocates and uploads on first use
+int initialize_context(Context* c, bool wait = true); // allocates and uploads on first use
 int check_context(Context* c);       // synchronises and reports the device error word
 std::string device_error_text(uint32_t word);
 

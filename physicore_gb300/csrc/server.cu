@@ -39,7 +39,7 @@ struct GpuBackend
 			cudaGetLastError();
 			return 0;
 		}
-		return f;
+		return f + pool_idle_bytes(device); // blocks kept by the library's pool are free to it
 	}
 	uint64_t total_bytes()
 	{
@@ -55,7 +55,10 @@ struct GpuBackend
 	}
 	int admit(void* ctx)
 	{
-		const int rc = pcg_initialize(static_cast<pcg_context*>(ctx));
+		// without waiting for the field fill: the batch step that follows orders it
+		Context* c = static_cast<pcg_context*>(ctx);
+		DeviceGuard g(c->device);
+		const int rc = initialize_context(c, false);
 		if (rc)
 			err = pcg_last_error();
 		return rc;
@@ -88,6 +91,20 @@ struct GpuBackend
 		if (rc)
 			err = pcg_last_error();
 		return rc;
+	}
+	int readback(const serve::Request& r)
+	{
+		const int rc = pcg_get_field(static_cast<pcg_context*>(r.ctx), r.out, r.out_layout, r.out_dtype);
+		if (rc)
+			err = pcg_last_error();
+		return rc;
+	}
+	bool busy()
+	{
+		void* s = nullptr;
+		if (!batch || pcg_batch_get_stream(batch, &s) != PCG_OK)
+			return false;
+		return cudaStreamQuery(static_cast<cudaStream_t>(s)) == cudaErrorNotReady;
 	}
 	int step_end()
 	{
@@ -235,8 +252,17 @@ int pcg_server_destroy(pcg_server* s)
 
 int pcg_server_submit(pcg_server* s, pcg_context* ctx, uint64_t steps, uint64_t tag)
 {
+	return pcg_server_submit_readback(s, ctx, steps, tag, nullptr, PCG_LAYOUT_INTERLEAVED, PCG_DTYPE_F64);
+}
+
+int pcg_server_submit_readback(pcg_server* s, pcg_context* ctx, uint64_t steps, uint64_t tag, void* host, int layout,
+							   int dtype)
+{
 	if (!s || !ctx)
 		return fail(PCG_ERR_INVALID, "null argument");
+	if (host && ((layout != PCG_LAYOUT_INTERLEAVED && layout != PCG_LAYOUT_PLANAR) ||
+				 (dtype != PCG_DTYPE_F32 && dtype != PCG_DTYPE_F64)))
+		return fail(PCG_ERR_INVALID, "bad layout or dtype");
 	pcg::Context* c = ctx;
 	if (c->precision != s->precision || c->device != s->device)
 		return fail(PCG_ERR_INVALID, "the request's precision or device differs from the server's");
@@ -250,6 +276,9 @@ int pcg_server_submit(pcg_server* s, pcg_context* ctx, uint64_t steps, uint64_t 
 	r.steps = steps;
 	r.bytes = pcg::estimate_device_bytes(c);
 	r.vss_per_step = c->V * c->S;
+	r.out = host;
+	r.out_layout = layout;
+	r.out_dtype = dtype;
 	{
 		std::lock_guard<std::mutex> lk(s->mu);
 		r.t_submit = s->now();
@@ -323,6 +352,9 @@ int pcg_server_get_stats(pcg_server* s, pcg_server_stats* st)
 	st->active = s->active_snapshot;
 	st->in_flight = s->in_flight;
 	st->uptime_s = s->now();
+	st->rebuild_s = x.rebuild_s;
+	st->step_s = x.step_s;
+	st->admit_s = x.admit_s;
 	return PCG_OK;
 }
 

@@ -11,6 +11,8 @@
 //   int step_begin(uint64_t k, const std::vector<uint64_t>& budgets)
 //                                          start k steps, simulation i taking part in the first budgets[i]
 //   int step_end();                        wait for them
+//   bool busy();                           the started steps are still running
+//   int readback(const Request&);          copy a finished request's field to its host buffer
 //   std::string last_error();
 // so the same code runs against the GPU (server.cu) and against a fake backend in
 // the CPU tests (admission refusals, allocation failures, malformed requests,
@@ -21,7 +23,13 @@
 // steps); while they run, admit queued requests in arrival order while the active
 // set has room and the next request's device bytes plus a reserve fit in free
 // memory (admission overlaps the device work; admitted requests join at the next
-// regroup); then wait for the steps and retire the finished simulations.
+// regroup); then wait for the steps and retire the finished simulations.  While
+// simulations are stepping, admission stops once the steps are done (after at
+// least one admission), so the device is not left idle behind host-side uploads;
+// with nothing active it admits everything that fits.  A request submitted with
+// a host buffer has its field copied there by the worker right after the tick in
+// which it finished (the device has no other work of the server then), before it
+// is reported done; a failed copy reports it failed.
 // A request that does not fit now waits (memory is freed as active requests
 // finish and as callers destroy returned ones); it is refused only when it could
 // never fit (its bytes plus the reserve exceed total_bytes) or when its allocation
@@ -30,6 +38,7 @@
 #pragma once
 
 #include <algorithm>
+#include <chrono>
 #include <cstdint>
 #include <deque>
 #include <string>
@@ -54,6 +63,8 @@ struct Request
 	uint64_t vss_per_step = 0;
 	double t_submit = -1, t_admit = -1, t_done = -1; // t_submit < 0: stamped by submit()
 	uint32_t attempts = 0;   // admissions that failed for lack of memory
+	void* out = nullptr;     // host buffer for the field when done (null: the caller reads it)
+	int out_layout = 0, out_dtype = 0;
 	Status status = Status::Done;
 	int code = 0;
 	std::string error;
@@ -73,6 +84,9 @@ struct Stats
 	uint64_t ticks = 0, rebuilds = 0, steps = 0;
 	uint64_t vss = 0;               // voxel-substrate-steps performed
 	uint64_t active_bytes = 0;      // device bytes of the active set
+	double rebuild_s = 0;           // host time regrouping the active set
+	double step_s = 0;              // host time starting and waiting for steps (admission excluded)
+	double admit_s = 0;             // host time admitting requests
 };
 
 constexpr uint32_t kMaxAttempts = 3;
@@ -142,7 +156,9 @@ public:
 				std::vector<void*> ctxs;
 				for (const Request& r : active_)
 					ctxs.push_back(r.ctx);
+				const auto t0 = clock::now();
 				const int rc = be_.rebuild(ctxs);
+				stats_.rebuild_s += seconds_since(t0);
 				stats_.rebuilds++;
 				if (rc)
 				{
@@ -154,17 +170,23 @@ public:
 			const uint64_t k = opt_.steps_per_tick;
 			for (const Request& r : active_)
 				budgets.push_back(std::min(k, r.remaining));
+			const auto t0 = clock::now();
 			const int rc = be_.step_begin(k, budgets);
+			stats_.step_s += seconds_since(t0);
 			if (rc)
 			{
 				fail_active(rc, be_.last_error(), now);
 				return true;
 			}
 		}
-		const size_t admitted = admit(now); // overlaps the steps just started
+		auto t0 = clock::now();
+		const size_t admitted = admit(now, stepped > 0); // overlaps the steps just started
+		stats_.admit_s += seconds_since(t0);
 		if (!stepped)
 			return admitted > 0;
+		t0 = clock::now();
 		const int rc = be_.step_end();
+		stats_.step_s += seconds_since(t0);
 		if (rc)
 		{
 			fail_active(rc, be_.last_error(), now);
@@ -183,7 +205,11 @@ public:
 				{
 					stats_.active_bytes -= r.bytes;
 					dirty_ = true;
-					finish(r, Status::Done, 0, "", now);
+					const int rb = r.out ? be_.readback(r) : 0;
+					if (rb)
+						finish(r, Status::Failed, rb, be_.last_error(), now);
+					else
+						finish(r, Status::Done, 0, "", now);
 					continue;
 				}
 			}
@@ -227,11 +253,19 @@ public:
 	const Stats& stats() const { return stats_; }
 
 private:
-	size_t admit(double now)
+	using clock = std::chrono::steady_clock;
+	static double seconds_since(clock::time_point t0)
+	{
+		return std::chrono::duration<double>(clock::now() - t0).count();
+	}
+
+	size_t admit(double now, bool while_busy)
 	{
 		size_t admitted = 0;
 		while (!queue_.empty() && active_.size() < opt_.max_active)
 		{
+			if (while_busy && admitted > 0 && !be_.busy())
+				break; // the steps are done: start the next ones before admitting more
 			Request& r = queue_.front();
 			const uint64_t total = be_.total_bytes();
 			if (r.bytes + opt_.reserve_bytes > total)

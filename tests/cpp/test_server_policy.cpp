@@ -83,6 +83,20 @@ struct FakeBackend
 		return 0;
 	}
 	int step_end() { return 0; }
+	std::vector<void*> read_back;    // contexts whose field was copied out, in order
+	bool fail_readback = false;
+	int readback(const Request& r)
+	{
+		if (fail_readback)
+		{
+			err = "readback failed";
+			return 4;
+		}
+		read_back.push_back(r.ctx);
+		return 0;
+	}
+	int busy_polls = 0; // busy() answers true this many times
+	bool busy() { return busy_polls > 0 && busy_polls--; }
 	std::string last_error() const { return err; }
 	void release(void* c) // the caller destroys a returned context
 	{
@@ -254,6 +268,55 @@ void step_fault_fails_the_active_set()
 	EXPECT(s.idle() && s.stats().active_bytes == 0);
 }
 
+void admission_stops_when_steps_finish()
+{
+	FakeBackend be;
+	Options o;
+	o.reserve_bytes = 0;
+	o.steps_per_tick = 1;
+	Scheduler<FakeBackend> s(be, o);
+	s.submit(req(be, 1, 100, 10), 0);
+	s.tick(0); // nothing active: admitted without waiting for anything
+	EXPECT(s.active() == 1);
+	for (int i = 2; i <= 6; i++)
+		s.submit(req(be, i, 100, 10), 0);
+	be.busy_polls = 0; // the steps finish at once: one admission, then the next tick
+	s.tick(1);
+	EXPECT(s.active() == 2 && s.queued() == 4);
+	be.busy_polls = 2; // still running for two more admissions
+	s.tick(2);
+	EXPECT(s.active() == 5 && s.queued() == 1);
+	EXPECT(s.stats().admit_s >= 0 && s.stats().step_s >= 0 && s.stats().rebuild_s >= 0);
+}
+
+void readback_before_done()
+{
+	FakeBackend be;
+	Options o;
+	o.reserve_bytes = 0;
+	o.steps_per_tick = 4;
+	Scheduler<FakeBackend> s(be, o);
+	static float buf[4];
+	Request a = req(be, 1, 4, 10);
+	a.out = buf;
+	Request b = req(be, 2, 8, 10); // no buffer: the caller reads the field itself
+	Request c = req(be, 3, 4, 10);
+	c.out = buf;
+	s.submit(a, 0);
+	s.submit(b, 0);
+	s.tick(0);
+	s.tick(1); // 1 finishes: read back before it is reported
+	auto f = s.take_finished();
+	EXPECT(f.size() == 1 && !f.empty() && f[0].tag == 1 && f[0].status == Status::Done);
+	EXPECT(be.read_back.size() == 1 && !be.read_back.empty() && be.read_back[0] == ctx(1));
+	be.fail_readback = true;
+	s.submit(c, 1);
+	auto done = run(s, be);
+	EXPECT(find(done, 2) && find(done, 2)->status == Status::Done);          // no readback asked
+	EXPECT(find(done, 3) && find(done, 3)->status == Status::Failed && find(done, 3)->error == "readback failed");
+	EXPECT(be.read_back.size() == 1);
+}
+
 void queue_limit_and_zero_steps()
 {
 	FakeBackend be;
@@ -283,6 +346,8 @@ int main()
 		{ "ServerPolicy.Cancellation", cancellation },
 		{ "ServerPolicy.StepFaultFailsTheActiveSet", step_fault_fails_the_active_set },
 		{ "ServerPolicy.QueueLimitAndZeroSteps", queue_limit_and_zero_steps },
+		{ "ServerPolicy.AdmissionStopsWhenStepsFinish", admission_stops_when_steps_finish },
+		{ "ServerPolicy.ReadbackBeforeDone", readback_before_done },
 	};
 	int n = 0;
 	for (auto& t : tests)

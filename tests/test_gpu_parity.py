@@ -127,8 +127,8 @@ def test_layouts_round_trip(pcg):
 
 
 def test_layouts_pinned_host_buffers(pcg):
-    """Pinned (device-mapped) host buffers take the direct path (the layout kernel
-    reads or writes host memory); results equal the staged copies of pageable ones."""
+    """Pinned host buffers (copied without driver staging) give the same fields as
+    pageable ones, in every layout and element type."""
     torch = pytest.importorskip("torch")
     for prec in (pcg.FP64, pcg.FP32):
         p = W.random_small(11)

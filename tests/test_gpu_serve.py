@@ -49,11 +49,22 @@ def test_served_results_equal_alone(pcg):
         s.close()
     srv = pcg.Server(pcg.FP32, steps_per_tick=4, reserve_bytes=0)
     half = len(probs) // 2
+    outs = {}
+
+    def submit(k, p, steps):
+        s = W.apply(pcg.Solver(pcg.FP32), p, initialize=False)
+        if k % 2:  # odd requests: the server reads the field back before returning them
+            nx, ny, nz = s.grid
+            outs[k] = np.full((s.S, nz, ny, nx), np.nan, np.float32)
+            srv.submit(s, steps, k, out=outs[k], layout=pcg.LAYOUT_PLANAR)
+        else:
+            srv.submit(s, steps, k)
+
     for k, (p, steps) in enumerate(probs[:half]):
-        srv.submit(W.apply(pcg.Solver(pcg.FP32), p, initialize=False), steps, k)
+        submit(k, p, steps)
     time.sleep(0.05)  # the first ones are running when the rest arrive
     for k, (p, steps) in enumerate(probs[half:], start=half):
-        srv.submit(W.apply(pcg.Solver(pcg.FP32), p, initialize=False), steps, k)
+        submit(k, p, steps)
     res = _wait_all(srv, len(probs))
     for k, (p, steps) in enumerate(probs):
         r = res[k]
@@ -61,6 +72,8 @@ def test_served_results_equal_alone(pcg):
         s = r["solver"]
         e = rel_err(s.get_field(), alone[k][0])
         assert e <= FP32_RTOL, f"{p['name']}: served vs alone {e:.3e}"
+        if k in outs:
+            assert np.array_equal(outs[k], s.get_field(layout=pcg.LAYOUT_PLANAR, dtype=np.float32)), k
         if alone[k][1] is not None:
             assert np.array_equal(s.get_counts(), alone[k][1]), p["name"]
         assert 0 <= r["t_submit"] <= r["t_admit"] <= r["t_done"]
