@@ -94,7 +94,9 @@ struct WorkList
 {
 	const uint64_t* base;
 	const uint32_t* dom;
+	const uint32_t* hint; // hint[j]: the entry holding unit j << shift
 	uint32_t count;
+	uint32_t shift;
 	uint64_t total;
 };
 
@@ -109,18 +111,15 @@ struct BatchArgs
 	uint32_t* steps_left;     // per domain: steps still to run in this call (0: the domain sits out)
 };
 
+// The entry holding unit u < total: from the hint of u's block, forward over the
+// entries that start inside the block (usually none or one), instead of a binary
+// search's chain of dependent loads.
 __device__ __forceinline__ uint32_t find_entry(const WorkList& l, uint64_t u)
 {
-	uint32_t lo = 0, hi = l.count;
-	while (hi - lo > 1)
-	{
-		const uint32_t mid = (lo + hi) >> 1;
-		if (__ldg(l.base + mid) <= u)
-			lo = mid;
-		else
-			hi = mid;
-	}
-	return lo;
+	uint32_t k = __ldg(l.hint + (u >> l.shift));
+	while (k + 1 < l.count && __ldg(l.base + k + 1) <= u)
+		k++;
+	return k;
 }
 
 // find_entry for the 32 lanes of a warp holding ascending units (all lanes must
@@ -267,14 +266,19 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 	}
 	__syncthreads();
 	uint32_t phase = 0;
+	uint32_t next = 0;
+	if (tid == 0)
+		next = atomicAdd(b.counter, 1u);
 	for (;;)
 	{
 		if (tid == 0)
-			s_ticket = atomicAdd(b.counter, 1u);
+			s_ticket = next;
 		__syncthreads();
 		const uint64_t t = s_ticket;
 		if (t >= b.list.total)
 			break;
+		if (tid == 0)
+			next = atomicAdd(b.counter, 1u); // the following tile's ticket, in flight meanwhile
 		const uint32_t k = find_entry(b.list, t);
 		const uint32_t di = __ldg(b.list.dom + k);
 		if (b.steps_left[di] == 0)
@@ -294,6 +298,13 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 		__syncthreads();
 		if (tid < nrows)
 			dev::bulk_g2s(tile + tid * spitch, g + tid * D.pitch, row_bytes, bar);
+		const T* cB = static_cast<const T*>(D.coef[0]);
+		const T* cE = cB + D.coef_len[0];
+		const T* cC = cE + D.coef_len[0];
+		const uint32_t rl = tid / S, s = tid % S;
+		LineCoef<T> L {};
+		if (D.x_mode != kMapRow) // coefficient loads overlap the tile's arrival
+			L = line_coef<T>(static_cast<const T*>(D.coef[0]) + D.coef_comp_off[0], S, D.coef_head[0], n, s);
 		const bool ok = __all_sync(0xffffffffu, dev::mbar_wait(bar, phase));
 		if (!ok)
 		{
@@ -301,24 +312,13 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 				report(b, DEV_ERR_WAIT_TIMEOUT, di);
 			return;
 		}
-		const T* cB = static_cast<const T*>(D.coef[0]);
-		const T* cE = cB + D.coef_len[0];
-		const T* cC = cE + D.coef_len[0];
 		if (D.x_mode == kMapRow)
 		{
 			if (tid < nrows)
 				solve_x_row<T>(tile + tid * spitch, cB, cE, cC, n, S);
 		}
-		else
-		{
-			const uint32_t rl = tid / S, s = tid % S;
-			if (rl < nrows)
-			{
-				const LineCoef<T> L =
-					line_coef<T>(static_cast<const T*>(D.coef[0]) + D.coef_comp_off[0], S, D.coef_head[0], n, s);
-				solve_line<T, 0>(tile + rl * spitch + s, n, S, L);
-			}
-		}
+		else if (rl < nrows)
+			solve_line<T, 0>(tile + rl * spitch + s, n, S, L);
 		dev::fence_proxy_async_smem();
 		__syncthreads();
 		if (tid < nrows)
@@ -350,14 +350,16 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 	__syncwarp();
 	uint32_t phase = 0, prev = 0xffffffffu, bad = 0;
 	bool ok = true;
+	uint32_t next = 0;
+	if (lane == 0)
+		next = atomicAdd(b.counter, 1u);
 	for (;; phase ^= 1)
 	{
-		uint32_t t32 = 0;
-		if (lane == 0)
-			t32 = atomicAdd(b.counter, 1u);
-		const uint64_t t = __shfl_sync(0xffffffffu, t32, 0);
+		const uint64_t t = __shfl_sync(0xffffffffu, next, 0);
 		if (t >= b.list.total)
 			break;
+		if (lane == 0)
+			next = atomicAdd(b.counter, 1u); // the following tile's ticket, in flight meanwhile
 		const uint32_t k = find_entry(b.list, t);
 		const uint32_t di = __ldg(b.list.dom + k);
 		if (b.steps_left[di] == 0)
@@ -386,6 +388,10 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 			}
 		}
 		prev = di;
+		// coefficient loads overlap the tile's arrival
+		const uint32_t s = (uint64_t)(x0 + lane) < D.row_len ? (uint32_t)((x0 + lane) % S) : 0;
+		const LineCoef<T> L =
+			line_coef<T>(static_cast<const T*>(D.coef[AXIS]) + D.coef_comp_off[AXIS], S, D.coef_head[AXIS], n, s);
 		ok = __all_sync(0xffffffffu, dev::mbar_wait(full, phase));
 		if (!ok)
 		{
@@ -393,9 +399,6 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 			break;
 		}
 		{
-			const uint32_t s = (uint64_t)(x0 + lane) < D.row_len ? (uint32_t)((x0 + lane) % S) : 0;
-			const LineCoef<T> L = line_coef<T>(static_cast<const T*>(D.coef[AXIS]) + D.coef_comp_off[AXIS], S,
-											   D.coef_head[AXIS], n, s);
 			solve_line<T, kLanes>(base + lane, n, 0, L);
 			// the last sweep of the domain writes its boundary faces (the batch's
 			// Dirichlet launch then covers interior nodes and 1-D domains only)
@@ -928,9 +931,31 @@ HostList build_list(pcg_batch* b, int id, const std::vector<size_t>& subset)
 int upload_lists(DeviceBuffer& buf, const std::vector<HostList>& hl, WorkList* out, cudaStream_t stream,
 				 int device)
 {
+	// lookup hints: one entry index per block of 2^shift units, at most 2^18 blocks
+	std::vector<std::vector<uint32_t>> hints(hl.size());
+	std::vector<uint32_t> shifts(hl.size(), 0);
 	size_t bytes = 0;
-	for (const auto& h : hl)
-		bytes += round_up(h.base.size() * 8, 256) + round_up(std::max<size_t>(h.dom.size(), 1) * 4, 256);
+	for (size_t i = 0; i < hl.size(); i++)
+	{
+		const HostList& h = hl[i];
+		const uint64_t total = h.base.back();
+		uint32_t shift = 0;
+		while ((total >> shift) > (1ull << 18))
+			shift++;
+		std::vector<uint32_t>& hint = hints[i];
+		hint.resize((size_t)(total >> shift) + 1);
+		uint32_t k = 0;
+		for (size_t j = 0; j < hint.size(); j++)
+		{
+			const uint64_t u = (uint64_t)j << shift;
+			while (k + 1 < h.dom.size() && h.base[k + 1] <= u)
+				k++;
+			hint[j] = k;
+		}
+		shifts[i] = shift;
+		bytes += round_up(h.base.size() * 8, 256) + round_up(std::max<size_t>(h.dom.size(), 1) * 4, 256) +
+				 round_up(hint.size() * 4, 256);
+	}
 	int rc = balloc(buf, bytes, stream, device);
 	if (rc)
 		return rc;
@@ -946,7 +971,11 @@ int upload_lists(DeviceBuffer& buf, const std::vector<HostList>& hl, WorkList* o
 			memcpy(host.data() + off, h.dom.data(), h.dom.size() * 4);
 		out[i].dom = reinterpret_cast<const uint32_t*>(static_cast<unsigned char*>(buf.ptr) + off);
 		off += round_up(std::max<size_t>(h.dom.size(), 1) * 4, 256);
+		memcpy(host.data() + off, hints[i].data(), hints[i].size() * 4);
+		out[i].hint = reinterpret_cast<const uint32_t*>(static_cast<unsigned char*>(buf.ptr) + off);
+		off += round_up(hints[i].size() * 4, 256);
 		out[i].count = (uint32_t)h.dom.size();
+		out[i].shift = shifts[i];
 		out[i].total = h.base.back();
 	}
 	PCG_CUDA_TRY(cudaMemcpyAsync(buf.ptr, host.data(), bytes, cudaMemcpyHostToDevice, stream));
