@@ -597,17 +597,24 @@ __global__ void batch_cells_apply_kernel(BatchArgs b)
 }
 
 template <typename T>
-__global__ void batch_cells_internalize_kernel(BatchArgs b)
+__global__ void batch_cells_internalize_kernel(BatchArgs b, uint32_t ndom)
 {
-	const uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-	const uint32_t k = warp_entry(b.list, u);
-	if (u >= b.list.total || !b.steps_left[__ldg(b.list.dom + k)])
-		return;
-	const CellArgs& a = b.doms[__ldg(b.list.dom + k)].cells;
-	// the first flags[1] agent slots of a domain take its list of agents in shared voxels
-	const uint64_t j = u - __ldg(b.list.base + k);
-	if (a.internalized && j < __ldg(a.flags + 1))
-		agent_internalize<T>(a, __ldg(a.shared + j));
+	// Work is the domains' lists of agents in shared voxels (a few percent of the
+	// agents), whose lengths are on the device: blocks take domains in turn, and
+	// with more blocks than domains each domain's list is split among its blocks.
+	const uint32_t G = gridDim.x;
+	const uint32_t first = G >= ndom ? blockIdx.x % ndom : blockIdx.x;
+	const uint32_t part = G >= ndom ? blockIdx.x / ndom : 0;
+	for (uint32_t d = first; d < ndom; d += (G >= ndom ? ndom : G))
+	{
+		const uint32_t parts = G >= ndom ? (G - d + ndom - 1) / ndom : 1;
+		const CellArgs& a = b.doms[d].cells;
+		if (!b.steps_left[d] || !a.internalized || !a.A)
+			continue;
+		const uint32_t count = __ldg(a.flags + 1);
+		for (uint64_t j = (uint64_t)part * blockDim.x + threadIdx.x; j < count; j += (uint64_t)parts * blockDim.x)
+			agent_internalize<T>(a, __ldg(a.shared + j));
+	}
 }
 
 // End of a step: one step fewer for every domain still running.
@@ -747,9 +754,12 @@ struct pcg_batch
 	bool dev_recompute_valid = false;
 
 	bool use_graph = true;
-	cudaGraphExec_t exec = nullptr;
-	uint64_t kernels_per_step = 0;
-	pcg::KernelStat graph_step[pcg::K_COUNT]; // launches and bytes of one replayed step
+	// graphs of one step with [1] and without [0] the ballot-rebuild kernels (clear,
+	// locate, ballot, reduce): calls in which no domain rebuilds its ballot skip them
+	cudaGraphExec_t exec[2] = { nullptr, nullptr };
+	uint64_t kernels_per_step[2] = { 0, 0 };
+	pcg::KernelStat graph_step[2][pcg::K_COUNT]; // launches and bytes of one replayed step
+	bool step_rebuilds = true;                    // launch_step includes the rebuild kernels
 
 	bool timing = false;
 	double step_bytes[pcg::K_COUNT] = {}; // algorithmic bytes of one launch of each kernel
@@ -1015,11 +1025,12 @@ int upload_domains(pcg_batch* b)
 
 void drop_graph(pcg_batch* b)
 {
-	if (b->exec)
-	{
-		cudaGraphExecDestroy(b->exec);
-		b->exec = nullptr;
-	}
+	for (auto& x : b->exec)
+		if (x)
+		{
+			cudaGraphExecDestroy(x);
+			x = nullptr;
+		}
 }
 
 template <typename T>
@@ -1271,26 +1282,29 @@ int launch_step(pcg_batch* b)
 	if (A)
 	{
 		const unsigned g = (unsigned)((A + 255) / 256);
+		if (b->step_rebuilds)
 		{
-			LaunchScope s(b, K_CELLS_CLEAR, sb[K_CELLS_CLEAR]);
-			batch_clear_counts_kernel<<<flat_grid(b, b->lists[L_CLEAR].total * 32, 256), 256, 0, b->stream>>>(
-				args_for(b, L_CLEAR, 3));
-			PCG_CUDA_TRY(cudaGetLastError());
-		}
-		{
-			LaunchScope s(b, K_CELLS_LOCATE, sb[K_CELLS_LOCATE]);
-			batch_cells_locate_kernel<T><<<g, 256, 0, b->stream>>>(args_for(b, L_AGENTS, 3));
-			PCG_CUDA_TRY(cudaGetLastError());
-		}
-		{
-			LaunchScope s(b, K_CELLS_BALLOT, sb[K_CELLS_BALLOT]);
-			batch_cells_ballot_kernel<<<g, 256, 0, b->stream>>>(args_for(b, L_AGENTS, 3));
-			PCG_CUDA_TRY(cudaGetLastError());
-		}
-		{
-			LaunchScope s(b, K_CELLS_REDUCE, sb[K_CELLS_REDUCE]);
-			batch_cells_reduce_kernel<T><<<g, 256, 0, b->stream>>>(args_for(b, L_AGENTS, 3));
-			PCG_CUDA_TRY(cudaGetLastError());
+			{
+				LaunchScope s(b, K_CELLS_CLEAR, sb[K_CELLS_CLEAR]);
+				batch_clear_counts_kernel<<<flat_grid(b, b->lists[L_CLEAR].total * 32, 256), 256, 0, b->stream>>>(
+					args_for(b, L_CLEAR, 3));
+				PCG_CUDA_TRY(cudaGetLastError());
+			}
+			{
+				LaunchScope s(b, K_CELLS_LOCATE, sb[K_CELLS_LOCATE]);
+				batch_cells_locate_kernel<T><<<g, 256, 0, b->stream>>>(args_for(b, L_AGENTS, 3));
+				PCG_CUDA_TRY(cudaGetLastError());
+			}
+			{
+				LaunchScope s(b, K_CELLS_BALLOT, sb[K_CELLS_BALLOT]);
+				batch_cells_ballot_kernel<<<g, 256, 0, b->stream>>>(args_for(b, L_AGENTS, 3));
+				PCG_CUDA_TRY(cudaGetLastError());
+			}
+			{
+				LaunchScope s(b, K_CELLS_REDUCE, sb[K_CELLS_REDUCE]);
+				batch_cells_reduce_kernel<T><<<g, 256, 0, b->stream>>>(args_for(b, L_AGENTS, 3));
+				PCG_CUDA_TRY(cudaGetLastError());
+			}
 		}
 		{
 			LaunchScope s(b, K_CELLS_APPLY, sb[K_CELLS_APPLY]);
@@ -1299,7 +1313,9 @@ int launch_step(pcg_batch* b)
 		}
 		{
 			LaunchScope s(b, K_CELLS_INTERNALIZE, sb[K_CELLS_INTERNALIZE]);
-			batch_cells_internalize_kernel<T><<<g, 256, 0, b->stream>>>(args_for(b, L_AGENTS, 3));
+			const uint32_t ndom = (uint32_t)b->ctx.size();
+			batch_cells_internalize_kernel<T><<<8 * std::max(b->sm_count, 1), 256, 0, b->stream>>>(
+				args_for(b, L_AGENTS, 3), ndom);
 			PCG_CUDA_TRY(cudaGetLastError());
 		}
 	}
@@ -1311,9 +1327,8 @@ int launch_step(pcg_batch* b)
 
 int step(pcg_batch* b) { return b->wsize == 4 ? launch_step<float>(b) : launch_step<double>(b); }
 
-int capture(pcg_batch* b)
+int capture(pcg_batch* b, int rebuilds)
 {
-	drop_graph(b);
 	cudaGraph_t g = nullptr;
 	const uint64_t before = b->launches;
 	KernelStat stats_before[K_COUNT];
@@ -1321,6 +1336,7 @@ int capture(pcg_batch* b)
 	PCG_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
 	const bool timing = b->timing;
 	b->timing = false;
+	b->step_rebuilds = rebuilds != 0;
 	int rc = step(b);
 	b->timing = timing;
 	cudaError_t e = cudaStreamEndCapture(b->stream, &g);
@@ -1332,21 +1348,21 @@ int capture(pcg_batch* b)
 	}
 	if (e != cudaSuccess)
 		return fail(PCG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-	e = cudaGraphInstantiate(&b->exec, g, 0);
+	e = cudaGraphInstantiate(&b->exec[rebuilds], g, 0);
 	cudaGraphDestroy(g);
 	if (e != cudaSuccess)
 	{
-		b->exec = nullptr;
+		b->exec[rebuilds] = nullptr;
 		return fail(PCG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
 	}
 	// capture counted the step's kernels once without running them: keep the
 	// per-step counts and add them on every replay instead
-	b->kernels_per_step = b->launches - before;
+	b->kernels_per_step[rebuilds] = b->launches - before;
 	b->launches = before;
 	for (int k = 0; k < K_COUNT; k++)
 	{
-		b->graph_step[k].launches = b->stats[k].launches - stats_before[k].launches;
-		b->graph_step[k].bytes = b->stats[k].bytes - stats_before[k].bytes;
+		b->graph_step[rebuilds][k].launches = b->stats[k].launches - stats_before[k].launches;
+		b->graph_step[rebuilds][k].bytes = b->stats[k].bytes - stats_before[k].bytes;
 		b->stats[k] = stats_before[k];
 	}
 	return PCG_OK;
@@ -1438,7 +1454,7 @@ int upload_recompute(pcg_batch* b)
 		for (size_t d = 0; d < N; d++)
 			sum += b->h_recompute[d] ? b->rebuild_bytes[d][k] : 0.0;
 		b->step_bytes[rebuild_kernels[k]] = sum;
-		b->graph_step[rebuild_kernels[k]].bytes = sum;
+		b->graph_step[1][rebuild_kernels[k]].bytes = sum;
 	}
 	if (b->dev_recompute_valid && b->dev_recompute == b->h_recompute)
 		return PCG_OK;
@@ -1839,21 +1855,26 @@ int pcg_batch_solve_budgets(pcg_batch* b, uint64_t iterations, const uint64_t* b
 	PCG_CUDA_TRY(cudaMemcpyAsync(b->d_steps_left.ptr, b->h_steps_left.data(), b->ctx.size() * sizeof(uint32_t),
 								 cudaMemcpyHostToDevice, b->stream));
 	// pageable source: the copy is staged before the call returns, so the next call may rewrite it
+	// the ballot-rebuild kernels run only in calls where some stepping domain rebuilds
+	int rebuilds = 0;
+	for (size_t d = 0; d < b->ctx.size(); d++)
+		rebuilds |= b->h_recompute[d] && b->h_steps_left[d] > 0;
+	b->step_rebuilds = rebuilds != 0;
 	const bool graph = b->use_graph && !b->timing;
-	if (graph && !b->exec && (rc = pcg::capture(b)))
+	if (graph && !b->exec[rebuilds] && (rc = pcg::capture(b, rebuilds)))
 		return rc;
 	for (uint64_t it = 0; it < iterations; it++)
 	{
 		if (graph)
 		{
-			cudaError_t e = cudaGraphLaunch(b->exec, b->stream);
+			cudaError_t e = cudaGraphLaunch(b->exec[rebuilds], b->stream);
 			if (e != cudaSuccess)
 				return fail(PCG_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
-			b->launches += b->kernels_per_step;
+			b->launches += b->kernels_per_step[rebuilds];
 			for (int k = 0; k < pcg::K_COUNT; k++)
 			{
-				b->stats[k].launches += b->graph_step[k].launches;
-				b->stats[k].bytes += b->graph_step[k].bytes;
+				b->stats[k].launches += b->graph_step[rebuilds][k].launches;
+				b->stats[k].bytes += b->graph_step[rebuilds][k].bytes;
 			}
 		}
 		else if ((rc = pcg::step(b)))

@@ -85,9 +85,22 @@ struct GpuBackend
 		}
 		return rc;
 	}
+	// The tick's first step in a call of its own: requests admitted since the last
+	// tick rebuild their ballots there (their agents do not move while served), and
+	// the remaining steps replay the step without the ballot-rebuild kernels.
+	std::vector<uint64_t> first_, rest_;
 	int step_begin(uint64_t k, const std::vector<uint64_t>& budgets)
 	{
-		const int rc = pcg_batch_solve_budgets(batch, k, budgets.data());
+		first_.resize(budgets.size());
+		rest_.resize(budgets.size());
+		for (size_t i = 0; i < budgets.size(); i++)
+		{
+			first_[i] = std::min<uint64_t>(budgets[i], 1);
+			rest_[i] = budgets[i] - first_[i];
+		}
+		int rc = pcg_batch_solve_budgets(batch, 1, first_.data());
+		if (!rc && k > 1)
+			rc = pcg_batch_solve_budgets(batch, k - 1, rest_.data());
 		if (rc)
 			err = pcg_last_error();
 		return rc;
