@@ -91,6 +91,27 @@ def test_random_fp32(pcg, oracle_mod, seed):
           den_max=max_denominator(p))
 
 
+@pytest.mark.parametrize("shape,S", [((6, 300, 5), 3), ((5, 4, 330), 2), ((4, 264, 250), 5), ((3, 7, 420), 1)])
+def test_long_lines_with_faces(pcg, oracle_mod, shape, S):
+    """y/z lines longer than the 216 points an FP32 tile keeps in shared memory
+    (the rest of each line is held in registers), with Dirichlet on all six faces
+    written by the last sweep, interior nodes and agents, against the oracle."""
+    rng = np.random.default_rng(sum(shape) * 7 + S)
+    nx, ny, nz = shape
+    pos = rng.random((400, 3)) * np.array(shape) * 10.0
+    ag = W.agents_block(rng, 400, S, pos)
+    vox = np.stack([rng.integers(0, v, 30) for v in shape], axis=1).astype(np.uint64)
+    lin = np.unique(vox[:, 0] + nx * (vox[:, 1] + ny * vox[:, 2]))
+    vox = np.stack([lin % nx, (lin // nx) % ny, lin // (nx * ny)], axis=1).astype(np.uint64)
+    p = dict(name=f"long_{nx}x{ny}x{nz}_{S}", dims=3, bbmin=(0, 0, 0), bbmax=(nx * 10, ny * 10, nz * 10),
+             voxel=(10, 10, 10), dt=0.05, D=W.log_uniform(rng, 1, 1e4, S), decay=W.log_uniform(rng, 1e-3, 1, S),
+             initial=np.zeros(S), field=rng.random((nz, ny, nx, S)), field_layout="interleaved",
+             boundary=[(ax, side, rng.random(S), [1] * S) for ax in range(3) for side in (0, 1)],
+             interior=(vox, rng.random((len(vox), S)), np.ones((len(vox), S), np.uint8)), bulk=None,
+             agents=ag, compute_internalized=True)
+    check(run_both(pcg, oracle_mod, p, pcg.FP32), 1e-5, p["name"], voxel_volume=1000.0, den_max=max_denominator(p))
+
+
 @pytest.mark.parametrize("n,S", [(1, 1), (2, 3), (3, 5), (4, 2), (33, 7), (64, 1), (65, 4), (130, 2), (320, 1)])
 def test_sweep_line_lengths(pcg, oracle_mod, n, S):
     """Line lengths around the 16-byte vector and 32-lane tile edges, in every axis."""
