@@ -307,6 +307,8 @@ def run_gb300(args, w):
         line["batched"] = run_batched(args, local, ClockSampler)
     if args.serve_duration > 0:
         line["serve"] = run_serve(args, local)
+    if args.dense_steps > 0:
+        line["dense"] = run_dense(args, local)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -564,6 +566,66 @@ def run_serve(args, local):
             "steps_per_tick": args.serve_tick, "wall_s": round(wall, 2)}
 
 
+def run_dense(args, local):
+    """The dense-agent stress workload (200^3 x 4 FP32, 4,000,000 agents in a
+    Gaussian cluster of sigma 200 um, up to ~100 agents per voxel): device time per
+    step with the agents fixed, and with the ballot rebuilt every step (as when the
+    agents move each step), with the cell kernels' times."""
+    import torch
+
+    import physicore_gb300 as pcg
+    from physicore_gb300 import workloads as W
+    p = W.dense()
+    s = W.apply(pcg.Solver(pcg.FP32, device=local), p)
+    cs = torch.cuda.Stream()
+    s.set_stream(cs.cuda_stream)
+    steps = args.dense_steps
+    for _ in range(max(3, args.warmup)):
+        s.solve(1)
+    s.synchronize()
+    counts = s.get_counts()
+
+    def timed(k, rebuild):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(cs)
+        for _ in range(k):
+            if rebuild:
+                s.recompute_positional_data()
+            s.solve(1)
+        ev1.record(cs)
+        ev1.synchronize()
+        return ev0.elapsed_time(ev1) / k
+
+    def kernels(k, rebuild):
+        s.set_kernel_timing(True)
+        s.reset_kernel_stats()
+        for _ in range(k):
+            if rebuild:
+                s.recompute_positional_data()
+            s.solve(1)
+        s.synchronize()
+        st = s.kernel_stats()
+        s.set_kernel_timing(False)
+        return {kk: round(v["ms"] / v["launches"] * 1e3, 1) for kk, v in st.items() if v["launches"]}
+
+    vss = s.voxels * s.S
+    A = int(p["agents"]["volumes"].size)
+    ms_fixed = timed(steps, False)
+    ms_moving = timed(max(10, steps // 5), True)
+    out = {"workload": "dense_200: 200^3 voxels x 4 substrates FP32, 4,000,000 agents N(centre, 200 um) "
+                       "(internalized tracking on)", "vss_per_step": vss, "agents": A,
+           "max_agents_per_voxel": int(counts.max()), "occupied_voxels": int((counts > 0).sum()),
+           "steps": steps,
+           "agents_fixed": {"ms_per_step": ms_fixed, "value": vss / (ms_fixed / 1e3), "unit": UNIT,
+                            "agent_steps_per_s": A / (ms_fixed / 1e3), "kernels_us": kernels(10, False)},
+           "ballot_rebuilt_every_step": {"ms_per_step": ms_moving, "value": vss / (ms_moving / 1e3), "unit": UNIT,
+                                         "agent_steps_per_s": A / (ms_moving / 1e3),
+                                         "kernels_us": kernels(10, True)}}
+    s.set_stream(None)
+    s.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -582,6 +644,8 @@ def main():
     ap.add_argument("--serve-tick", type=int, default=8, help="steps between admission points")
     ap.add_argument("--only-serve", action="store_true", help="run only the served request stream")
     ap.add_argument("--serve-plain-sample", type=int, default=100, help="requests timed one after another")
+    ap.add_argument("--dense-steps", type=int, default=100, help="steps of the dense-agent workload (0: skip)")
+    ap.add_argument("--only-dense", action="store_true", help="run only the dense-agent workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -592,6 +656,10 @@ def main():
         import torch
         torch.cuda.set_device(dist_env()[2])
         print(json.dumps(run_serve(args, dist_env()[2])), flush=True)
+    elif args.only_dense:
+        import torch
+        torch.cuda.set_device(dist_env()[2])
+        print(json.dumps(run_dense(args, dist_env()[2])), flush=True)
     elif args.only_batched:
         import torch
         torch.cuda.set_device(dist_env()[2])

@@ -708,6 +708,31 @@ static int alloc_agents(Context* c, uint64_t A)
 	return PCG_OK;
 }
 
+// FP32 contexts hold internalized amounts as pairs of floats hi + lo in the 8 bytes
+// of each double (hi first; cells_device.cuh, pair_add); conversions at the API.
+static void to_pairs(const double* in, std::vector<double>& out, size_t n)
+{
+	out.resize(n);
+	for (size_t k = 0; k < n; k++)
+	{
+		const float hi = (float)in[k];
+		const float lo = (float)(in[k] - (double)hi);
+		std::memcpy(reinterpret_cast<char*>(&out[k]), &hi, sizeof(float));
+		std::memcpy(reinterpret_cast<char*>(&out[k]) + sizeof(float), &lo, sizeof(float));
+	}
+}
+
+static void from_pairs(double* buf, size_t n)
+{
+	for (size_t k = 0; k < n; k++)
+	{
+		float hi, lo;
+		std::memcpy(&hi, reinterpret_cast<const char*>(&buf[k]), sizeof(float));
+		std::memcpy(&lo, reinterpret_cast<const char*>(&buf[k]) + sizeof(float), sizeof(float));
+		buf[k] = (double)hi + (double)lo;
+	}
+}
+
 int upload_agents(Context* c, uint64_t A, const double* positions, const double* secretion, const double* saturation,
 				  const double* uptake, const double* net_export, const double* volumes, const uint8_t* is_active,
 				  const double* internalized, const double* fraction_released, bool compute_internalized)
@@ -729,6 +754,12 @@ int upload_agents(Context* c, uint64_t A, const double* positions, const double*
 										 c->stream));
 		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_vol.ptr, volumes, A * sizeof(double), cudaMemcpyHostToDevice, c->stream));
 		PCG_CUDA_TRY(cudaMemcpyAsync(c->a_active.ptr, is_active, A, cudaMemcpyHostToDevice, c->stream));
+		std::vector<double> pairs;
+		if (internalized && c->wsize == 4)
+		{
+			to_pairs(internalized, pairs, A * S);
+			internalized = pairs.data(); // lives until the wait below
+		}
 		if (internalized)
 			PCG_CUDA_TRY(cudaMemcpyAsync(c->a_internal.ptr, internalized, A * S * sizeof(double),
 										 cudaMemcpyHostToDevice, c->stream));
@@ -1079,6 +1110,12 @@ int pcg_set_internalized(pcg_context* c, const double* internalized)
 		return PCG_OK;
 	}
 	pcg::DeviceGuard g(c->device);
+	std::vector<double> pairs;
+	if (c->wsize == 4)
+	{
+		pcg::to_pairs(internalized, pairs, c->A * c->S);
+		internalized = pairs.data();
+	}
 	PCG_CUDA_TRY(cudaMemcpyAsync(c->a_internal.ptr, internalized, c->A * c->S * sizeof(double),
 								 cudaMemcpyHostToDevice, c->stream));
 	PCG_CUDA_TRY(stream_wait(c));
@@ -1338,7 +1375,11 @@ int pcg_get_internalized(pcg_context* c, double* host)
 	if (rc)
 		return rc;
 	if (c->A)
+	{
 		PCG_CUDA_TRY(cudaMemcpy(host, c->a_internal.ptr, c->A * c->S * sizeof(double), cudaMemcpyDeviceToHost));
+		if (c->wsize == 4)
+			pcg::from_pairs(host, c->A * c->S);
+	}
 	return PCG_OK;
 }
 

@@ -93,8 +93,9 @@ __global__ void cells_release_kernel(CellArgs a, uint64_t agent)
 	}
 	T* D = static_cast<T*>(a.field) + (idx[2] * a.n[1] + idx[1]) * a.pitch + idx[0] * a.S + s;
 	const uint64_t k = agent * a.S + s;
-	*D = (T)((double)*D + a.internal[k] * a.frac[k] / a.Vv);
-	a.internal[k] = 0.0;
+	const double I = a.pairs ? pair_value(a.internal[k]) : a.internal[k];
+	*D = (T)((double)*D + I * a.frac[k] / a.Vv);
+	a.internal[k] = 0.0; // zero bits: a zero pair too
 }
 
 } // namespace
@@ -143,6 +144,7 @@ CellArgs make_cell_args(const Context* c)
 	a.internalized = c->compute_internalized ? 1 : 0;
 	a.vec = rows_vectorizable(a, c->wsize);
 	a.terms = 1;
+	a.pairs = c->wsize == 4 ? 1 : 0; // FP32 contexts store internalized amounts as float pairs
 	return a;
 }
 
@@ -248,6 +250,7 @@ int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream)
 	a.internalized = b.internalized;
 	a.vec = rows_vectorizable(a, sizeof(float));
 	a.terms = 1;
+	a.pairs = 0; // the caller's FP64 amounts
 	const uint64_t V = b.n[0] * b.n[1] * b.n[2];
 	const unsigned block = 256;
 	const unsigned grid = (unsigned)((b.A + block - 1) / block);

@@ -51,6 +51,7 @@ struct CellArgs
 	void* field;
 	int internalized;
 	int vec;   // rows of S values start on 16-byte boundaries and S is a multiple of 16 / sizeof(T)
+	int pairs; // internalized amounts stored as float pairs (FP32 contexts; see pair_add)
 	int terms; // recompute the agent terms (their rates or volumes changed), not only positions
 };
 
@@ -217,18 +218,55 @@ __device__ __forceinline__ void list_shared(const CellArgs& a, uint64_t i, bool 
 // Change of an internalized amount.  The FP64 build evaluates the reference's
 // expressions in FP64 in its order: fused Vv (D - D') (cell_solver.cpp:166-185),
 // after a conflict -Vv (num - D' den + fac) (cell_solver.cpp:132-143).  The FP32
-// build evaluates them in FP32 (the product inside one fma) and only the
-// accumulation into the FP64 amount in FP64: double-precision arithmetic runs at a
-// small fraction of the single-precision rate on this GPU.
+// build evaluates them in FP32 (the product inside one fma; *_inc): double-
+// precision arithmetic runs at a small fraction of the single-precision rate on
+// this GPU.
 __device__ __forceinline__ double fused_delta(double Vv, double D, double Dn) { return Vv * (D - Dn); }
-__device__ __forceinline__ double fused_delta(double Vv, float D, float Dn) { return (double)((float)Vv * (D - Dn)); }
 __device__ __forceinline__ double conflict_delta(double Vv, double n, double Dn, double d, double f)
 {
 	return -(Vv * (n - Dn * d + f));
 }
-__device__ __forceinline__ double conflict_delta(double Vv, float n, float Dn, float d, float f)
+__device__ __forceinline__ float fused_inc(double Vv, float D, float Dn) { return (float)Vv * (D - Dn); }
+__device__ __forceinline__ float conflict_inc(double Vv, float n, float Dn, float d, float f)
 {
-	return (double)(-(float)Vv * (fmaf(-Dn, d, n) + f));
+	return -(float)Vv * (fmaf(-Dn, d, n) + f);
+}
+
+// FP32 contexts store each internalized amount as an unevaluated pair of floats
+// hi + lo (hi first in memory, the same 8 bytes as a double; about 48 significant
+// bits) and accumulate the FP32 increments with error-free transformations
+// (Knuth's TwoSum), so the per-step update needs no FP64 instruction; the host
+// converts to and from doubles at the API.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+	s = __fadd_rn(a, b);
+	const float bb = __fsub_rn(s, a);
+	e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ double pair_add(double stored, float x)
+{
+	const unsigned long long bits = (unsigned long long)__double_as_longlong(stored);
+	const float hi = __uint_as_float((unsigned)bits), lo = __uint_as_float((unsigned)(bits >> 32));
+	float s, e, h2, l2;
+	two_sum(hi, x, s, e);
+	two_sum(s, __fadd_rn(lo, e), h2, l2);
+	return __longlong_as_double(
+		(long long)(((unsigned long long)__float_as_uint(l2) << 32) | (unsigned long long)__float_as_uint(h2)));
+}
+
+__device__ __forceinline__ double pair_value(double stored)
+{
+	const unsigned long long bits = (unsigned long long)__double_as_longlong(stored);
+	return (double)__uint_as_float((unsigned)bits) + (double)__uint_as_float((unsigned)(bits >> 32));
+}
+
+// Adds the increment x to a stored amount: FP64 build in FP64; FP32 build into a
+// float pair, or (caller-owned FP64 amounts) into the double.
+__device__ __forceinline__ double accumulate(double stored, double x, int) { return stored + x; }
+__device__ __forceinline__ double accumulate(double stored, float x, int pairs)
+{
+	return pairs ? pair_add(stored, x) : stored + (double)x;
 }
 
 // Accesses to values s0 .. s0 + kSubBatch - 1 (those below S) of an agent's row.
@@ -334,10 +372,20 @@ __device__ __forceinline__ void agent_apply(const CellArgs& a, uint64_t i)
 			if (s0 + q < S)
 			{
 				nx[q] = (dv[q] + n_[q]) / (alone ? d_[q] + T(1) : d_[q]) + f_[q];
-				if (fused)
-					iv[q] += fused_delta(a.Vv, dv[q], nx[q]);
-				else if (track)
-					iv[q] += conflict_delta(a.Vv, n_[q], nx[q], d_[q], f_[q]);
+				if constexpr (sizeof(T) == 4)
+				{
+					if (fused)
+						iv[q] = accumulate(iv[q], fused_inc(a.Vv, dv[q], nx[q]), a.pairs);
+					else if (track)
+						iv[q] = accumulate(iv[q], conflict_inc(a.Vv, n_[q], nx[q], d_[q], f_[q]), a.pairs);
+				}
+				else
+				{
+					if (fused)
+						iv[q] += fused_delta(a.Vv, dv[q], nx[q]);
+					else if (track)
+						iv[q] += conflict_delta(a.Vv, n_[q], nx[q], d_[q], f_[q]);
+				}
 			}
 		row_store(D, s0, S, vec, nx);
 		if (track)
@@ -369,7 +417,12 @@ __device__ __forceinline__ void agent_internalize(const CellArgs& a, uint64_t i)
 #pragma unroll
 		for (int q = 0; q < kSubBatch; q++)
 			if (s0 + q < S)
-				iv[q] += conflict_delta(a.Vv, n_[q], dv[q], d_[q], f_[q]);
+			{
+				if constexpr (sizeof(T) == 4)
+					iv[q] = accumulate(iv[q], conflict_inc(a.Vv, n_[q], dv[q], d_[q], f_[q]), a.pairs);
+				else
+					iv[q] += conflict_delta(a.Vv, n_[q], dv[q], d_[q], f_[q]);
+			}
 		row_store(I, s0, S, vec, iv);
 	}
 }

@@ -20,9 +20,9 @@ pytestmark = pytest.mark.gpu
 SEEDS = list(range(40))
 
 
-def run_both(pcg, oracle_mod, p, precision, steps=(1, 2, 1)):
+def run_both(pcg, oracle_mod, p, precision, steps=(1, 2, 1), threads=2):
     g = W.apply(pcg.Solver(precision), p)
-    o = W.apply(oracle_mod.OracleSolver(threads=2), p)
+    o = W.apply(oracle_mod.OracleSolver(threads=threads), p)
     rng = np.random.default_rng(1000 + zlib.crc32(p["name"].encode()) % 1000)
     snaps = []
     for k, n in enumerate(steps):
