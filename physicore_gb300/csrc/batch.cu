@@ -62,6 +62,8 @@ constexpr uint32_t kMaxChunks = 64;        // y/z boxes per line (TMA operations
 constexpr uint64_t kClearChunk = 4096;     // voxels of the ballot counts cleared per warp item
 constexpr uint64_t kXSmemDefault = 32768;  // default shared-memory budget of an x tile
 constexpr double kTuneShare = 0.01;        // buckets below this share of an axis keep the defaults
+constexpr uint64_t kGroupBytes = 16 * 1024; // y/z: tiles of a domain taken together up to this many bytes
+constexpr uint32_t kMaxGroup = 8;
 
 struct BatchDomain
 {
@@ -74,6 +76,7 @@ struct BatchDomain
 	uint64_t x_smem_pitch;
 	uint32_t box_rows[3], boxes[3];
 	uint64_t yz_xblocks;       // y/z: tiles across a row (32 elements each)
+	uint32_t yz_group[3];      // y/z: consecutive tiles per work unit (short lines share a CTA's buffer)
 	const void* coef[3];
 	uint64_t coef_len[3];
 	uint64_t coef_comp_off[3]; // compressed tables (elements into coef)
@@ -368,54 +371,75 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 			continue;
 		}
 		const BatchDomain& D = b.doms[di];
-		const uint64_t lt = t - __ldg(b.list.base + k);
-		const int x0 = (int)((lt % D.yz_xblocks) * kLanes);
-		const int o = (int)(lt / D.yz_xblocks);
+		// a unit is `group` consecutive tiles of the domain (short lines: several
+		// tiles share the buffer, so one ticket, lookup and wait serve them all)
+		const uint32_t group = D.yz_group[AXIS];
+		const uint64_t tiles = D.yz_xblocks * (AXIS == 1 ? D.n[2] : D.n[1]);
+		const uint64_t lt0 = (t - __ldg(b.list.base + k)) * group;
+		const uint32_t gcount = (uint32_t)min((uint64_t)group, tiles - lt0);
 		const uint32_t R = D.box_rows[AXIS], nc = D.boxes[AXIS], n = D.n[AXIS], S = D.S;
-		const uint32_t chunk_elems = R * kLanes;
+		const uint32_t chunk_elems = R * kLanes, tile_elems = nc * chunk_elems;
 		const CUtensorMap* map = b.tmaps + 2 * di + (AXIS - 1);
 		if (lane == 0)
 		{
 			if (di != prev)
 				fence_tensormap_acquire(map);
-			dev::mbar_arrive_expect_tx(full, nc * chunk_elems * (uint32_t)sizeof(T));
-			for (uint32_t c = 0; c < nc; c++)
+			dev::mbar_arrive_expect_tx(full, gcount * tile_elems * (uint32_t)sizeof(T));
+			for (uint32_t j = 0; j < gcount; j++)
 			{
-				if (AXIS == 1)
-					dev::tma_load_3d(base + c * chunk_elems, map, x0, (int)(c * R), o, full);
-				else
-					dev::tma_load_3d(base + c * chunk_elems, map, x0, o, (int)(c * R), full);
+				const int x0 = (int)(((lt0 + j) % D.yz_xblocks) * kLanes), o = (int)((lt0 + j) / D.yz_xblocks);
+				for (uint32_t c = 0; c < nc; c++)
+				{
+					T* dst = base + j * tile_elems + c * chunk_elems;
+					if (AXIS == 1)
+						dev::tma_load_3d(dst, map, x0, (int)(c * R), o, full);
+					else
+						dev::tma_load_3d(dst, map, x0, o, (int)(c * R), full);
+				}
 			}
 		}
 		prev = di;
-		// coefficient loads overlap the tile's arrival
-		const uint32_t s = (uint64_t)(x0 + lane) < D.row_len ? (uint32_t)((x0 + lane) % S) : 0;
-		const LineCoef<T> L =
-			line_coef<T>(static_cast<const T*>(D.coef[AXIS]) + D.coef_comp_off[AXIS], S, D.coef_head[AXIS], n, s);
+		const T* comp = static_cast<const T*>(D.coef[AXIS]) + D.coef_comp_off[AXIS];
+		// the first tile's coefficient loads overlap the group's arrival
+		int x0 = (int)((lt0 % D.yz_xblocks) * kLanes), o = (int)(lt0 / D.yz_xblocks);
+		LineCoef<T> L = line_coef<T>(comp, S, D.coef_head[AXIS], n,
+									 (uint64_t)(x0 + lane) < D.row_len ? (uint32_t)((x0 + lane) % S) : 0);
 		ok = __all_sync(0xffffffffu, dev::mbar_wait(full, phase));
 		if (!ok)
 		{
 			bad = di;
 			break;
 		}
+		for (uint32_t j = 0; j < gcount; j++)
 		{
-			solve_line<T, kLanes>(base + lane, n, 0, L);
+			if (j)
+			{
+				x0 = (int)(((lt0 + j) % D.yz_xblocks) * kLanes), o = (int)((lt0 + j) / D.yz_xblocks);
+				L = line_coef<T>(comp, S, D.coef_head[AXIS], n,
+								 (uint64_t)(x0 + lane) < D.row_len ? (uint32_t)((x0 + lane) % S) : 0);
+			}
+			solve_line<T, kLanes>(base + j * tile_elems + lane, n, 0, L);
 			// the last sweep of the domain writes its boundary faces (the batch's
 			// Dirichlet launch then covers interior nodes and 1-D domains only)
 			if (D.dims == AXIS + 1)
-				fielddev::faces_on_column<T, AXIS>(D.faces, base + lane, n, kLanes, (uint64_t)x0 + lane,
-												   (uint64_t)o);
+				fielddev::faces_on_column<T, AXIS>(D.faces, base + j * tile_elems + lane, n, kLanes,
+												   (uint64_t)x0 + lane, (uint64_t)o);
 		}
 		dev::fence_proxy_async_smem();
 		__syncwarp();
 		if (lane == 0)
 		{
-			for (uint32_t c = 0; c < nc; c++)
+			for (uint32_t j = 0; j < gcount; j++)
 			{
-				if (AXIS == 1)
-					dev::tma_store_3d(map, x0, (int)(c * R), o, base + c * chunk_elems);
-				else
-					dev::tma_store_3d(map, x0, o, (int)(c * R), base + c * chunk_elems);
+				const int xs = (int)(((lt0 + j) % D.yz_xblocks) * kLanes), os = (int)((lt0 + j) / D.yz_xblocks);
+				for (uint32_t c = 0; c < nc; c++)
+				{
+					T* src = base + j * tile_elems + c * chunk_elems;
+					if (AXIS == 1)
+						dev::tma_store_3d(map, xs, (int)(c * R), os, src);
+					else
+						dev::tma_store_3d(map, xs, os, (int)(c * R), src);
+				}
 			}
 			dev::bulk_commit();
 			dev::bulk_wait_read();
@@ -852,6 +876,8 @@ BatchDomain describe_domain(pcg_batch* b, size_t d)
 	{
 		D.box_rows[a] = b->cfg[a][d].rows;
 		D.boxes[a] = (uint32_t)((c->n[a] + D.box_rows[a] - 1) / D.box_rows[a]);
+		const uint64_t tile_bytes = (uint64_t)D.boxes[a] * D.box_rows[a] * kLanes * c->wsize;
+		D.yz_group[a] = (uint32_t)std::min<uint64_t>(kMaxGroup, std::max<uint64_t>(1, kGroupBytes / tile_bytes));
 	}
 	D.yz_xblocks = (c->row_len + kLanes - 1) / kLanes;
 	for (int a = 0; a < c->dims; a++)
@@ -895,11 +921,13 @@ void list_units(pcg_batch* b, int id, size_t d, uint64_t& units, double& cost)
 		break;
 	case L_Y:
 		if (c->dims >= 2)
-			units = D.yz_xblocks * c->n[2], cost = (double)c->n[1];
+			units = (D.yz_xblocks * c->n[2] + D.yz_group[1] - 1) / D.yz_group[1],
+			cost = (double)c->n[1] * D.yz_group[1];
 		break;
 	case L_Z:
 		if (c->dims >= 3)
-			units = D.yz_xblocks * c->n[1], cost = (double)c->n[2];
+			units = (D.yz_xblocks * c->n[1] + D.yz_group[2] - 1) / D.yz_group[2],
+			cost = (double)c->n[2] * D.yz_group[2];
 		break;
 	case L_FACES: units = (D.faces.face_mask && c->dims == 1) ? D.faces.total * c->S : 0; break; // else fused
 	case L_INTERIOR: units = c->K * c->S; break;
@@ -1046,7 +1074,8 @@ uint64_t sweep_smem(pcg_batch* b, int axis, const std::vector<size_t>& subset)
 		if (axis == 0)
 			best = std::max<uint64_t>(best, 16 + (uint64_t)D.x_rows * D.x_smem_pitch * sizeof(T));
 		else
-			best = std::max<uint64_t>(best, (uint64_t)D.boxes[axis] * D.box_rows[axis] * kLanes * sizeof(T));
+			best = std::max<uint64_t>(best, (uint64_t)D.yz_group[axis] * D.boxes[axis] * D.box_rows[axis] * kLanes *
+												sizeof(T));
 	}
 	if (axis > 0)
 		best += 128; // the tile's mbarrier
