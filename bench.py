@@ -59,6 +59,22 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(x, world, device="cuda"):
+    """The largest of every rank's x (the slowest replica sets the job's time)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, world, seconds):
+    """Whole-job throughput of `world` replicas that each processed units_per_rank
+    units, timed by the slowest (weak scaling: the per-GPU work is fixed)."""
+    return units_per_rank * world / seconds
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -223,11 +239,8 @@ def run_gb300(args, w):
     launches = s.launch_count() - launches0
     stats = s.kernel_stats()
     s.set_kernel_timing(False)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = vss_step * args.steps * world / (ms / 1e3)
+    ms = max_over_ranks(ms, world)
+    value = job_rate(vss_step * args.steps, world, ms / 1e3)
 
     # roofline of the dominant kernel (largest share of device time)
     peak, peak_src = measured_peaks()
@@ -270,12 +283,8 @@ def run_gb300(args, w):
     for k in range(e2e_steps):
         e2e_step(k)
     s.wait_field(pending.pop(0))  # every step's field is in host memory
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": vss_step * e2e_steps * world / e2e_s, "unit": UNIT,
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = {"value": job_rate(vss_step * e2e_steps, world, e2e_s), "unit": UNIT,
            "h2d_bytes_per_step": int(pos_np.nbytes + act_np.nbytes),
            "d2h_bytes_per_step": int(field_np.nbytes), "steps": e2e_steps,
            "path": "pcg_update_agents(pinned) -> pcg_recompute_positional_data -> pcg_solve(1) -> "

@@ -1,0 +1,61 @@
+"""The multi-GPU path of bench.py on the CPU: two replicas as gloo ranks (no GPU).
+Every rank must see the slowest rank's time, the job rate must count every
+rank's units over that time, and the reference arm must run on rank 0 only."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.distributed as dist  # noqa: E402
+import torch.multiprocessing as mp  # noqa: E402
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    sys.path.insert(0, ROOT)
+    import bench
+    seconds = [2.0, 3.5][rank]  # rank 1 is the slow replica
+    slowest = bench.max_over_ranks(seconds, world, device="cpu")
+    out[rank] = (slowest, bench.job_rate(1000.0, world, slowest))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_max_over_ranks_and_job_rate_gloo():
+    port = _free_port()
+    with mp.Manager() as m:
+        out = m.dict()
+        mp.spawn(_worker, args=(2, port, out), nprocs=2, join=True)
+        got = dict(out)
+    for rank in (0, 1):
+        slowest, rate = got[rank]
+        assert slowest == 3.5
+        assert rate == pytest.approx(1000.0 * 2 / 3.5)
+
+
+def test_single_rank_needs_no_process_group():
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.max_over_ranks(1.25, 1) == 1.25
+    assert bench.job_rate(10.0, 1, 2.0) == 5.0
+
+
+def test_reference_arm_runs_on_rank_zero_only():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1"],
+                       capture_output=True, text=True, timeout=120, env=env, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip() == "", "ranks other than 0 print nothing"
