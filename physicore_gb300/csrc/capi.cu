@@ -803,6 +803,28 @@ uint64_t estimate_device_bytes(const Context* c)
 	return b;
 }
 
+int readback_ready(Context* c, uint64_t ticket, bool* done)
+{
+	if (ticket >= c->rb_issued)
+		return fail(PCG_ERR_INVALID, "no readback with this ticket was started");
+	DeviceGuard g(c->device);
+	const int j = (int)(ticket % 2);
+	*done = true;
+	if (!c->rb_pending[j])
+		return PCG_OK;
+	// the slot's event is this readback's or a later one's on the same copy stream
+	const cudaError_t e = cudaEventQuery(c->rb_done[j]);
+	if (e == cudaErrorNotReady)
+	{
+		*done = false;
+		return PCG_OK;
+	}
+	if (e != cudaSuccess)
+		return fail(PCG_ERR_CUDA, std::string("readback: ") + cudaGetErrorString(e));
+	c->rb_pending[j] = false;
+	return PCG_OK;
+}
+
 } // namespace pcg
 
 using pcg::Context;

@@ -148,6 +148,9 @@ uint32_t* pinned_words_get();
 void pinned_words_put(uint32_t* w);
 // Host wait for the context's stream, asleep rather than spinning (capi.cu).
 cudaError_t stream_wait(Context* c);
+// Whether the field readback `ticket` of pcg_get_field_async is in host memory,
+// without waiting (capi.cu).
+int readback_ready(Context* c, uint64_t ticket, bool* done);
 void dfree(DeviceBuffer& b);
 
 struct KernelStat

@@ -105,9 +105,19 @@ struct GpuBackend
 			err = pcg_last_error();
 		return rc;
 	}
-	int readback(const serve::Request& r)
+	// The finished request left the batch, so its field no longer changes: the
+	// conversion and the copy run on its own streams while the next steps run.
+	int readback_begin(serve::Request& r)
 	{
-		const int rc = pcg_get_field(static_cast<pcg_context*>(r.ctx), r.out, r.out_layout, r.out_dtype);
+		const int rc =
+			pcg_get_field_async(static_cast<pcg_context*>(r.ctx), r.out, r.out_layout, r.out_dtype, &r.out_ticket);
+		if (rc)
+			err = pcg_last_error();
+		return rc;
+	}
+	int readback_poll(const serve::Request& r, bool* done)
+	{
+		const int rc = readback_ready(static_cast<pcg_context*>(r.ctx), r.out_ticket, done);
 		if (rc)
 			err = pcg_last_error();
 		return rc;

@@ -12,7 +12,8 @@
 //                                          start k steps, simulation i taking part in the first budgets[i]
 //   int step_end();                        wait for them
 //   bool busy();                           the started steps are still running
-//   int readback(const Request&);          copy a finished request's field to its host buffer
+//   int readback_begin(Request&);          start copying a finished request's field to its buffer
+//   int readback_poll(const Request&, bool* done)  whether that copy has completed (no wait)
 //   std::string last_error();
 // so the same code runs against the GPU (server.cu) and against a fake backend in
 // the CPU tests (admission refusals, allocation failures, malformed requests,
@@ -27,9 +28,10 @@
 // simulations are stepping, admission stops once the steps are done (after at
 // least one admission), so the device is not left idle behind host-side uploads;
 // with nothing active it admits everything that fits.  A request submitted with
-// a host buffer has its field copied there by the worker right after the tick in
-// which it finished (the device has no other work of the server then), before it
-// is reported done; a failed copy reports it failed.
+// a host buffer has its field copy started right after the tick in which it
+// finished (the copy overlaps the following ticks: the request left the batch),
+// and it is reported done once the copy has completed; a failed copy reports it
+// failed.
 // A request that does not fit now waits (memory is freed as active requests
 // finish and as callers destroy returned ones); it is refused only when it could
 // never fit (its bytes plus the reserve exceed total_bytes) or when its allocation
@@ -65,6 +67,7 @@ struct Request
 	uint32_t attempts = 0;   // admissions that failed for lack of memory
 	void* out = nullptr;     // host buffer for the field when done (null: the caller reads it)
 	int out_layout = 0, out_dtype = 0;
+	uint64_t out_ticket = 0; // the backend's handle of the copy in flight
 	Status status = Status::Done;
 	int code = 0;
 	std::string error;
@@ -146,6 +149,7 @@ public:
 	// One scheduling step; returns false when there is nothing to do.
 	bool tick(double now)
 	{
+		const bool copied = poll_readbacks(now);
 		const size_t stepped = active_.size();
 		std::vector<uint64_t> budgets;
 		if (stepped)
@@ -183,7 +187,7 @@ public:
 		const size_t admitted = admit(now, stepped > 0); // overlaps the steps just started
 		stats_.admit_s += seconds_since(t0);
 		if (!stepped)
-			return admitted > 0;
+			return admitted > 0 || copied;
 		t0 = clock::now();
 		const int rc = be_.step_end();
 		stats_.step_s += seconds_since(t0);
@@ -205,9 +209,11 @@ public:
 				{
 					stats_.active_bytes -= r.bytes;
 					dirty_ = true;
-					const int rb = r.out ? be_.readback(r) : 0;
+					const int rb = r.out ? be_.readback_begin(r) : 0;
 					if (rb)
 						finish(r, Status::Failed, rb, be_.last_error(), now);
+					else if (r.out)
+						reading_.push_back(std::move(r));
 					else
 						finish(r, Status::Done, 0, "", now);
 					continue;
@@ -229,9 +235,12 @@ public:
 			out.push_back(r.ctx);
 		for (auto& r : finished_)
 			out.push_back(r.ctx);
+		for (auto& r : reading_)
+			out.push_back(r.ctx);
 		queue_.clear();
 		active_.clear();
 		finished_.clear();
+		reading_.clear();
 		stats_.active_bytes = 0;
 		dirty_ = true;
 		return out;
@@ -247,12 +256,36 @@ public:
 	// The active set changed since the last rebuild (the backend's batch refers to
 	// retired contexts until it is rebuilt or dropped).
 	bool dirty() const { return dirty_; }
-	bool idle() const { return queue_.empty() && active_.empty(); }
+	bool idle() const { return queue_.empty() && active_.empty() && reading_.empty(); }
 	size_t queued() const { return queue_.size(); }
 	size_t active() const { return active_.size(); }
 	const Stats& stats() const { return stats_; }
 
 private:
+	// Requests whose field copy has completed (or failed) are finished.
+	bool poll_readbacks(double now)
+	{
+		bool any = false;
+		std::vector<Request> still;
+		for (Request& r : reading_)
+		{
+			bool done = false;
+			const int rc = be_.readback_poll(r, &done);
+			if (rc)
+				finish(r, Status::Failed, rc, be_.last_error(), now);
+			else if (done)
+				finish(r, Status::Done, 0, "", now);
+			else
+			{
+				still.push_back(std::move(r));
+				continue;
+			}
+			any = true;
+		}
+		reading_.swap(still);
+		return any;
+	}
+
 	using clock = std::chrono::steady_clock;
 	static double seconds_since(clock::time_point t0)
 	{
@@ -336,6 +369,7 @@ private:
 	std::deque<Request> queue_;
 	std::vector<Request> active_;
 	std::vector<Request> finished_;
+	std::vector<Request> reading_; // done stepping, field copy in flight
 	Stats stats_;
 	bool dirty_ = false;
 };

@@ -83,16 +83,25 @@ struct FakeBackend
 		return 0;
 	}
 	int step_end() { return 0; }
-	std::vector<void*> read_back;    // contexts whose field was copied out, in order
-	bool fail_readback = false;
-	int readback(const Request& r)
+	std::vector<void*> read_back;    // contexts whose field copy started, in order
+	bool fail_readback = false;      // the copy fails when polled
+	int copy_polls = 1;              // polls before a copy has completed
+	std::map<void*, int> polls_left;
+	int readback_begin(Request& r)
+	{
+		read_back.push_back(r.ctx);
+		polls_left[r.ctx] = copy_polls;
+		r.out_ticket = read_back.size();
+		return 0;
+	}
+	int readback_poll(const Request& r, bool* done)
 	{
 		if (fail_readback)
 		{
 			err = "readback failed";
 			return 4;
 		}
-		read_back.push_back(r.ctx);
+		*done = --polls_left[r.ctx] <= 0;
 		return 0;
 	}
 	int busy_polls = 0; // busy() answers true this many times
@@ -302,19 +311,24 @@ void readback_before_done()
 	Request b = req(be, 2, 8, 10); // no buffer: the caller reads the field itself
 	Request c = req(be, 3, 4, 10);
 	c.out = buf;
+	be.copy_polls = 2;
 	s.submit(a, 0);
 	s.submit(b, 0);
 	s.tick(0);
-	s.tick(1); // 1 finishes: read back before it is reported
+	s.tick(1); // 1 finishes stepping: its copy starts and overlaps the next ticks
+	EXPECT(s.take_finished().empty() && be.read_back.size() == 1 && be.read_back[0] == ctx(1));
+	EXPECT(!s.idle());
+	s.tick(2); // first poll: 1 still copying; 2 (no buffer) finishes and is reported at once
 	auto f = s.take_finished();
+	EXPECT(f.size() == 1 && !f.empty() && f[0].tag == 2 && f[0].status == Status::Done);
+	s.tick(3); // second poll: 1's copy is done, reported only now
+	f = s.take_finished();
 	EXPECT(f.size() == 1 && !f.empty() && f[0].tag == 1 && f[0].status == Status::Done);
-	EXPECT(be.read_back.size() == 1 && !be.read_back.empty() && be.read_back[0] == ctx(1));
 	be.fail_readback = true;
-	s.submit(c, 1);
+	s.submit(c, 3);
 	auto done = run(s, be);
-	EXPECT(find(done, 2) && find(done, 2)->status == Status::Done);          // no readback asked
 	EXPECT(find(done, 3) && find(done, 3)->status == Status::Failed && find(done, 3)->error == "readback failed");
-	EXPECT(be.read_back.size() == 1);
+	EXPECT(be.read_back.size() == 2 && s.idle());
 }
 
 void queue_limit_and_zero_steps()
