@@ -149,6 +149,13 @@ void gb300_solver::transfer_to_host(microenvironment& m)
 		check(pcg_get_internalized(ctx_, m.agents->internalized_substrates.data()));
 }
 
+void gb300_solver::read_field_planar(real_t* out) const
+{
+	if (!ctx_)
+		throw std::runtime_error("gb300_solver: read before initialize");
+	check(pcg_get_field(ctx_, out, PCG_LAYOUT_PLANAR, PCG_DTYPE_F64));
+}
+
 void gb300_solver::reinitialize_dirichlet(microenvironment& m)
 {
 	initialize(m);

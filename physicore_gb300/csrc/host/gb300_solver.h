@@ -39,6 +39,10 @@ public:
 	// The underlying context (for batching several solvers with pcg_batch_create).
 	pcg_context* context() const { return ctx_; }
 
+	// The device field in planar order [s][z][y][x], FP64, one bulk copy (the
+	// image serializer's read; the host mirror is not involved).
+	void read_field_planar(real_t* out) const;
+
 	// Registers "gb300_solver" (FP64) and "gb300_solver_fp32".
 	static void attach_to_registry();
 
