@@ -255,6 +255,32 @@ def run_gb300(args, w):
                    "gbps": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] > 0 else None}
                for k, v in timed.items()}
 
+    # the per-step FP64 mass check on the same workload (off in the timed step above)
+    mc_steps = max(3, min(args.steps, 100))
+    s.set_mass_check(True)
+    s.solve(1)
+    s.synchronize()
+    s.set_mass_check(True)  # record from here on
+    s.set_kernel_timing(True)
+    s.reset_kernel_stats()
+    ev0.record(stream)
+    for _ in range(mc_steps):
+        s.solve(1)
+    ev1.record(stream)
+    ev1.synchronize()
+    mc_ms = ev0.elapsed_time(ev1) / mc_steps
+    mc_stats = s.kernel_stats().get("mass_check", {})
+    s.set_kernel_timing(False)
+    chk = s.get_mass_check()
+    s.set_mass_check(False)
+    mass_check = {"steps": chk["steps"], "ms_per_step": round(mc_ms, 4),
+                  "overhead": round(mc_ms / (ms / args.steps) - 1.0, 4),
+                  "worst_residual": float(chk["worst"].max()),
+                  "residual": "max over substrates and steps of |after*f - before|/|before|, f the product of "
+                              "the sweep matrices' column sums",
+                  "kernel_gbps": round(mc_stats["bytes"] / (mc_stats["ms"] / 1e3) / 1e9, 1)
+                  if mc_stats.get("ms") else None}
+
     # end to end through the C ABI with host buffers
     A = p["agents"]["volumes"].size
     pos_h = torch.empty((A, 3), dtype=torch.float64, pin_memory=True)
@@ -311,7 +337,7 @@ def run_gb300(args, w):
                               "frac": round(step_bytes / (ms / args.steps / 1e3) / 1e9 / peak, 4),
                               "algorithmic_bytes_per_step": step_bytes},
             "kernels": kernels, "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e,
-            "cpu_baseline": cpu}
+            "cpu_baseline": cpu, "mass_check": mass_check}
     if args.batch_domains > 0:
         line["batched"] = run_batched(args, local, ClockSampler)
     if args.serve_duration > 0:

@@ -179,6 +179,22 @@ int pcg_get_counts(pcg_context* ctx, uint32_t* host);
 int pcg_get_conflict(pcg_context* ctx, int* conflict);
 /* Total mass per substrate, summed on the device in FP64. */
 int pcg_mass(pcg_context* ctx, double* host);
+
+/* Per-step mass conservation check, off by default.  Each sweep matrix has
+ * column sums 1 + decay*dt/dims (diffusion_solver.cpp:29-86, the reference's
+ * Uniform tests rest on this; an axis of length 1 adds r = dt*D/h^2, its single
+ * diagonal entry having r subtracted once), so every step's sweeps must divide
+ * each substrate's total by f, the product of those sums over the axes, whatever
+ * Dirichlet, bulk and agents then add.  When enabled, every step that runs the diffusion
+ * phase sums the field in FP64 before the x sweep and after the last sweep (two
+ * extra passes over the field, and the boundary faces are then written by their
+ * own kernel) and keeps, per substrate, the worst |after*f - before| / |before|.
+ * Enabling resets the record; contexts stepped by a batch are not checked. */
+int pcg_set_mass_check(pcg_context* ctx, int enable);
+/* The last checked step's totals before and after its sweeps, the worst residual
+ * since the check was enabled (each [S], NULL to skip) and the steps checked. */
+int pcg_get_mass_check(pcg_context* ctx, double* mass_before, double* mass_after, double* worst_residual,
+					   uint64_t* steps_checked);
 int pcg_synchronize(pcg_context* ctx);
 
 /* ---- device-resident access (benchmarks, zero-copy integration) -------- */

@@ -69,6 +69,8 @@ SIGNATURES = {
     "pcg_get_counts": [_P, _P],
     "pcg_get_conflict": [_P, _P],
     "pcg_mass": [_P, _P],
+    "pcg_set_mass_check": [_P, ctypes.c_int],
+    "pcg_get_mass_check": [_P, _P, _P, _P, _P],
     "pcg_synchronize": [_P],
     "pcg_get_field_device": [_P, _P, _P, _P],
     "pcg_set_kernel_timing": [_P, _i32],
@@ -319,6 +321,19 @@ class Solver:
         out = np.empty(self.S)
         self._check(self._L.pcg_mass(self._h, _ptr(out)))
         return out
+
+    def set_mass_check(self, enable=True):
+        """Per-step FP64 check of the sweeps' mass identity (pcg_set_mass_check)."""
+        self._check(self._L.pcg_set_mass_check(self._h, int(bool(enable))))
+
+    def get_mass_check(self):
+        """dict(before, after, worst, steps): the last checked step's totals before
+        and after its sweeps, the worst relative residual, the steps checked."""
+        before, after, worst = np.empty(self.S), np.empty(self.S), np.empty(self.S)
+        steps = ctypes.c_uint64(0)
+        self._check(self._L.pcg_get_mass_check(self._h, _ptr(before), _ptr(after), _ptr(worst),
+                                               ctypes.byref(steps)))
+        return dict(before=before, after=after, worst=worst, steps=int(steps.value))
 
     # -- device access and measurement -------------------------------------
     def field_device(self):

@@ -32,7 +32,7 @@ const char* kernel_name(int id)
 	static const char* names[K_COUNT] = { "sweep_x",	  "sweep_y",		"sweep_z",	   "dirichlet_faces",
 										  "dirichlet_interior", "bulk", "cells_locate", "cells_ballot",
 										  "cells_reduce", "cells_apply", "cells_internalize", "cells_release",
-										  "mass",		  "layout", "cells_clear" };
+										  "mass",		  "layout", "cells_clear", "mass_check" };
 	return (id >= 0 && id < K_COUNT) ? names[id] : "?";
 }
 
@@ -520,15 +520,23 @@ static int run_phases(Context* c, uint32_t phases, bool recompute)
 	// with both phases in this call, the last sweep writes the boundary faces into
 	// its tiles before storing them (the reference's next step, dirichlet_solver.cpp:
 	// 59-83), which saves a pass of scattered writes
-	const bool fuse = (phases & PCG_PHASE_DIFFUSION) && (phases & PCG_PHASE_DIRICHLET) && faces_fusable(c);
+	// (not while the mass check reads the field between the sweeps and Dirichlet)
+	const bool check = c->mass_check && (phases & PCG_PHASE_DIFFUSION);
+	const bool fuse =
+		!check && (phases & PCG_PHASE_DIFFUSION) && (phases & PCG_PHASE_DIRICHLET) && faces_fusable(c);
 	if (phases & PCG_PHASE_DIFFUSION)
 	{
+		if (check && (rc = launch_mass_check(c, 0)))
+			return rc;
 		if ((rc = launch_sweep_x(c)))
 			return rc;
 		if (c->dims >= 2 && (rc = launch_sweep_yz(c, 1, fuse && c->dims == 2)))
 			return rc;
 		if (c->dims >= 3 && (rc = launch_sweep_yz(c, 2, fuse)))
 			return rc;
+		if (check && (rc = launch_mass_check(c, 1)))
+			return rc;
+		c->mass_checked_steps += check;
 	}
 	if ((phases & PCG_PHASE_DIRICHLET) && (rc = launch_dirichlet(c, fuse)))
 		return rc;
@@ -1445,6 +1453,76 @@ int pcg_mass(pcg_context* c, double* host)
 		return rc;
 	PCG_CUDA_TRY(cudaMemcpyAsync(host, c->mass.ptr, c->S * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
 	return pcg::check_device(c);
+}
+
+// Buffers of the mass check and its per-substrate sweep factors: each sweep
+// matrix has column sums 1 + decay*dt/dims, plus r = dt*D/h^2 on an axis of
+// length 1, whose single diagonal entry has r subtracted once rather than twice
+// (diffusion_solver.cpp:29-86), so the sweeps divide every substrate's total by
+// the product of those sums over the mesh's axes.
+static int prepare_mass_check(Context* c)
+{
+	int rc;
+	if ((rc = pcg::dalloc(c, c->mc_cols, 2 * c->row_len * sizeof(double))) ||
+		(rc = pcg::dalloc(c, c->mc_out, 4 * c->S * sizeof(double))))
+		return rc;
+	std::vector<double> h(4 * c->S, 0.0);
+	for (uint64_t s = 0; s < c->S; s++)
+	{
+		double p = 1.0;
+		for (int a = 0; a < c->dims; a++)
+		{
+			const double h = (double)c->voxel[a];
+			const double r = c->n[a] == 1 ? c->dt * c->D[s] / (h * h) : 0.0;
+			p *= 1.0 + c->decay[s] * c->dt / (double)c->dims + r;
+		}
+		h[3 * c->S + s] = p;
+	}
+	PCG_CUDA_TRY(pcg::stream_wait(c));
+	PCG_CUDA_TRY(cudaMemcpyAsync(c->mc_out.ptr, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+	PCG_CUDA_TRY(pcg::stream_wait(c));
+	c->mass_checked_steps = 0;
+	return PCG_OK;
+}
+
+int pcg_set_mass_check(pcg_context* c, int enable)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::do_initialize(c);
+	if (rc)
+		return rc;
+	if (enable && (rc = prepare_mass_check(c)))
+		return rc;
+	c->mass_check = enable != 0;
+	return PCG_OK;
+}
+
+int pcg_get_mass_check(pcg_context* c, double* mass_before, double* mass_after, double* worst_residual,
+					   uint64_t* steps_checked)
+{
+	CTX_CHECK(c);
+	pcg::DeviceGuard g(c->device);
+	if (!c->mc_out.ptr)
+		return fail(PCG_ERR_INVALID, "the mass check was never enabled");
+	std::vector<double> h(3 * c->S);
+	PCG_CUDA_TRY(pcg::stream_wait(c));
+	PCG_CUDA_TRY(cudaMemcpyAsync(h.data(), c->mc_out.ptr, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+	const int rc = pcg::check_device(c);
+	if (rc)
+		return rc;
+	for (uint64_t s = 0; s < c->S; s++)
+	{
+		if (mass_before)
+			mass_before[s] = h[s];
+		if (mass_after)
+			mass_after[s] = h[c->S + s];
+		if (worst_residual)
+			worst_residual[s] = h[2 * c->S + s];
+	}
+	if (steps_checked)
+		*steps_checked = c->mass_checked_steps;
+	return PCG_OK;
 }
 
 int pcg_synchronize(pcg_context* c)

@@ -62,6 +62,7 @@ enum KernelId : int
 	K_MASS,
 	K_LAYOUT,
 	K_CELLS_CLEAR,
+	K_MASS_CHECK,
 	K_COUNT
 };
 
@@ -217,6 +218,13 @@ struct Context
 	DeviceBuffer tickets;  // uint32 [4]: tile counters of the persistent sweeps
 	DeviceBuffer flags;    // uint32 [4]: [0] ballot conflict, [1] agents in shared voxels
 	DeviceBuffer mass;     // double [S]
+	// per-step mass check (pcg_set_mass_check): column sums before and after the
+	// sweeps [2 * row_len], and [4 * S]: mass before, mass after, worst residual,
+	// (1 + decay*dt/dims)^dims
+	bool mass_check = false;
+	uint64_t mass_checked_steps = 0;
+	DeviceBuffer mc_cols;
+	DeviceBuffer mc_out;
 	DeviceBuffer staging;  // layout conversion
 	// asynchronous field readback: two staging buffers used in turn, copied to the
 	// host on a stream of their own; readback k uses slot k % 2
@@ -299,6 +307,9 @@ int launch_bulk(Context* c);
 int launch_cells(Context* c, bool recompute);
 int launch_release(Context* c, uint64_t agent);
 int launch_mass(Context* c, double* dev_out);
+// Column sums of the field into c->mc_cols (half 0: before the sweeps, 1: after);
+// after half 1, the per-substrate masses and the residual into c->mc_out.
+int launch_mass_check(Context* c, int half);
 int launch_to_host_layout(Context* c, void* dst, int layout, int dtype);
 int launch_from_host_layout(Context* c, const void* src, int layout, int dtype);
 int launch_fill_initial(Context* c); // from the initial values already in c->mass (as T)

@@ -1,0 +1,65 @@
+"""The per-step FP64 mass check (pcg_set_mass_check / pcg_get_mass_check): on
+random problems with Dirichlet faces and nodes, bulk and agents, every checked
+step's sweeps keep the identity after * f = before (f: the product of the sweep
+matrices' column sums; worst residual <= 1e-12 in the FP64 build, <= 1e-5 in
+FP32), the last step's
+totals equal the oracle's before and after its diffusion phase, and the field
+is the same with the check on as with it off (to the parity tolerance)."""
+import numpy as np
+import pytest
+
+from physicore_gb300 import workloads as W
+from test_gpu_golden import rel_err
+
+pytestmark = pytest.mark.gpu
+
+STEPS = 5
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("seed", range(12))
+def test_mass_check_matches_oracle(pcg, oracle_mod, seed, precision):
+    p = W.random_small(seed)
+    g = W.apply(pcg.Solver(precision), p)
+    g.set_mass_check(True)
+    g.solve(STEPS)
+    chk = g.get_mass_check()
+    tol = 1e-12 if precision == 1 else 1e-5
+    assert chk["steps"] == STEPS
+    assert np.all(chk["worst"] <= tol), chk["worst"]
+
+    o = W.apply(oracle_mod.OracleSolver(threads=2), p)
+    o.solve(STEPS - 1)
+    before = o.mass()
+    o.run_phases(oracle_mod.PHASE_DIFFUSION, False)
+    after = o.mass()
+    scale = np.maximum(np.abs(before), 1e-300)
+    assert np.all(np.abs(chk["before"] - before) <= tol * scale), (chk["before"], before)
+    assert np.all(np.abs(chk["after"] - after) <= tol * scale), (chk["after"], after)
+
+    # the field of an unchecked run (faces then come from their own kernel); not
+    # bit-equal in general: sums over agents sharing a voxel are atomic, in any order
+    h = W.apply(pcg.Solver(precision), p)
+    h.solve(STEPS)
+    assert rel_err(g.get_field(), h.get_field()) <= tol
+
+
+def test_mass_check_reset_and_off(pcg):
+    p = W.random_small(3)
+    g = W.apply(pcg.Solver(0), p)
+    g.set_mass_check(True)
+    g.solve(2)
+    assert g.get_mass_check()["steps"] == 2
+    g.set_mass_check(False)
+    g.solve(3)
+    assert g.get_mass_check()["steps"] == 2
+    g.set_mass_check(True)
+    assert g.get_mass_check()["steps"] == 0 and np.all(g.get_mass_check()["worst"] == 0)
+    g.solve(1)
+    assert g.get_mass_check()["steps"] == 1
+
+
+def test_mass_check_never_enabled(pcg):
+    g = W.apply(pcg.Solver(0), W.random_small(4))
+    with pytest.raises(pcg.PcgError):
+        g.get_mass_check()

@@ -57,3 +57,23 @@ def test_workload_shapes():
     q = W.large(n=16, S=3, agents=100, interior=20)
     assert q["field"].shape == (3, 16, 16, 16) and q["field"].dtype == np.float32
     assert q["interior"][0].shape[1] == 3
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_oracle_sweep_mass_identity_mixed_problems(oracle_mod, seed):
+    """The premise of the per-step mass check: whatever Dirichlet, bulk and agents
+    did before, the sweeps of one step divide every substrate's total by the
+    product over the axes of the matrix column sums, 1 + decay*dt/dims, plus
+    r = dt*D/h^2 on an axis of length 1 (its diagonal loses r once, not twice)."""
+    p = W.random_small(seed)
+    o = W.apply(oracle_mod.OracleSolver(threads=2), p)
+    o.solve(2)
+    before = o.mass()
+    o.run_phases(oracle_mod.PHASE_DIFFUSION, False)
+    after = o.mass()
+    decay, D = np.asarray(p["decay"], float), np.asarray(p["D"], float)
+    f = np.ones_like(decay)
+    for a in range(p["dims"]):
+        r = D * p["dt"] / float(p["voxel"][a]) ** 2 if o.grid[a] == 1 else 0.0
+        f = f * (1.0 + decay * p["dt"] / p["dims"] + r)
+    assert np.allclose(after * f, before, rtol=1e-12, atol=1e-300)
