@@ -534,7 +534,12 @@ def run_serve(args, local):
     lat_dev, lat_host, statuses, vss_done, agent_steps = [], [], {}, 0, 0
     t_first = t_last = None
     got = 0
+    profile, next_sample = [], 0.5  # [t, active, queued, cumulative vss] every half second
     while got < n and not err:
+        if time.perf_counter() - t_start >= next_sample:
+            sp = srv.stats()
+            profile.append([round(time.perf_counter() - t_start, 2), sp["active"], sp["queued"], sp["vss"]])
+            next_sample += 0.5
         for r in srv.poll(64, wait_ms=20):
             got += 1
             statuses[r["status"]] = statuses.get(r["status"], 0) + 1
@@ -596,9 +601,12 @@ def run_serve(args, local):
             "feeder_lag_s": {"p50": q(lag, 50), "max": float(lag.max()) if n else None},
             "result_buffers": {"pinned": int(n - pageable[0]), "pageable": int(pageable[0])},
             "server": {k: (round(st[k], 3) if isinstance(st[k], float) else st[k])
-                       for k in ("ticks", "rebuilds", "steps", "admitted", "refused", "failed", "rebuild_s", "step_s",
-                                 "admit_s")},
-            "steps_per_tick": args.serve_tick, "wall_s": round(wall, 2)}
+                       for k in ("ticks", "rebuilds", "prebuilds", "steps", "admitted", "refused", "failed",
+                                 "rebuild_s", "prebuild_s", "step_s", "admit_s")},
+            "steps_per_tick": args.serve_tick, "wall_s": round(wall, 2),
+            "profile": {"columns": ["t_s", "active", "queued", "vss_per_s_over_the_half_second"],
+                        "rows": [[t, a, q, (v - profile[k - 1][3]) / (t - profile[k - 1][0]) if k else v / t]
+                                 for k, (t, a, q, v) in enumerate(profile)]}}
 
 
 def run_dense(args, local):

@@ -243,6 +243,11 @@ int pcg_batch_synchronize(pcg_batch* batch);
 int pcg_batch_get_stream(pcg_batch* batch, void** stream);
 /* Replays the step from a CUDA graph (default 1) or launches it directly. */
 int pcg_batch_set_graph(pcg_batch* batch, int enable);
+/* Builds the descriptors and captures both step graphs (with and without the
+ * ballot-rebuild kernels) now, without running anything, so that the first solve
+ * launches at once.  It touches only the batch's own buffers and stream: a batch
+ * can be prepared while another batch over the same contexts is stepping them. */
+int pcg_batch_prepare(pcg_batch* batch);
 /* Times candidate line mappings and tile shapes of each sweep axis for each size
  * bucket (line length, substrates) present in the batch and keeps the fastest;
  * results are cached for the process.  Field contents are restored afterwards. */
@@ -323,6 +328,11 @@ typedef struct pcg_server_stats
 	/* worker time regrouping the active set into a batch, starting and waiting
 	 * for steps, and admitting requests */
 	double rebuild_s, step_s, admit_s;
+	/* next-tick batches built (and their graphs captured) while a tick's steps
+	 * ran, and the worker time spent on them; a tick whose set matches its
+	 * prepared batch starts without a rebuild */
+	uint64_t prebuilds;
+	double prebuild_s;
 } pcg_server_stats;
 
 int pcg_server_create(pcg_server** out, int precision, int device, const pcg_server_options* options);

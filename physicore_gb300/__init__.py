@@ -84,6 +84,7 @@ SIGNATURES = {
     "pcg_batch_synchronize": [_P],
     "pcg_batch_get_stream": [_P, _P],
     "pcg_batch_set_graph": [_P, _i32],
+    "pcg_batch_prepare": [_P],
     "pcg_batch_autotune": [_P],
     "pcg_batch_force_config": [_P, _i32, _i32, _u32],
     "pcg_batch_describe": [_P, _P, _u64, _P],
@@ -419,6 +420,10 @@ class Batch:
     def set_graph(self, enable):
         self._check(self._L.pcg_batch_set_graph(self._h, int(bool(enable))))
 
+    def prepare(self):
+        """Descriptors built and step graphs captured now (pcg_batch_prepare)."""
+        self._check(self._L.pcg_batch_prepare(self._h))
+
     def autotune(self):
         self._check(self._L.pcg_batch_autotune(self._h))
 
@@ -470,7 +475,8 @@ class ServerStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "admitted", "completed", "cancelled", "refused",
                                                "failed", "ticks", "rebuilds", "steps", "vss", "active_bytes",
                                                "queued", "active", "in_flight")] + [
-        (n, ctypes.c_double) for n in ("uptime_s", "rebuild_s", "step_s", "admit_s")]
+        (n, ctypes.c_double) for n in ("uptime_s", "rebuild_s", "step_s", "admit_s")] + [
+        ("prebuilds", ctypes.c_uint64), ("prebuild_s", ctypes.c_double)]
 
 
 REQUEST_DONE, REQUEST_CANCELLED, REQUEST_REFUSED, REQUEST_FAILED = 0, 1, 2, 3

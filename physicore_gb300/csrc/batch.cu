@@ -62,7 +62,8 @@ constexpr uint32_t kMaxChunks = 64;        // y/z boxes per line (TMA operations
 constexpr uint64_t kClearChunk = 4096;     // voxels of the ballot counts cleared per warp item
 constexpr uint64_t kXSmemDefault = 32768;  // default shared-memory budget of an x tile
 constexpr double kTuneShare = 0.01;        // buckets below this share of an axis keep the defaults
-constexpr uint64_t kGroupBytes = 16 * 1024; // y/z: tiles of a domain taken together up to this many bytes
+constexpr uint64_t kGroupBytes = 16 * 1024; // y/z: tiles of a domain taken together up to this many bytes,
+											 // or up to the batch's largest tile when that is larger
 constexpr uint32_t kMaxGroup = 8;
 
 struct BatchDomain
@@ -1039,6 +1040,24 @@ int upload_domains(pcg_batch* b)
 	const size_t N = b->ctx.size();
 	for (size_t d = 0; d < N; d++)
 		b->h_doms[d] = describe_domain(b, d);
+	// y/z: every CTA's buffer holds the batch's largest tile, so a short-line
+	// domain groups its tiles up to that size (at least kGroupBytes) instead of
+	// leaving most of the buffer empty
+	for (int a = 1; a < 3; a++)
+	{
+		auto tile_bytes = [&](size_t d) {
+			const BatchDomain& D = b->h_doms[d];
+			return (uint64_t)D.boxes[a] * D.box_rows[a] * kLanes * b->wsize;
+		};
+		uint64_t cap = kGroupBytes;
+		for (size_t d = 0; d < N; d++)
+			if (a < C(b, d)->dims)
+				cap = std::max(cap, tile_bytes(d));
+		for (size_t d = 0; d < N; d++)
+			if (a < C(b, d)->dims)
+				b->h_doms[d].yz_group[a] =
+					(uint32_t)std::min<uint64_t>(kMaxGroup, std::max<uint64_t>(1, cap / tile_bytes(d)));
+	}
 	int rc;
 	if ((rc = balloc(b->d_doms, N * sizeof(BatchDomain), b->stream, b->device)) ||
 		(rc = balloc(b->d_tmaps, N * 2 * sizeof(CUtensorMap), b->stream, b->device)))
@@ -1913,6 +1932,21 @@ int pcg_batch_solve_budgets(pcg_batch* b, uint64_t iterations, const uint64_t* b
 		if (!budgets || budgets[d] > 0)
 			static_cast<Context*>(b->ctx[d])->recompute_cells = false;
 	return pcg::sync_out(b);
+}
+
+int pcg_batch_prepare(pcg_batch* b)
+{
+	BATCH_CHECK(b);
+	pcg::DeviceGuard g(b->device);
+	int rc;
+	if ((rc = pcg::refresh(b)))
+		return rc;
+	if (!b->use_graph)
+		return PCG_OK;
+	for (int rebuilds = 0; rebuilds < 2; rebuilds++)
+		if (!b->exec[rebuilds] && (rc = pcg::capture(b, rebuilds)))
+			return rc;
+	return PCG_OK;
 }
 
 int pcg_batch_synchronize(pcg_batch* b)

@@ -69,8 +69,47 @@ struct GpuBackend
 			pcg_batch_destroy(batch);
 		batch = nullptr;
 	}
+	// The next tick's batch, built and captured while the current tick runs.
+	pcg_batch* next = nullptr;
+	std::vector<void*> next_ctxs;
+	void drop_next()
+	{
+		if (next)
+			pcg_batch_destroy(next);
+		next = nullptr;
+		next_ctxs.clear();
+	}
+	int prebuild(const std::vector<void*>& ctxs)
+	{
+		drop_next();
+		if (autotune || ctxs.empty())
+			return PCG_OK; // the tuner times launches on the real fields: not beside running steps
+		std::vector<pcg_context*> c(ctxs.size());
+		for (size_t i = 0; i < ctxs.size(); i++)
+			c[i] = static_cast<pcg_context*>(ctxs[i]);
+		int rc = pcg_batch_create(&next, c.data(), c.size());
+		if (!rc)
+			rc = pcg_batch_prepare(next);
+		if (rc)
+		{
+			err = pcg_last_error();
+			drop_next();
+			return rc;
+		}
+		next_ctxs = ctxs;
+		return PCG_OK;
+	}
 	int rebuild(const std::vector<void*>& ctxs)
 	{
+		if (next && next_ctxs == ctxs)
+		{
+			drop();
+			batch = next;
+			next = nullptr;
+			next_ctxs.clear();
+			return PCG_OK;
+		}
+		drop_next();
 		drop();
 		std::vector<pcg_context*> c(ctxs.size());
 		for (size_t i = 0; i < ctxs.size(); i++)
@@ -187,6 +226,9 @@ struct pcg_server
 			if (sched->dirty())
 				backend.drop(); // the batch may refer to retired contexts: never keep it past them
 			std::vector<pcg::serve::Request> done = sched->take_finished();
+			for (const auto& r : done) // a request cancelled or failed out of the prepared batch
+				if (std::find(backend.next_ctxs.begin(), backend.next_ctxs.end(), r.ctx) != backend.next_ctxs.end())
+					backend.drop_next();
 			{
 				std::unique_lock<std::mutex> lk(mu);
 				for (auto& r : done)
@@ -201,6 +243,7 @@ struct pcg_server
 					cv_in.wait_for(lk, std::chrono::milliseconds(2));
 			}
 		}
+		backend.drop_next();
 		backend.drop();
 	}
 };
@@ -266,6 +309,7 @@ int pcg_server_destroy(pcg_server* s)
 	if (s->sched)
 		for (void* c : s->sched->release_all())
 			held.push_back(c);
+	s->backend.drop_next();
 	s->backend.drop();
 	for (void* c : held)
 		pcg_destroy(static_cast<pcg_context*>(c));
@@ -378,6 +422,8 @@ int pcg_server_get_stats(pcg_server* s, pcg_server_stats* st)
 	st->rebuild_s = x.rebuild_s;
 	st->step_s = x.step_s;
 	st->admit_s = x.admit_s;
+	st->prebuilds = x.prebuilds;
+	st->prebuild_s = x.prebuild_s;
 	return PCG_OK;
 }
 

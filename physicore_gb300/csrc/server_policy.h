@@ -85,11 +85,13 @@ struct Stats
 {
 	uint64_t submitted = 0, admitted = 0, completed = 0, cancelled = 0, refused = 0, failed = 0;
 	uint64_t ticks = 0, rebuilds = 0, steps = 0;
+	uint64_t prebuilds = 0;         // next-tick batches built while a tick ran
 	uint64_t vss = 0;               // voxel-substrate-steps performed
 	uint64_t active_bytes = 0;      // device bytes of the active set
 	double rebuild_s = 0;           // host time regrouping the active set
 	double step_s = 0;              // host time starting and waiting for steps (admission excluded)
 	double admit_s = 0;             // host time admitting requests
+	double prebuild_s = 0;          // host time building next-tick batches (the device busy meanwhile)
 };
 
 constexpr uint32_t kMaxAttempts = 3;
@@ -188,6 +190,19 @@ public:
 		stats_.admit_s += seconds_since(t0);
 		if (!stepped)
 			return admitted > 0 || copied;
+		if (be_.busy())
+		{
+			// the next tick's set is known now (requests finish when their budget
+			// runs out): build its batch while these steps run
+			std::vector<void*> next;
+			for (size_t i = 0; i < active_.size(); i++)
+				if (i >= stepped || active_[i].remaining > budgets[i])
+					next.push_back(active_[i].ctx);
+			t0 = clock::now();
+			if (be_.prebuild(next) == 0 && !next.empty())
+				stats_.prebuilds++;
+			stats_.prebuild_s += seconds_since(t0);
+		}
 		t0 = clock::now();
 		const int rc = be_.step_end();
 		stats_.step_s += seconds_since(t0);

@@ -104,6 +104,12 @@ struct FakeBackend
 		*done = --polls_left[r.ctx] <= 0;
 		return 0;
 	}
+	std::vector<std::vector<void*>> prebuilt; // sets passed to prebuild, in order
+	int prebuild(const std::vector<void*>& c)
+	{
+		prebuilt.push_back(c);
+		return 0;
+	}
 	int busy_polls = 0; // busy() answers true this many times
 	bool busy() { return busy_polls > 0 && busy_polls--; }
 	std::string last_error() const { return err; }
@@ -298,6 +304,30 @@ void admission_stops_when_steps_finish()
 	EXPECT(s.stats().admit_s >= 0 && s.stats().step_s >= 0 && s.stats().rebuild_s >= 0);
 }
 
+// While a tick's steps run, the next tick's set (those not finishing in it, then
+// those admitted meanwhile) is handed to the backend to prepare; not when the
+// steps are already done.
+void prebuilds_the_next_set()
+{
+	FakeBackend be;
+	Options o;
+	o.reserve_bytes = 0;
+	o.steps_per_tick = 4;
+	Scheduler<FakeBackend> s(be, o);
+	s.submit(req(be, 1, 4, 10), 0);   // finishes in the next tick
+	s.submit(req(be, 2, 100, 10), 0);
+	s.tick(0);
+	EXPECT(s.active() == 2 && be.prebuilt.empty());
+	s.submit(req(be, 3, 50, 10), 0);
+	be.busy_polls = 1; // the steps run on while request 3 is admitted
+	s.tick(1);
+	EXPECT(be.prebuilt.size() == 1 && s.stats().prebuilds == 1);
+	EXPECT(be.prebuilt.back() == (std::vector<void*> { ctx(2), ctx(3) }));
+	be.busy_polls = 0; // done before the backend could prepare anything
+	s.tick(2);
+	EXPECT(be.prebuilt.size() == 1 && s.stats().prebuilds == 1 && s.stats().prebuild_s >= 0);
+}
+
 void readback_before_done()
 {
 	FakeBackend be;
@@ -362,6 +392,7 @@ int main()
 		{ "ServerPolicy.QueueLimitAndZeroSteps", queue_limit_and_zero_steps },
 		{ "ServerPolicy.AdmissionStopsWhenStepsFinish", admission_stops_when_steps_finish },
 		{ "ServerPolicy.ReadbackBeforeDone", readback_before_done },
+		{ "ServerPolicy.PrebuildsTheNextSet", prebuilds_the_next_set },
 	};
 	int n = 0;
 	for (auto& t : tests)

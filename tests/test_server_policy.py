@@ -19,4 +19,4 @@ def test_server_policy_with_fake_backend(tmp_path):
                     os.path.join(ROOT, "tests", "cpp", "test_server_policy.cpp"), "-o", exe], check=True)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert "9 tests, 0 failures" in r.stdout
+    assert "10 tests, 0 failures" in r.stdout
