@@ -204,6 +204,15 @@ int pcg_synchronize(pcg_context* ctx);
  * (s,x,y,z) is at ptr[(z*ny + y)*pitch + x*S + s]. */
 int pcg_get_field_device(pcg_context* ctx, void** ptr, uint64_t* elem_bytes, uint64_t* pitch);
 
+/* Device pointers of the agents' positions [A*dims] (FP64, agent-major) and
+ * activity flags [A] (uint8), for a GPU module that moves agents in place instead
+ * of uploading the host SoA every step (the per-step transfers of
+ * data_manager.cpp:35-93).  Writes must be ordered before the next step on the
+ * context's stream (pcg_get_stream); then pcg_recompute_positional_data, as after
+ * pcg_update_agents.  Valid until the agents are set again or the context is
+ * destroyed.  Initialises the context if needed. */
+int pcg_get_agents_device(pcg_context* ctx, double** positions, uint8_t** is_active);
+
 /* ---- measurement -------------------------------------------------------- */
 
 /* Wraps every kernel launch in CUDA events (per-kernel time) when enabled. */

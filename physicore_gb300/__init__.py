@@ -73,6 +73,7 @@ SIGNATURES = {
     "pcg_get_mass_check": [_P, _P, _P, _P, _P],
     "pcg_synchronize": [_P],
     "pcg_get_field_device": [_P, _P, _P, _P],
+    "pcg_get_agents_device": [_P, _P, _P],
     "pcg_set_kernel_timing": [_P, _i32],
     "pcg_get_kernel_stats": [_P, _P, _u64, _P],
     "pcg_reset_kernel_stats": [_P],
@@ -341,6 +342,12 @@ class Solver:
         p, eb, pitch = ctypes.c_void_p(), ctypes.c_uint64(), ctypes.c_uint64()
         self._check(self._L.pcg_get_field_device(self._h, ctypes.byref(p), ctypes.byref(eb), ctypes.byref(pitch)))
         return p.value, eb.value, pitch.value
+
+    def agents_device(self):
+        """(positions, is_active) device pointers of the agents (pcg_get_agents_device)."""
+        pos, act = ctypes.c_void_p(), ctypes.c_void_p()
+        self._check(self._L.pcg_get_agents_device(self._h, ctypes.byref(pos), ctypes.byref(act)))
+        return pos.value, act.value
 
     def set_stream(self, stream_handle):
         """Queues this context's work on `stream_handle` (None: its own stream).  The

@@ -1545,6 +1545,22 @@ int pcg_get_field_device(pcg_context* c, void** ptr, uint64_t* elem_bytes, uint6
 	return PCG_OK;
 }
 
+int pcg_get_agents_device(pcg_context* c, double** positions, uint8_t** is_active)
+{
+	CTX_CHECK(c);
+	if (!positions || !is_active)
+		return fail(PCG_ERR_INVALID, "null argument");
+	pcg::DeviceGuard g(c->device);
+	int rc = pcg::do_initialize(c);
+	if (rc)
+		return rc;
+	if (c->A == 0)
+		return fail(PCG_ERR_INVALID, "the context holds no agents");
+	*positions = static_cast<double*>(c->a_pos.ptr);
+	*is_active = static_cast<uint8_t*>(c->a_active.ptr);
+	return PCG_OK;
+}
+
 int pcg_set_kernel_timing(pcg_context* c, int enable)
 {
 	CTX_CHECK(c);
