@@ -611,8 +611,10 @@ __global__ void batch_cells_reduce_kernel(BatchArgs b)
 	list_shared(b.doms[di].cells, i, role == kRoleWinner || role == kRoleLoser, di);
 }
 
+// FP32: registers capped for 3 blocks of 256 per SM (a latency-bound gather:
+// more loads in flight; the FP64 build would spill)
 template <typename T>
-__global__ void batch_cells_apply_kernel(BatchArgs b)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) batch_cells_apply_kernel(BatchArgs b)
 {
 	const uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	const uint32_t k = warp_entry(b.list, u);

@@ -61,8 +61,10 @@ __global__ void cells_reduce_kernel(CellArgs a)
 	list_shared(a, i, role == kRoleWinner || role == kRoleLoser, 0);
 }
 
+// FP32: registers capped for 3 blocks of 256 per SM (a latency-bound gather:
+// more loads in flight; the FP64 build would spill)
 template <typename T>
-__global__ void cells_apply_kernel(CellArgs a)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) cells_apply_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	if (i < a.A)

@@ -158,7 +158,9 @@ def test_driver_matches_oracle(diffuse_exe, oracle_mod, tmp_path, seed, dims, so
 
 def test_driver_transfer_every_step_same_field(diffuse_exe, tmp_path):
     """The reference's loop (field to and from the device around every step) and
-    the resident loop write identical images."""
+    the resident loop write the same images, to the FP32 tolerance: the round trip
+    through the FP64 host mirror is exact, but sums over agents sharing a voxel
+    are atomics in any order, so two runs need not be bit-equal."""
     p, xml, agents_txt = _problem(5, 3)
     a = tmp_path / "resident"
     b = tmp_path / "transfer"
@@ -167,7 +169,7 @@ def test_driver_transfer_every_step_same_field(diffuse_exe, tmp_path):
     _, ia, _ = _run(diffuse_exe, str(a), xml, agents_txt, 6, "gb300_solver_fp32")
     _, ib, _ = _run(diffuse_exe, str(b), xml, agents_txt, 6, "gb300_solver_fp32", ("--transfer-every-step",))
     for name in ia[-1]["arrays"]:
-        assert np.array_equal(ia[-1]["arrays"][name], ib[-1]["arrays"][name]), name
+        assert rel_err(ia[-1]["arrays"][name], ib[-1]["arrays"][name]) <= 1e-5, name
 
 
 def test_example_settings_run(diffuse_exe, tmp_path):
