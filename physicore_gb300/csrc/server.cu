@@ -79,11 +79,13 @@ struct GpuBackend
 		next = nullptr;
 		next_ctxs.clear();
 	}
+	// 0 when a batch was prepared; -1 when none is (empty set, or the tuner, which
+	// times launches on the real fields, is on: not beside running steps)
 	int prebuild(const std::vector<void*>& ctxs)
 	{
 		drop_next();
 		if (autotune || ctxs.empty())
-			return PCG_OK; // the tuner times launches on the real fields: not beside running steps
+			return -1;
 		std::vector<pcg_context*> c(ctxs.size());
 		for (size_t i = 0; i < ctxs.size(); i++)
 			c[i] = static_cast<pcg_context*>(ctxs[i]);

@@ -199,7 +199,7 @@ public:
 				if (i >= stepped || active_[i].remaining > budgets[i])
 					next.push_back(active_[i].ctx);
 			t0 = clock::now();
-			if (be_.prebuild(next) == 0 && !next.empty())
+			if (be_.prebuild(next) == 0)
 				stats_.prebuilds++;
 			stats_.prebuild_s += seconds_since(t0);
 		}
