@@ -14,6 +14,7 @@
 #include <fstream>
 #include <functional>
 #include <memory>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -363,6 +364,43 @@ void serializer_writes()
 	EXPECT(std::filesystem::exists(std::filesystem::path(g_scratch) / "out2" / "microenvironment.pvd"));
 }
 
+// Corrupted settings (random deletions, insertions and replacements of
+// characters) either parse or throw std::runtime_error: the reader never crashes,
+// hangs or throws anything else.
+void mutated_settings_fail_cleanly()
+{
+	std::mt19937_64 rng(12345);
+	const std::string base = kSettings;
+	const char alphabet[] = "<>/=\"'&;!?-[]abcxyz0129 \n";
+	int parsed = 0, rejected = 0;
+	for (int trial = 0; trial < 3000; trial++)
+	{
+		std::string t = base;
+		const int edits = 1 + (int)(rng() % 6);
+		for (int e = 0; e < edits && !t.empty(); e++)
+		{
+			const std::size_t at = rng() % t.size();
+			const char ch = alphabet[rng() % (sizeof alphabet - 1)];
+			switch (rng() % 3)
+			{
+			case 0: t.erase(at, 1 + rng() % 8); break;
+			case 1: t.insert(at, 1, ch); break;
+			default: t[at] = ch; break;
+			}
+		}
+		try
+		{
+			(void)parse_physicell_config_text(t);
+			parsed++;
+		}
+		catch (const std::runtime_error&)
+		{
+			rejected++;
+		}
+	}
+	EXPECT(parsed + rejected == 3000 && rejected > 0);
+}
+
 struct test_case
 {
 	const char* name;
@@ -388,6 +426,7 @@ int main(int argc, char** argv)
 		{ "MicroenvironmentTest.CreateFromConfig", create_from_config_builds },
 		{ "MicroenvironmentBuilderTest.Checks", builder_checks },
 		{ "VtkSerializerTest.Writes", serializer_writes },
+		{ "ConfigReaderTest.MutatedSettingsFailCleanly", mutated_settings_fail_cleanly },
 	};
 	int ran = 0;
 	for (const auto& t : tests)

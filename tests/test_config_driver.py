@@ -32,7 +32,7 @@ def config_run(pcg, tmp_path_factory):
 
 def test_config_reader_and_builder(config_run):
     r, _ = config_run
-    assert r.returncode == 0 and "7 tests, 0 failures" in r.stdout, r.stdout + r.stderr
+    assert r.returncode == 0 and "8 tests, 0 failures" in r.stdout, r.stdout + r.stderr
 
 
 @pytest.mark.parametrize("dims", [3, 2])
