@@ -37,7 +37,7 @@ extern "C" {
 #define PCG_ERR_CUDA 2        /* CUDA runtime error */
 #define PCG_ERR_NOMEM 3       /* device or host allocation failed / admission refused */
 #define PCG_ERR_DEVICE 4      /* a kernel flagged a fault (see pcg_last_error) */
-#define PCG_ERR_UNSUPPORTED 5 /* size beyond this build's limits */
+#define PCG_ERR_UNSUPPORTED 5 /* size beyond the library's limits */
 
 /* Arithmetic of the device field: the reference is FP64 throughout
  * (types.h:7); the FP32 build keeps FP64 coefficients/positions/internalized
