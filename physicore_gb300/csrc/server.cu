@@ -69,6 +69,23 @@ struct GpuBackend
 			pcg_batch_destroy(batch);
 		batch = nullptr;
 	}
+	// A batch whose steps are done and whose set changed: destroyed once the next
+	// tick's steps are queued, so that its teardown does not delay them.  It is
+	// never stepped again (its contexts may be destroyed by their owners
+	// meanwhile; destroying a batch does not touch its contexts).
+	std::vector<pcg_batch*> retired;
+	void retire()
+	{
+		if (batch)
+			retired.push_back(batch);
+		batch = nullptr;
+	}
+	void reap()
+	{
+		for (pcg_batch* r : retired)
+			pcg_batch_destroy(r);
+		retired.clear();
+	}
 	// The next tick's batch, built and captured while the current tick runs.
 	pcg_batch* next = nullptr;
 	std::vector<void*> next_ctxs;
@@ -144,6 +161,7 @@ struct GpuBackend
 			rc = pcg_batch_solve_budgets(batch, k - 1, rest_.data());
 		if (rc)
 			err = pcg_last_error();
+		reap();
 		return rc;
 	}
 	// The finished request left the batch, so its field no longer changes: the
@@ -226,7 +244,7 @@ struct pcg_server
 				sched->cancel(tag, t);
 			const bool worked = sched->tick(now());
 			if (sched->dirty())
-				backend.drop(); // the batch may refer to retired contexts: never keep it past them
+				backend.retire(); // the batch may refer to retired contexts: never step it again
 			std::vector<pcg::serve::Request> done = sched->take_finished();
 			for (const auto& r : done) // a request cancelled or failed out of the prepared batch
 				if (std::find(backend.next_ctxs.begin(), backend.next_ctxs.end(), r.ctx) != backend.next_ctxs.end())
@@ -245,6 +263,7 @@ struct pcg_server
 					cv_in.wait_for(lk, std::chrono::milliseconds(2));
 			}
 		}
+		backend.reap();
 		backend.drop_next();
 		backend.drop();
 	}
@@ -311,6 +330,7 @@ int pcg_server_destroy(pcg_server* s)
 	if (s->sched)
 		for (void* c : s->sched->release_all())
 			held.push_back(c);
+	s->backend.reap();
 	s->backend.drop_next();
 	s->backend.drop();
 	for (void* c : held)
