@@ -1465,12 +1465,12 @@ int refresh(pcg_batch* b)
 std::vector<cudaStream_t> context_streams(pcg_batch* b)
 {
 	std::vector<cudaStream_t> out;
+	out.reserve(b->ctx.size());
 	for (size_t d = 0; d < b->ctx.size(); d++)
-	{
-		cudaStream_t s = C(b, d)->stream;
-		if (s != b->stream && std::find(out.begin(), out.end(), s) == out.end())
-			out.push_back(s);
-	}
+		if (C(b, d)->stream != b->stream)
+			out.push_back(C(b, d)->stream);
+	std::sort(out.begin(), out.end());
+	out.erase(std::unique(out.begin(), out.end()), out.end());
 	return out;
 }
 
@@ -1478,6 +1478,10 @@ int sync_in(pcg_batch* b)
 {
 	for (cudaStream_t s : context_streams(b))
 	{
+		// a stream with nothing left to run needs no wait (hundreds of served
+		// requests: one query instead of an event record and a wait each)
+		if (cudaStreamQuery(s) == cudaSuccess)
+			continue;
 		PCG_CUDA_TRY(cudaEventRecord(b->ev_sync, s));
 		PCG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_sync, 0));
 	}
