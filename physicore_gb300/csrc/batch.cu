@@ -624,24 +624,28 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) batch_cells_apply
 }
 
 template <typename T>
-__global__ void batch_cells_internalize_kernel(BatchArgs b, uint32_t ndom)
+__global__ void batch_cells_internalize_kernel(BatchArgs b, const uint32_t* __restrict__ block0, uint32_t ndom)
 {
-	// Work is the domains' lists of agents in shared voxels (a few percent of the
-	// agents), whose lengths are on the device: blocks take domains in turn, and
-	// with more blocks than domains each domain's list is split among its blocks.
-	const uint32_t G = gridDim.x;
-	const uint32_t first = G >= ndom ? blockIdx.x % ndom : blockIdx.x;
-	const uint32_t part = G >= ndom ? blockIdx.x / ndom : 0;
-	for (uint32_t d = first; d < ndom; d += (G >= ndom ? ndom : G))
+	// Work is the domains' lists of agents in shared voxels, whose lengths are on
+	// the device.  Domain d owns blocks [block0[d], block0[d+1]) (in proportion to
+	// its agents, set when the batch is built) and splits its list among them.
+	uint32_t lo = 0, hi = ndom; // the last d with block0[d] <= blockIdx.x
+	while (hi - lo > 1)
 	{
-		const uint32_t parts = G >= ndom ? (G - d + ndom - 1) / ndom : 1;
-		const CellArgs& a = b.doms[d].cells;
-		if (!b.steps_left[d] || !a.internalized || !a.A)
-			continue;
-		const uint32_t count = __ldg(a.flags + 1);
-		for (uint64_t j = (uint64_t)part * blockDim.x + threadIdx.x; j < count; j += (uint64_t)parts * blockDim.x)
-			agent_internalize<T>(a, __ldg(a.shared + j));
+		const uint32_t mid = (lo + hi) / 2;
+		if (__ldg(block0 + mid) <= blockIdx.x)
+			lo = mid;
+		else
+			hi = mid;
 	}
+	const uint32_t d = lo;
+	const uint32_t part = blockIdx.x - __ldg(block0 + d), parts = __ldg(block0 + d + 1) - __ldg(block0 + d);
+	const CellArgs& a = b.doms[d].cells;
+	if (!b.steps_left[d] || !a.internalized || !a.A || part >= parts)
+		return;
+	const uint32_t count = __ldg(a.flags + 1);
+	for (uint64_t j = (uint64_t)part * blockDim.x + threadIdx.x; j < count; j += (uint64_t)parts * blockDim.x)
+		agent_internalize<T>(a, __ldg(a.shared + j));
 }
 
 // End of a step: one step fewer for every domain still running.
@@ -758,6 +762,8 @@ struct pcg_batch
 {
 	int device = 0;
 	uint32_t* h_words = nullptr; // pinned host words for reading the error words
+	pcg::DeviceBuffer d_iblocks;   // internalize: first block of each domain [N + 1]
+	uint32_t internalize_blocks = 0;
 	cudaEvent_t ev_block = nullptr; // blocking-sync event for host waits on the stream
 	size_t wsize = 4;
 	int sm_count = 0;
@@ -1174,6 +1180,28 @@ int build_t(pcg_batch* b)
 		if ((rc = sweep_grid<T>(b, axis, b->smem[axis], b->lists[axis].total, &b->grid[axis])))
 			return rc;
 	}
+	// internalize blocks per domain in proportion to its agents (those in shared
+	// voxels are only known on the device): block0[d] .. block0[d+1]
+	{
+		std::vector<uint32_t> block0(N + 1, 0);
+		double total = 0;
+		for (size_t d = 0; d < N; d++)
+			total += C(b, d)->compute_internalized ? (double)C(b, d)->A : 0.0;
+		const double G = 8.0 * std::max(b->sm_count, 1);
+		for (size_t d = 0; d < N; d++)
+		{
+			const Context* c = C(b, d);
+			const double w = c->compute_internalized ? (double)c->A : 0.0;
+			const uint32_t blocks = w > 0 ? (uint32_t)std::max(1.0, std::floor(G * w / total)) : 0u;
+			block0[d + 1] = block0[d] + blocks;
+		}
+		b->internalize_blocks = block0[N];
+		if ((rc = balloc(b->d_iblocks, (N + 1) * sizeof(uint32_t), b->stream, b->device)))
+			return rc;
+		PCG_CUDA_TRY(cudaMemcpyAsync(b->d_iblocks.ptr, block0.data(), (N + 1) * sizeof(uint32_t),
+									 cudaMemcpyHostToDevice, b->stream));
+		PCG_CUDA_TRY(batch_wait(b));
+	}
 	// algorithmic bytes per launch, with the single-domain launchers' per-item counts
 	std::fill(b->step_bytes, b->step_bytes + K_COUNT, 0.0);
 	b->rebuild_bytes.assign(N, { 0.0, 0.0, 0.0, 0.0 });
@@ -1364,8 +1392,8 @@ int launch_step(pcg_batch* b)
 		{
 			LaunchScope s(b, K_CELLS_INTERNALIZE, sb[K_CELLS_INTERNALIZE]);
 			const uint32_t ndom = (uint32_t)b->ctx.size();
-			batch_cells_internalize_kernel<T><<<8 * std::max(b->sm_count, 1), 256, 0, b->stream>>>(
-				args_for(b, L_AGENTS, 3), ndom);
+			batch_cells_internalize_kernel<T><<<std::max(b->internalize_blocks, 1u), 256, 0, b->stream>>>(
+				args_for(b, L_AGENTS, 3), static_cast<const uint32_t*>(b->d_iblocks.ptr), ndom);
 			PCG_CUDA_TRY(cudaGetLastError());
 		}
 	}
@@ -1874,7 +1902,7 @@ int pcg_batch_destroy(pcg_batch* b)
 	for (cudaEvent_t e : b->event_pool)
 		cudaEventDestroy(e);
 	DeviceBuffer* bufs[] = { &b->d_doms,	 &b->d_tmaps,	  &b->d_lists,		&b->d_counters,
-							 &b->d_err, &b->d_recompute, &b->d_steps_left };
+							 &b->d_err, &b->d_recompute, &b->d_steps_left, &b->d_iblocks };
 	for (DeviceBuffer* x : bufs)
 		pcg::free_buf(*x);
 	if (b->ev_sync)
