@@ -375,15 +375,20 @@ int pcg_server_get_stats(pcg_server* server, pcg_server_stats* stats);
  *    elements (>= grid_shape[0] * substrates), rows ordered by y then z.
  *  - All agent arrays are device pointers, laid out as in pcg_set_agents;
  *    internalized is updated in place when compute_internalized is non-zero.
- *  - Work is queued on `stream` (NULL: the default stream), and the call then
- *    synchronises that stream to report device faults (PCG_ERR_DEVICE).
+ *  - Work is queued on `stream` (NULL: the default stream); every call then
+ *    copies the device error word to the host and synchronises that stream to
+ *    report device faults (PCG_ERR_DEVICE), so the call blocks until its work is
+ *    done and cannot be recorded into a CUDA graph by stream capture.
  *  - Scratch comes from one fixed 16 MiB array in device memory that every GPU
  *    loading this library holds until the process exits; a problem that needs
  *    more (about 8 bytes per voxel plus 13 + 24*substrates bytes per agent) is
- *    rejected with PCG_ERR_UNSUPPORTED.  The first call on a device looks up the
- *    array's device address, so make that first call before any stream capture.
- *  - All calls share the array: calls that overlap on the GPU (other streams,
- *    other host threads) race with each other and must be serialised. */
+ *    rejected with PCG_ERR_UNSUPPORTED, as are meshes of 2^32 - 1 or more voxels,
+ *    2^32 - 1 or more agents and fields of 2^32 or more elements (pitch * ny *
+ *    nz).  grid_shape must be 1 on the axes beyond dims (PCG_ERR_INVALID).  The
+ *    first call on a device looks up the array's device address.
+ *  - All calls share the array, which keeps the last call's contents: calls that
+ *    overlap on the GPU (other streams, other host threads) race with each other
+ *    and must be serialised by the caller. */
 int pcg_cells_noalloc(float* field, uint64_t pitch, int dims, const int64_t bbox_min[3],
 					  const uint64_t voxel_shape[3], const uint64_t grid_shape[3], uint64_t substrates, double dt,
 					  uint64_t agents, const double* positions, const double* secretion, const double* saturation,

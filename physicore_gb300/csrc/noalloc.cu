@@ -65,18 +65,38 @@ extern "C" int pcg_cells_noalloc(float* field, uint64_t pitch, int dims, const i
 	{
 		if (grid_shape[d] == 0 || (d < dims && voxel_shape[d] == 0))
 			return fail(PCG_ERR_INVALID, "pcg_cells_noalloc: empty grid axis or zero voxel shape");
-		V *= grid_shape[d];
+		if (d >= dims && grid_shape[d] != 1)
+			return fail(PCG_ERR_INVALID, "pcg_cells_noalloc: grid_shape must be 1 on the axes beyond dims");
+		if (__builtin_mul_overflow(V, grid_shape[d], &V))
+			return fail(PCG_ERR_UNSUPPORTED, "pcg_cells_noalloc: the voxel count overflows 64 bits");
 	}
-	if (pitch < grid_shape[0] * substrates)
+	uint64_t row = 0, field_elems = 0, terms = 0;
+	if (__builtin_mul_overflow(grid_shape[0], substrates, &row))
+		return fail(PCG_ERR_UNSUPPORTED, "pcg_cells_noalloc: nx * substrates overflows 64 bits");
+	if (pitch < row)
 		return fail(PCG_ERR_INVALID, "pcg_cells_noalloc: pitch shorter than a row (nx * substrates)");
+	// voxel indices, agent indices and field offsets are 32-bit on the device
+	if (V >= 0xffffffffull)
+		return fail(PCG_ERR_UNSUPPORTED, "pcg_cells_noalloc: meshes of 2^32 - 1 or more voxels are not supported");
+	if (agents >= 0xffffffffull)
+		return fail(PCG_ERR_UNSUPPORTED, "pcg_cells_noalloc: 2^32 - 1 or more agents are not supported");
+	if (__builtin_mul_overflow(pitch, grid_shape[1] * grid_shape[2], &field_elems) || field_elems >= (1ull << 32))
+		return fail(PCG_ERR_UNSUPPORTED,
+					"pcg_cells_noalloc: fields of 2^32 or more elements (pitch * ny * nz) are not supported");
+	if (__builtin_mul_overflow(agents, substrates, &terms) || __builtin_mul_overflow(terms, sizeof(float), &terms))
+		return fail(PCG_ERR_UNSUPPORTED, "pcg_cells_noalloc: agents * substrates overflows 64 bits");
 	if (agents && (!positions || !secretion || !saturation || !uptake || !net_export || !volumes || !is_active ||
 				   (compute_internalized && !internalized)))
 		return fail(PCG_ERR_INVALID, "pcg_cells_noalloc: null agent array");
 	if (agents == 0)
 		return PCG_OK;
+	// every piece below is at most kScratchBytes before the total is compared
+	if (V > kScratchBytes || terms > kScratchBytes)
+		return fail(PCG_ERR_UNSUPPORTED,
+					"pcg_cells_noalloc: the mesh and agents need more than the fixed " + std::to_string(kScratchBytes) +
+						" bytes of scratch (about 8 bytes per voxel + (13 + 24*S) bytes per agent)");
 
 	// scratch layout: flags | err | owner[V] | counts[V] | vox[A] | foff[A] | shared[A] | role[A] | 6 x terms[A*S]
-	const size_t terms = agents * substrates * sizeof(float);
 	size_t off = 0;
 	const size_t o_flags = off;
 	off += 256;

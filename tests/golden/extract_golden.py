@@ -7,9 +7,10 @@ every `std::vector<double> expected = {...}` array.  The tests in tests/ rebuild
 each scenario from the cited lines and compare the oracle (and the GPU path)
 against these values.
 
-Usage:  python tests/golden/extract_golden.py [REFERENCE_ROOT]
-(REFERENCE_ROOT defaults to /root/reference; it is only needed to regenerate the
-committed JSON, never at test time.)
+Usage:  python tests/golden/extract_golden.py REFERENCE_ROOT
+   or:  PHYSICORE_REFERENCE_ROOT=... python tests/golden/extract_golden.py
+(REFERENCE_ROOT is a checkout of the reference project; it is only needed to
+regenerate the committed JSON, never at test time.)
 """
 from __future__ import annotations
 
@@ -76,7 +77,9 @@ def parse(path: str, rel: str) -> dict:
 
 
 def main() -> None:
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PHYSICORE_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: extract_golden.py REFERENCE_ROOT (or set PHYSICORE_REFERENCE_ROOT)")
     data = {"source": "bsc-life/PhysiCore reference tests (paths relative to the project root)", "tests": {}}
     for rel in FILES:
         data["tests"].update(parse(os.path.join(root, rel), rel))
