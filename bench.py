@@ -540,14 +540,21 @@ def run_error_long(args, w, p, local, det):
     g = W.apply(pcg.Solver(pcg.FP32), p)
     o = W.apply(oracle.OracleSolver(threads=cpu_threads()), p)
     t0 = time.perf_counter()
-    checkpoints = sorted({c for c in (1, 10, 100, steps) if c <= steps})
+    checkpoints = sorted({c for c in (1, 10, 100, 300, steps) if c <= steps})
     rows, done = [], 0
     for c in checkpoints:
         g.solve(c - done)
         o.solve(c - done)
         done = c
-        mr, l2 = field_error(g.get_field(), o.get_field())
-        rows.append({"steps": c, "max_rel": mr, "l2_rel": l2})
+        fg, fo = g.get_field(), o.get_field()
+        mr, l2 = field_error(fg, fo)
+        Sx = fo.shape[-1]
+        dd = np.abs(fg.reshape(-1, Sx) - fo.reshape(-1, Sx))
+        per_s = (dd.max(axis=0) / np.abs(fo.reshape(-1, Sx)).max(axis=0)).tolist()
+        mass_rel = (np.abs(fg.reshape(-1, Sx).sum(axis=0) - fo.reshape(-1, Sx).sum(axis=0))
+                    / np.abs(fo.reshape(-1, Sx).sum(axis=0))).tolist()
+        rows.append({"steps": c, "max_rel": mr, "l2_rel": l2, "max_rel_by_substrate": [r4(v) for v in per_s],
+                     "mass_rel_by_substrate": [r4(v) for v in mass_rel]})
     out = {"steps": steps, "max_rel": rows[-1]["max_rel"], "l2_rel": rows[-1]["l2_rel"],
            "counts_bit_exact": bool(np.array_equal(g.get_counts().reshape(-1), o.get_counts().reshape(-1))),
            "by_steps": rows, "oracle_s": round(time.perf_counter() - t0, 1), "tolerance": FP32_RTOL}

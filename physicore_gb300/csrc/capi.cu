@@ -520,21 +520,19 @@ static int run_phases(Context* c, uint32_t phases, bool recompute)
 	// with both phases in this call, the last sweep writes the boundary faces into
 	// its tiles before storing them (the reference's next step, dirichlet_solver.cpp:
 	// 59-83), which saves a pass of scattered writes
-	// (not while the mass check reads the field between the sweeps and Dirichlet)
+	// With the mass check on, the x sweep adds up its inputs and the last sweep its
+	// outputs (before writing any face), so the check reads no extra field pass.
 	const bool check = c->mass_check && (phases & PCG_PHASE_DIFFUSION);
-	const bool fuse =
-		!check && (phases & PCG_PHASE_DIFFUSION) && (phases & PCG_PHASE_DIRICHLET) && faces_fusable(c);
+	const bool fuse = (phases & PCG_PHASE_DIFFUSION) && (phases & PCG_PHASE_DIRICHLET) && faces_fusable(c);
 	if (phases & PCG_PHASE_DIFFUSION)
 	{
-		if (check && (rc = launch_mass_check(c, 0)))
+		if ((rc = launch_sweep_x(c, check)))
 			return rc;
-		if ((rc = launch_sweep_x(c)))
+		if (c->dims >= 2 && (rc = launch_sweep_yz(c, 1, fuse && c->dims == 2, check && c->dims == 2)))
 			return rc;
-		if (c->dims >= 2 && (rc = launch_sweep_yz(c, 1, fuse && c->dims == 2)))
+		if (c->dims >= 3 && (rc = launch_sweep_yz(c, 2, fuse, check)))
 			return rc;
-		if (c->dims >= 3 && (rc = launch_sweep_yz(c, 2, fuse)))
-			return rc;
-		if (check && (rc = launch_mass_check(c, 1)))
+		if (check && (rc = launch_mass_check_finish(c)))
 			return rc;
 		c->mass_checked_steps += check;
 	}
@@ -1463,9 +1461,10 @@ int pcg_mass(pcg_context* c, double* host)
 static int prepare_mass_check(Context* c)
 {
 	int rc;
-	if ((rc = pcg::dalloc(c, c->mc_cols, 2 * c->row_len * sizeof(double))) ||
+	if ((rc = pcg::dalloc(c, c->mc_tot, 2 * c->S * sizeof(double))) ||
 		(rc = pcg::dalloc(c, c->mc_out, 4 * c->S * sizeof(double))))
 		return rc;
+	PCG_CUDA_TRY(cudaMemsetAsync(c->mc_tot.ptr, 0, 2 * c->S * sizeof(double), c->stream));
 	std::vector<double> h(4 * c->S, 0.0);
 	for (uint64_t s = 0; s < c->S; s++)
 	{

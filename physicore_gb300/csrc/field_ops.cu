@@ -64,79 +64,21 @@ __global__ void mass_kernel(const T* field, double* out, uint64_t nx, uint64_t p
 	}
 }
 
-// Per-column totals of the field: a thread per (x, s) column of the rows
-// [blockIdx.y * chunk, +chunk), coalesced across the warp.  FP32 fields are summed
-// as float pairs (Knuth's TwoSum with the errors accumulated, about 2^-44
-// relative), so the FP64 pipe only takes one add per column and chunk; FP64
-// fields are summed in FP64.
-template <typename T>
-__global__ void column_mass_kernel(const T* field, double* cols, uint64_t row_len, uint64_t pitch, uint64_t rows,
-								   uint64_t chunk)
+// One small block after a checked step's sweeps: per substrate, the totals the
+// sweeps added before (tot[0, S)) and after (tot[S, 2S)), the worst relative
+// residual of after * factor = before, and the totals cleared for the next step.
+// out = [before S | after S | worst S | factor S].
+__global__ void mass_check_finish_kernel(double* tot, uint32_t S, double* out)
 {
-	const uint64_t col = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-	if (col >= row_len)
-		return;
-	const uint64_t r0 = blockIdx.y * chunk;
-	const uint64_t r1 = r0 + chunk < rows ? r0 + chunk : rows;
-	const T* p = field + col;
-	if constexpr (sizeof(T) == 4)
+	for (uint32_t s = threadIdx.x; s < S; s += blockDim.x)
 	{
-		float hi = 0.f, lo = 0.f;
-#pragma unroll 8
-		for (uint64_t r = r0; r < r1; r++)
-		{
-			const float x = __ldg(p + r * pitch);
-			const float s = __fadd_rn(hi, x);
-			const float bb = __fsub_rn(s, hi);
-			lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb)));
-			hi = s;
-		}
-		atomicAdd(cols + col, (double)hi + (double)lo);
-	}
-	else
-	{
-		double acc = 0.0;
-#pragma unroll 8
-		for (uint64_t r = r0; r < r1; r++)
-			acc += __ldg(p + r * pitch);
-		atomicAdd(cols + col, acc);
-	}
-}
-
-// One block: per substrate, the totals before (cols[0, row_len)) and after
-// (cols[row_len, 2 row_len)) the sweeps, and the worst relative residual of
-// after * factor = before.  out = [before S | after S | worst S | factor S].
-__global__ void mass_check_finish_kernel(const double* cols, uint64_t row_len, uint32_t S, double* out)
-{
-	__shared__ double part[2][32];
-	const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-	for (uint32_t s = 0; s < S; s++)
-	{
-		double b = 0.0, a = 0.0;
-		for (uint64_t c = s + (uint64_t)threadIdx.x * S; c < row_len; c += (uint64_t)blockDim.x * S)
-		{
-			b += cols[c];
-			a += cols[row_len + c];
-		}
-		for (int o = 16; o > 0; o >>= 1)
-		{
-			b += __shfl_xor_sync(0xffffffffu, b, o);
-			a += __shfl_xor_sync(0xffffffffu, a, o);
-		}
-		if (lane == 0)
-			part[0][warp] = b, part[1][warp] = a;
-		__syncthreads();
-		if (threadIdx.x == 0)
-		{
-			b = a = 0.0;
-			for (uint32_t w = 0; w < nwarps; w++)
-				b += part[0][w], a += part[1][w];
-			out[s] = b;
-			out[S + s] = a;
-			const double res = fabs(a * out[3 * S + s] - b) / fmax(fabs(b), 1e-300);
-			out[2 * S + s] = fmax(out[2 * S + s], res);
-		}
-		__syncthreads();
+		const double b = tot[s], a = tot[S + s];
+		out[s] = b;
+		out[S + s] = a;
+		const double res = fabs(a * out[3 * S + s] - b) / fmax(fabs(b), 1e-300);
+		out[2 * S + s] = fmax(out[2 * S + s], res);
+		tot[s] = 0.0;
+		tot[S + s] = 0.0;
 	}
 }
 
@@ -285,37 +227,15 @@ static int run_mass(Context* c, double* out)
 
 int launch_mass(Context* c, double* out) { return c->wsize == 4 ? run_mass<float>(c, out) : run_mass<double>(c, out); }
 
-template <typename T>
-static int run_mass_check(Context* c, int half)
+int launch_mass_check_finish(Context* c)
 {
-	double* cols = static_cast<double*>(c->mc_cols.ptr);
-	if (half == 0)
-		PCG_CUDA_TRY(cudaMemsetAsync(cols, 0, 2 * c->row_len * sizeof(double), c->stream));
-	// about 2048 threads per SM in total, each over a chunk of rows
-	const unsigned bx = (unsigned)((c->row_len + 255) / 256);
-	const uint64_t want = (uint64_t)(c->sm_count > 0 ? c->sm_count : 152) * 8;
-	uint64_t ny = (want + bx - 1) / bx;
-	ny = ny < c->rows ? ny : c->rows;
-	ny = ny < 65535 ? ny : 65535;
-	ny = ny > 0 ? ny : 1;
-	const uint64_t chunk = (c->rows + ny - 1) / ny;
-	const dim3 grid(bx, (unsigned)((c->rows + chunk - 1) / chunk));
 	cudaEvent_t ev;
-	launch_begin(c, K_MASS_CHECK, (double)(c->V * c->S * sizeof(T)), &ev);
-	column_mass_kernel<T><<<grid, 256, 0, c->stream>>>(static_cast<const T*>(c->field.ptr), cols + half * c->row_len,
-													   c->row_len, c->pitch, c->rows, chunk);
-	if (half == 1)
-		mass_check_finish_kernel<<<1, 256, 0, c->stream>>>(cols, c->row_len, (uint32_t)c->S,
-														   static_cast<double*>(c->mc_out.ptr));
+	launch_begin(c, K_MASS_CHECK, (double)(c->S * 6 * sizeof(double)), &ev);
+	mass_check_finish_kernel<<<1, 64, 0, c->stream>>>(static_cast<double*>(c->mc_tot.ptr), (uint32_t)c->S,
+													  static_cast<double*>(c->mc_out.ptr));
 	launch_end(c, K_MASS_CHECK, ev);
-	c->launches += half; // the finish kernel
 	PCG_CUDA_TRY(cudaGetLastError());
 	return PCG_OK;
-}
-
-int launch_mass_check(Context* c, int half)
-{
-	return c->wsize == 4 ? run_mass_check<float>(c, half) : run_mass_check<double>(c, half);
 }
 
 template <typename T>

@@ -119,6 +119,11 @@ struct SweepArgs
 	const uint8_t* face_conds;
 	uint32_t face_mask;
 	uint64_t nx, ny, nz;
+	// mass check (kernels instantiated with it): FP64 totals [before S | after S];
+	// the x sweep adds its inputs, the last sweep its outputs (x as well when the
+	// mesh is 1-D: mc_x_out)
+	double* mc_tot;
+	uint32_t mc_x_out;
 };
 
 // ------------------------------------------------------------------ context
@@ -218,12 +223,13 @@ struct Context
 	DeviceBuffer tickets;  // uint32 [4]: tile counters of the persistent sweeps
 	DeviceBuffer flags;    // uint32 [4]: [0] ballot conflict, [1] agents in shared voxels
 	DeviceBuffer mass;     // double [S]
-	// per-step mass check (pcg_set_mass_check): column sums before and after the
-	// sweeps [2 * row_len], and [4 * S]: mass before, mass after, worst residual,
-	// (1 + decay*dt/dims)^dims
+	// per-step mass check (pcg_set_mass_check): FP64 totals [2 * S] before the
+	// first sweep and after the last one, added by the sweeps themselves, and
+	// [4 * S]: mass before, mass after, worst residual, the product of the sweep
+	// matrices' column sums
 	bool mass_check = false;
 	uint64_t mass_checked_steps = 0;
-	DeviceBuffer mc_cols;
+	DeviceBuffer mc_tot;
 	DeviceBuffer mc_out;
 	DeviceBuffer staging;  // layout conversion
 	// asynchronous field readback: two staging buffers used in turn, copied to the
@@ -297,8 +303,8 @@ void collect_timings(Context* c);
 
 // ------------------------------------------------------------------ kernel launchers (defined in .cu files)
 
-int launch_sweep_x(Context* c);
-int launch_sweep_yz(Context* c, int axis, bool fuse_faces = false);
+int launch_sweep_x(Context* c, bool mass_check = false);
+int launch_sweep_yz(Context* c, int axis, bool fuse_faces = false, bool mass_check = false);
 // Dirichlet faces (unless the last sweep already wrote them) and interior nodes
 int launch_dirichlet(Context* c, bool faces_done = false);
 // true when the last sweep of c can apply the boundary faces itself
@@ -307,9 +313,10 @@ int launch_bulk(Context* c);
 int launch_cells(Context* c, bool recompute);
 int launch_release(Context* c, uint64_t agent);
 int launch_mass(Context* c, double* dev_out);
-// Column sums of the field into c->mc_cols (half 0: before the sweeps, 1: after);
-// after half 1, the per-substrate masses and the residual into c->mc_out.
-int launch_mass_check(Context* c, int half);
+// After a checked step's sweeps: the per-substrate masses before and after them
+// and the residual into c->mc_out, from the totals the sweeps added to
+// c->mc_tot (cleared for the next step).
+int launch_mass_check_finish(Context* c);
 int launch_to_host_layout(Context* c, void* dst, int layout, int dtype);
 int launch_from_host_layout(Context* c, const void* src, int layout, int dtype);
 int launch_fill_initial(Context* c); // from the initial values already in c->mass (as T)

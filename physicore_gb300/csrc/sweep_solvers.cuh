@@ -45,6 +45,76 @@ __device__ __forceinline__ V ldg_vec(const V* p)
 	return __ldg(p);
 }
 
+// Mass-check accumulators: a lane's running total of the values a sweep reads
+// (before the step's first sweep) or writes (after its last sweep), fused into
+// the solvers so the check needs no pass of its own.  FP32: a float pair
+// hi + lo accumulated with Knuth's TwoSum (error-free), fed with FP32 sums of
+// blocks of points, so about one extra instruction per point; FP64: a double.
+template <typename T>
+struct MassAcc;
+
+template <>
+struct MassAcc<float>
+{
+	float hi, lo;
+	__device__ __forceinline__ void zero() { hi = lo = 0.f; }
+	__device__ __forceinline__ void add(float x)
+	{
+		const float s = __fadd_rn(hi, x);
+		const float bb = __fsub_rn(s, hi);
+		lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb)));
+		hi = s;
+	}
+	template <int P>
+	__device__ __forceinline__ void add_block(const float (&x)[P])
+	{
+		static_assert(P == 8, "blocks of 8 points");
+		add(__fadd_rn(__fadd_rn(__fadd_rn(x[0], x[1]), __fadd_rn(x[2], x[3])),
+					  __fadd_rn(__fadd_rn(x[4], x[5]), __fadd_rn(x[6], x[7]))));
+	}
+	__device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+template <>
+struct MassAcc<double>
+{
+	double v;
+	__device__ __forceinline__ void zero() { v = 0.0; }
+	__device__ __forceinline__ void add(double x) { v += x; }
+	template <int P>
+	__device__ __forceinline__ void add_block(const double (&x)[P])
+	{
+		static_assert(P == 8, "blocks of 8 points");
+		v += ((x[0] + x[1]) + (x[2] + x[3])) + ((x[4] + x[5]) + (x[6] + x[7]));
+	}
+	__device__ __forceinline__ double value() const { return v; }
+};
+
+// Mass-check modes of a solver call (bits): sum the inputs, sum the outputs.
+enum : int
+{
+	kMcIn = 1,
+	kMcOut = 2,
+};
+
+// Adds the totals v of the first `width` lanes of the warp to FP64 totals with
+// atomics, where lanes l and l + stride (stride <= 32) add to the same total: the
+// classes are summed by a tree over strides stride, 2*stride, ..., then lane
+// l < stride adds its class's sum to *dst (its own target).  All `width` lanes
+// of the warp call it.
+__device__ __forceinline__ void flush_classes(double v, uint32_t stride, uint32_t width, double* dst)
+{
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t mask = width >= 32 ? 0xffffffffu : ((1u << width) - 1u);
+	for (uint32_t k = stride; k < 32; k <<= 1)
+	{
+		const double t = __shfl_down_sync(mask, v, k);
+		if (lane + k < width)
+			v += t;
+	}
+	if (lane < stride && lane < width && v != 0.0)
+		atomicAdd(dst, v);
+}
 
 // One lane's coefficients along a line, from the compressed tables of an axis:
 // points j < H read the substrate's head rows, points H <= j < n-1 share the middle
@@ -115,8 +185,12 @@ __device__ __forceinline__ T coef_at(const T* head, uint32_t H, T mid, T last, u
 // kBlock points are pipelined: the next block's points and coefficients are
 // requested before the current block's dependent chain, so load latency overlaps
 // it; most blocks take their coefficients from registers (the middle constants).
-template <typename T, int STRIDE>
-__device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint32_t rt_stride, const LineCoef<T>& L)
+//
+// MC (kMcIn / kMcOut bits) adds the line's input values to *acc_in and its
+// solved values to *acc_out.
+template <typename T, int STRIDE, int MC = 0>
+__device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint32_t rt_stride, const LineCoef<T>& L,
+										   MassAcc<T>* acc_in = nullptr, MassAcc<T>* acc_out = nullptr)
 {
 	using V = typename Vec16<T>::type;
 	constexpr int P = kBlock, VN = Vec16<T>::N, NV = P / VN;
@@ -144,6 +218,8 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 					xn[q] = blk[(P + q) * st];
 				fetch_block<T, V, NV>(L.hE, L.H, L.mE, L.lE, n, (b + 1) * P, en);
 			}
+			if constexpr ((MC & kMcIn) != 0)
+				acc_in->add_block(x);
 #pragma unroll
 			for (int q = 0; q < P; q++)
 			{
@@ -159,7 +235,10 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 		}
 		for (uint32_t j = nb * P; j < n; j++)
 		{
-			d = dev::fmadd(coef_at(L.hE, L.H, L.mE, L.lE, n, j), d, col[(uint64_t)j * st]);
+			const T xj = col[(uint64_t)j * st];
+			if constexpr ((MC & kMcIn) != 0)
+				acc_in->add(xj);
+			d = dev::fmadd(coef_at(L.hE, L.H, L.mE, L.lE, n, j), d, xj);
 			col[(uint64_t)j * st] = d;
 		}
 	}
@@ -168,6 +247,8 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 	{
 		d = dev::fmadd(c, d, col[(uint64_t)j * st]) * coef_at(L.hB, L.H, L.mB, L.lB, n, (uint32_t)j);
 		col[(uint64_t)j * st] = d;
+		if constexpr ((MC & kMcOut) != 0)
+			acc_out->add(d);
 	}
 	{
 		T x[P], xn[P];
@@ -190,12 +271,16 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 					xn[q] = blk[(q - P) * (int)st];
 				fetch_block<T, V, NV>(L.hB, L.H, L.mB, L.lB, n, (uint32_t)(b - 1) * P, bn);
 			}
+			T y[P];
 #pragma unroll
 			for (int q = P - 1; q >= 0; q--)
 			{
 				d = dev::fmadd(c, d, x[q]) * vget<V, T>(bb[q / VN], q % VN);
 				blk[q * st] = d;
+				y[q] = d;
 			}
+			if constexpr ((MC & kMcOut) != 0)
+				acc_out->add_block(y);
 #pragma unroll
 			for (int q = 0; q < P; q++)
 				x[q] = xn[q];
@@ -209,9 +294,11 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 
 // S*sizeof(T) a multiple of 16 bytes: thread h of a row's TPR threads owns chunk
 // slot h of every x position (VN substrates, VN independent recurrences).
-template <typename T, int TPR>
+// MC adds element u's inputs / outputs to acc_in[u] / acc_out[u] (substrate h*VN + u).
+template <typename T, int TPR, int MC = 0>
 __device__ __forceinline__ void solve_row_chunks(T* row, const T* __restrict__ cB, const T* __restrict__ cE,
-												 const T* __restrict__ cC, uint32_t n, int h)
+												 const T* __restrict__ cC, uint32_t n, int h,
+												 MassAcc<T>* acc_in = nullptr, MassAcc<T>* acc_out = nullptr)
 {
 	using V = typename Vec16<T>::type;
 	constexpr int VN = Vec16<T>::N, P = kChunkBlock;
@@ -230,6 +317,8 @@ __device__ __forceinline__ void solve_row_chunks(T* row, const T* __restrict__ c
 #pragma unroll
 		for (int u = 0; u < VN; u++)
 		{
+			if constexpr ((MC & kMcIn) != 0)
+				acc_in[u].add(vget<V, T>(v, u));
 			d[u] = dev::fmadd(vget<V, T>(e, u), d[u], vget<V, T>(v, u));
 			vset<V, T>(v, u, d[u]);
 		}
@@ -240,6 +329,8 @@ __device__ __forceinline__ void solve_row_chunks(T* row, const T* __restrict__ c
 		{
 			d[u] = dev::fmadd(c[u], d[u], vget<V, T>(v, u)) * vget<V, T>(b, u);
 			vset<V, T>(v, u, d[u]);
+			if constexpr ((MC & kMcOut) != 0)
+				acc_out[u].add(d[u]);
 		}
 	};
 	{
@@ -328,9 +419,11 @@ __device__ __forceinline__ void solve_row_chunks(T* row, const T* __restrict__ c
 // ST substrates (1..8) not filling whole chunks: the row is a stream of chunks,
 // element k of substrate k % ST.  Blocks of NB chunks hold whole groups of
 // lcm(ST, VN) elements, so each element's substrate is a compile-time index.
-template <typename T, int ST>
+// MC adds substrate s's inputs / outputs to acc_in[s] / acc_out[s].
+template <typename T, int ST, int MC = 0>
 __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, const T* __restrict__ cE,
-											  const T* __restrict__ cC, uint32_t n)
+											  const T* __restrict__ cC, uint32_t n, MassAcc<T>* acc_in = nullptr,
+											  MassAcc<T>* acc_out = nullptr)
 {
 	using V = typename Vec16<T>::type;
 	constexpr int VN = Vec16<T>::N;
@@ -358,6 +451,8 @@ __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, 
 			const int s = (q * VN + u) % ST;
 			if (k * VN + u < total)
 			{
+				if constexpr ((MC & kMcIn) != 0)
+					acc_in[s].add(vget<V, T>(v, u));
 				d[s] = dev::fmadd(vget<V, T>(e, u), d[s], vget<V, T>(v, u));
 				vset<V, T>(v, u, d[s]);
 			}
@@ -372,6 +467,8 @@ __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, 
 			{
 				d[s] = dev::fmadd(c[s], d[s], vget<V, T>(v, u)) * vget<V, T>(b, u);
 				vset<V, T>(v, u, d[s]);
+				if constexpr ((MC & kMcOut) != 0)
+					acc_out[s].add(d[s]);
 			}
 		}
 	};
@@ -468,16 +565,23 @@ __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, 
 	}
 }
 
-// Any S: one recurrence at a time, scalar shared-memory accesses.
-template <typename T>
+// Any S: one recurrence at a time, scalar shared-memory accesses.  MC adds
+// substrate s's input / output total of the row to mc_in[s] / mc_out[s] (FP64
+// atomics per row; a path for rare substrate counts).
+template <typename T, int MC = 0>
 __device__ __forceinline__ void solve_row_generic(T* row, const T* cB, const T* cE, const T* cC, uint32_t n,
-												  uint32_t S)
+												  uint32_t S, double* mc_in = nullptr, double* mc_out = nullptr)
 {
 	for (uint32_t s = 0; s < S; s++)
 	{
+		MassAcc<T> ai, ao;
+		ai.zero();
+		ao.zero();
 		T d = T(0);
 		for (uint32_t i = 0; i < n; i++)
 		{
+			if constexpr ((MC & kMcIn) != 0)
+				ai.add(row[i * S + s]);
 			d = dev::fmadd(__ldg(cE + i * S + s), d, row[i * S + s]);
 			row[i * S + s] = d;
 		}
@@ -487,7 +591,15 @@ __device__ __forceinline__ void solve_row_generic(T* row, const T* cB, const T* 
 		{
 			d = dev::fmadd(c, d, row[i * S + s]) * __ldg(cB + i * S + s);
 			row[i * S + s] = d;
+			if constexpr ((MC & kMcOut) != 0)
+				ao.add(d);
 		}
+		if constexpr ((MC & kMcIn) != 0)
+			if (mc_in)
+				atomicAdd(mc_in + s, ai.value());
+		if constexpr ((MC & kMcOut) != 0)
+			if (mc_out)
+				atomicAdd(mc_out + s, ao.value());
 	}
 }
 

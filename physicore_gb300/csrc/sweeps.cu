@@ -52,7 +52,12 @@ using namespace solvers;
 // runs without per-chunk bookkeeping.  Coefficients come from the compressed
 // tables (head rows, then per-substrate constants), so most points need no
 // coefficient load at all.
-template <typename T, int AXIS>
+//
+// MC = kMcOut (the step's last sweep with the mass check on): the lanes also sum
+// their solved values before the faces are written, into a.mc_tot[S + s].  A
+// lane's substrate is the same in every tile when S divides 32 (it then keeps one
+// running total and adds it once at the end), else it adds its total per tile.
+template <typename T, int AXIS, int MC>
 __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __grid_constant__ CUtensorMap tmap)
 {
 	extern __shared__ __align__(128) unsigned char smem[];
@@ -69,6 +74,10 @@ __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __g
 	}
 	__syncwarp();
 	bool ok = true;
+	MassAcc<T> acc;
+	acc.zero();
+	const bool per_tile = (kLanes % S) != 0;
+	const uint32_t classes = S < kLanes ? S : kLanes;
 	for (uint32_t phase = 0;; phase ^= 1)
 	{
 		uint32_t t32 = 0;
@@ -96,7 +105,13 @@ __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __g
 		ok = __all_sync(0xffffffffu, dev::mbar_wait(full, phase));
 		if (!ok)
 			break;
-		solve_line<T, kLanes>(base + lane, n, 0, L);
+		solve_line<T, kLanes, MC>(base + lane, n, 0, L, nullptr, &acc);
+		if constexpr ((MC & kMcOut) != 0)
+			if (per_tile)
+			{
+				flush_classes(acc.value(), classes, kLanes, a.mc_tot + S + ((uint64_t)x0 + lane) % S);
+				acc.zero();
+			}
 		if (a.face_mask)
 		{
 			FaceArgs f {};
@@ -123,6 +138,9 @@ __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __g
 		}
 		__syncwarp();
 	}
+	if constexpr ((MC & kMcOut) != 0)
+		if (!per_tile)
+			flush_classes(acc.value(), classes, kLanes, a.mc_tot + S + lane % S);
 	if (!ok && lane == 0)
 		atomicOr(a.err, DEV_ERR_WAIT_TIMEOUT);
 	if (lane == 0)
@@ -134,10 +152,21 @@ __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __g
 // Row-per-thread mapping: a tile is rows_per_tile consecutive rows and the CTA has
 // rows_per_tile * TPR threads (<= 32); TPR threads share a row when its substrates
 // fill whole 16-byte chunks.
-template <typename T, int ST>
+// MC = kMcIn | kMcOut (the mass check on): the threads also sum their rows'
+// inputs (and outputs on a 1-D mesh, where x is the last sweep) per substrate.
+template <typename T, int ST, int MC>
 __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 {
 	constexpr int TPR = x_tpr<T, ST>();
+	constexpr bool kChunks = ST > 0 && (ST * (int)sizeof(T)) % 16 == 0;
+	constexpr int NA = kChunks ? Vec16<T>::N : (ST > 0 ? ST : 1);
+	MassAcc<T> ai[NA], ao[NA];
+#pragma unroll
+	for (int u = 0; u < NA; u++)
+	{
+		ai[u].zero();
+		ao[u].zero();
+	}
 	extern __shared__ __align__(128) unsigned char smem[];
 	uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
 	uint32_t& ticket = *reinterpret_cast<uint32_t*>(smem + 8);
@@ -183,11 +212,11 @@ __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 		{
 			T* row = tile + r_local * a.smem_pitch;
 			if constexpr (ST == 0)
-				solve_row_generic<T>(row, cB, cE, cC, n, a.S);
-			else if constexpr ((ST * (int)sizeof(T)) % 16 == 0)
-				solve_row_chunks<T, TPR>(row, cB, cE, cC, n, h);
+				solve_row_generic<T, MC>(row, cB, cE, cC, n, a.S, a.mc_tot, a.mc_x_out ? a.mc_tot + a.S : nullptr);
+			else if constexpr (kChunks)
+				solve_row_chunks<T, TPR, MC>(row, cB, cE, cC, n, h, ai, ao);
 			else
-				solve_row_vec<T, ST>(row, cB, cE, cC, n);
+				solve_row_vec<T, ST, MC>(row, cB, cE, cC, n, ai, ao);
 		}
 		dev::fence_proxy_async_smem();
 		__syncthreads();
@@ -196,6 +225,18 @@ __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 		dev::bulk_commit();
 		dev::bulk_wait_read();
 		__syncthreads();
+	}
+	if constexpr (MC != 0 && ST > 0)
+	{
+		// thread r * TPR + h holds substrates h * VN + u (chunks) or u (one thread per row)
+#pragma unroll
+		for (int u = 0; u < NA; u++)
+		{
+			const uint32_t sub = kChunks ? (uint32_t)(h * Vec16<T>::N + u) : (uint32_t)u;
+			flush_classes(ai[u].value(), TPR, blockDim.x, a.mc_tot + sub);
+			if (a.mc_x_out)
+				flush_classes(ao[u].value(), TPR, blockDim.x, a.mc_tot + a.S + sub);
+		}
 	}
 	dev::bulk_wait_all();
 }
@@ -206,8 +247,10 @@ __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 // points need no coefficient load).  Row pitches are chosen so that the lanes of
 // a warp touch distinct banks.
 // ST = S when it is a compile-time constant (stride-S shared-memory accesses with
-// immediate offsets), 0 for the run-time path.
-template <typename T, int ST>
+// immediate offsets), 0 for the run-time path.  MC = kMcIn | kMcOut (the mass
+// check on): lane (r, s) also sums its lines' inputs (and outputs on a 1-D mesh)
+// over all its tiles, added once at the end.
+template <typename T, int ST, int MC>
 __global__ void __launch_bounds__(kLanes) sweep_x_sub_kernel(SweepArgs a)
 {
 	extern __shared__ __align__(128) unsigned char smem[];
@@ -219,6 +262,9 @@ __global__ void __launch_bounds__(kLanes) sweep_x_sub_kernel(SweepArgs a)
 	const uint32_t r_local = tid / S, s = tid % S;
 	const uint32_t row_bytes = (uint32_t)round_up(a.row_len * sizeof(T), 16);
 	const LineCoef<T> L = line_coef<T>(static_cast<const T*>(a.coef) + a.comp_off, S, a.head, n, s);
+	MassAcc<T> ai, ao;
+	ai.zero();
+	ao.zero();
 	if (tid == 0)
 	{
 		dev::mbar_init(bar, 1);
@@ -248,7 +294,7 @@ __global__ void __launch_bounds__(kLanes) sweep_x_sub_kernel(SweepArgs a)
 			break;
 		}
 		if (r_local < nrows)
-			solve_line<T, ST>(tile + r_local * a.smem_pitch + s, n, S, L);
+			solve_line<T, ST, MC>(tile + r_local * a.smem_pitch + s, n, S, L, &ai, &ao);
 		dev::fence_proxy_async_smem();
 		__syncthreads();
 		if (tid < nrows)
@@ -256,6 +302,13 @@ __global__ void __launch_bounds__(kLanes) sweep_x_sub_kernel(SweepArgs a)
 		dev::bulk_commit();
 		dev::bulk_wait_read();
 		__syncthreads();
+	}
+	if constexpr (MC != 0)
+	{
+		// lanes r * S + s share substrate s (S <= 32 on this mapping)
+		flush_classes(ai.value(), S, kLanes, a.mc_tot + s);
+		if (a.mc_x_out)
+			flush_classes(ao.value(), S, kLanes, a.mc_tot + S + s);
 	}
 	dev::bulk_wait_all();
 }
@@ -339,8 +392,37 @@ SweepArgs base_args(const Context* c, int axis)
 	return a;
 }
 
+template <typename T, int MC>
+int dispatch_sweep_x(Context* c, const SweepArgs& a, const Plan& p, bool sub)
+{
+	const double bytes = 2.0 * (double)(c->V * c->S) * (double)sizeof(T);
+	if (sub)
+		switch (c->S)
+		{
+		case 3: return launch_persistent(c, sweep_x_sub_kernel<T, 3, MC>, a, p, K_SWEEP_X, bytes);
+		case 4: return launch_persistent(c, sweep_x_sub_kernel<T, 4, MC>, a, p, K_SWEEP_X, bytes);
+		case 5: return launch_persistent(c, sweep_x_sub_kernel<T, 5, MC>, a, p, K_SWEEP_X, bytes);
+		case 6: return launch_persistent(c, sweep_x_sub_kernel<T, 6, MC>, a, p, K_SWEEP_X, bytes);
+		case 7: return launch_persistent(c, sweep_x_sub_kernel<T, 7, MC>, a, p, K_SWEEP_X, bytes);
+		case 8: return launch_persistent(c, sweep_x_sub_kernel<T, 8, MC>, a, p, K_SWEEP_X, bytes);
+		default: return launch_persistent(c, sweep_x_sub_kernel<T, 0, MC>, a, p, K_SWEEP_X, bytes);
+		}
+	switch (c->S)
+	{
+	case 1: return launch_persistent(c, sweep_x_kernel<T, 1, MC>, a, p, K_SWEEP_X, bytes);
+	case 2: return launch_persistent(c, sweep_x_kernel<T, 2, MC>, a, p, K_SWEEP_X, bytes);
+	case 3: return launch_persistent(c, sweep_x_kernel<T, 3, MC>, a, p, K_SWEEP_X, bytes);
+	case 4: return launch_persistent(c, sweep_x_kernel<T, 4, MC>, a, p, K_SWEEP_X, bytes);
+	case 5: return launch_persistent(c, sweep_x_kernel<T, 5, MC>, a, p, K_SWEEP_X, bytes);
+	case 6: return launch_persistent(c, sweep_x_kernel<T, 6, MC>, a, p, K_SWEEP_X, bytes);
+	case 7: return launch_persistent(c, sweep_x_kernel<T, 7, MC>, a, p, K_SWEEP_X, bytes);
+	case 8: return launch_persistent(c, sweep_x_kernel<T, 8, MC>, a, p, K_SWEEP_X, bytes);
+	default: return launch_persistent(c, sweep_x_kernel<T, 0, MC>, a, p, K_SWEEP_X, bytes);
+	}
+}
+
 template <typename T>
-int run_sweep_x(Context* c)
+int run_sweep_x(Context* c, bool mass_check)
 {
 	SweepArgs a = base_args(c, 0);
 	const bool sub = x_substrate_mapping(c->S);
@@ -352,36 +434,19 @@ int run_sweep_x(Context* c)
 		return fail(PCG_ERR_UNSUPPORTED, "x rows too long for the shared-memory x sweep");
 	a.rows_per_tile = (uint32_t)p.rows_per_tile;
 	a.tiles = (c->rows + p.rows_per_tile - 1) / p.rows_per_tile;
-	const double bytes = 2.0 * (double)(c->V * c->S) * (double)sizeof(T);
-	if (sub)
-		switch (c->S)
-		{
-		case 3: return launch_persistent(c, sweep_x_sub_kernel<T, 3>, a, p, K_SWEEP_X, bytes);
-		case 4: return launch_persistent(c, sweep_x_sub_kernel<T, 4>, a, p, K_SWEEP_X, bytes);
-		case 5: return launch_persistent(c, sweep_x_sub_kernel<T, 5>, a, p, K_SWEEP_X, bytes);
-		case 6: return launch_persistent(c, sweep_x_sub_kernel<T, 6>, a, p, K_SWEEP_X, bytes);
-		case 7: return launch_persistent(c, sweep_x_sub_kernel<T, 7>, a, p, K_SWEEP_X, bytes);
-		case 8: return launch_persistent(c, sweep_x_sub_kernel<T, 8>, a, p, K_SWEEP_X, bytes);
-		default: return launch_persistent(c, sweep_x_sub_kernel<T, 0>, a, p, K_SWEEP_X, bytes);
-		}
-	switch (c->S)
-	{
-	case 1: return launch_persistent(c, sweep_x_kernel<T, 1>, a, p, K_SWEEP_X, bytes);
-	case 2: return launch_persistent(c, sweep_x_kernel<T, 2>, a, p, K_SWEEP_X, bytes);
-	case 3: return launch_persistent(c, sweep_x_kernel<T, 3>, a, p, K_SWEEP_X, bytes);
-	case 4: return launch_persistent(c, sweep_x_kernel<T, 4>, a, p, K_SWEEP_X, bytes);
-	case 5: return launch_persistent(c, sweep_x_kernel<T, 5>, a, p, K_SWEEP_X, bytes);
-	case 6: return launch_persistent(c, sweep_x_kernel<T, 6>, a, p, K_SWEEP_X, bytes);
-	case 7: return launch_persistent(c, sweep_x_kernel<T, 7>, a, p, K_SWEEP_X, bytes);
-	case 8: return launch_persistent(c, sweep_x_kernel<T, 8>, a, p, K_SWEEP_X, bytes);
-	default: return launch_persistent(c, sweep_x_kernel<T, 0>, a, p, K_SWEEP_X, bytes);
-	}
+	if (!mass_check)
+		return dispatch_sweep_x<T, 0>(c, a, p, sub);
+	a.mc_tot = static_cast<double*>(c->mc_tot.ptr);
+	a.mc_x_out = c->dims == 1 ? 1u : 0u;
+	return dispatch_sweep_x<T, kMcIn | kMcOut>(c, a, p, sub);
 }
 
 template <typename T>
-int run_sweep_yz(Context* c, int axis, bool fuse_faces)
+int run_sweep_yz(Context* c, int axis, bool fuse_faces, bool mass_check)
 {
 	SweepArgs a = base_args(c, axis);
+	if (mass_check)
+		a.mc_tot = static_cast<double*>(c->mc_tot.ptr);
 	if (fuse_faces)
 	{
 		const FaceArgs f = make_face_args(c);
@@ -415,7 +480,8 @@ int run_sweep_yz(Context* c, int axis, bool fuse_faces)
 		return fail(PCG_ERR_INVALID, "tensor maps of the field were not prepared");
 	const int kid = axis == 1 ? K_SWEEP_Y : K_SWEEP_Z;
 	const double bytes = 2.0 * (double)(c->V * c->S) * (double)sizeof(T);
-	auto kernel = axis == 1 ? sweep_yz_kernel<T, 1> : sweep_yz_kernel<T, 2>;
+	auto kernel = mass_check ? (axis == 1 ? sweep_yz_kernel<T, 1, kMcOut> : sweep_yz_kernel<T, 2, kMcOut>)
+							 : (axis == 1 ? sweep_yz_kernel<T, 1, 0> : sweep_yz_kernel<T, 2, 0>);
 	PCG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem));
 	int per_sm = 0;
 	PCG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, p.threads, p.smem));
@@ -546,11 +612,15 @@ uint64_t sweep_smem_bytes(const Context* c, int axis)
 	return c->wsize == 4 ? plan<float>(c, axis).smem : plan<double>(c, axis).smem;
 }
 
-int launch_sweep_x(Context* c) { return c->wsize == 4 ? run_sweep_x<float>(c) : run_sweep_x<double>(c); }
-
-int launch_sweep_yz(Context* c, int axis, bool fuse_faces)
+int launch_sweep_x(Context* c, bool mass_check)
 {
-	return c->wsize == 4 ? run_sweep_yz<float>(c, axis, fuse_faces) : run_sweep_yz<double>(c, axis, fuse_faces);
+	return c->wsize == 4 ? run_sweep_x<float>(c, mass_check) : run_sweep_x<double>(c, mass_check);
+}
+
+int launch_sweep_yz(Context* c, int axis, bool fuse_faces, bool mass_check)
+{
+	return c->wsize == 4 ? run_sweep_yz<float>(c, axis, fuse_faces, mass_check)
+						 : run_sweep_yz<double>(c, axis, fuse_faces, mass_check);
 }
 
 bool faces_fusable(const Context* c) { return c->dims >= 2; }

@@ -63,3 +63,29 @@ def test_mass_check_never_enabled(pcg):
     g = W.apply(pcg.Solver(0), W.random_small(4))
     with pytest.raises(pcg.PcgError):
         g.get_mass_check()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_mass_check_many_substrates(pcg, oracle_mod, precision):
+    """40 substrates: the x sweep takes its row-per-thread path for any S (totals
+    added per row) and the y/z sweeps add per tile (40 does not divide 32)."""
+    rng = np.random.default_rng(77)
+    S, n = 40, (7, 6, 5)
+    p = dict(name="many_substrates", dims=3, bbmin=(0, 0, 0), bbmax=tuple(v * 20 for v in n), voxel=(20, 20, 20),
+             dt=0.01, D=np.geomspace(10.0, 1e5, S), decay=np.geomspace(1e-4, 1.0, S), initial=np.zeros(S),
+             field=rng.random((n[2], n[1], n[0], S)), field_layout="interleaved",
+             boundary=[(0, 0, rng.random(S), np.ones(S, np.uint8))], interior=None, bulk=None, agents=None,
+             compute_internalized=False)
+    g = W.apply(pcg.Solver(precision), p)
+    g.set_mass_check(True)
+    g.solve(STEPS)
+    chk = g.get_mass_check()
+    tol = 1e-12 if precision == 1 else 1e-5
+    assert chk["steps"] == STEPS and np.all(chk["worst"] <= tol), chk["worst"]
+    o = W.apply(oracle_mod.OracleSolver(threads=2), p)
+    o.solve(STEPS - 1)
+    before = o.mass()
+    o.run_phases(oracle_mod.PHASE_DIFFUSION, False)
+    after = o.mass()
+    assert np.all(np.abs(chk["before"] - before) <= tol * np.abs(before))
+    assert np.all(np.abs(chk["after"] - after) <= tol * np.abs(before))
