@@ -502,6 +502,7 @@ def run_gb300(args, w):
     if args.fp64:
         head["fp64"] = run_fp64(args, w, local, det)
         head["plain_100_fp64"] = run_plain_100(args, local, det)
+        head["s1_sweeps"] = run_s1(args, local, det)
     if args.batch_domains > 0:
         b = run_batched(args, local, ClockSampler)
         det.add("batched", b)
@@ -599,6 +600,33 @@ def run_fp64(args, w, local, det):
     out = {"value": vss / (ms / 1e3), "ms_per_step": round(ms, 4), "step_gbps": round(gbs, 1),
            "frac": round(gbs / peak, 4), "steps": k}
     det.add("fp64_large", dict(out, kernels=kernel_table(stats)))
+    return out
+
+
+def run_s1(args, local, det):
+    """One substrate at 320^3 in FP32 (x sweep on its row-per-thread path, y/z tiles
+    of 32 voxels): per-kernel device times and achieved bandwidth."""
+    import physicore_gb300 as pcg
+    from physicore_gb300 import workloads as W
+    p = W.large(seed=5, n=args.n, S=1, agents=0, interior=0)
+    p["agents"] = None
+    s = W.apply(pcg.Solver(pcg.FP32, device=local), p)
+    del p
+    for _ in range(3):
+        s.solve(1)
+    s.synchronize()
+    s.set_kernel_timing(True)
+    s.reset_kernel_stats()
+    steps = max(3, min(args.steps, 30))
+    for _ in range(steps):
+        s.solve(1)
+    s.synchronize()
+    kt = kernel_table(s.kernel_stats())
+    s.close()
+    peak, _ = measured_peaks()
+    out = {k: {"us": v["us_per_launch"], "gbps": v["gbps"], "frac": round(v["gbps"] / peak, 4)}
+           for k, v in kt.items() if k.startswith("sweep")}
+    det.add("s1_320", {"workload": f"{args.n}^3 x 1 substrate FP32, x faces Dirichlet, no agents", "kernels": kt})
     return out
 
 

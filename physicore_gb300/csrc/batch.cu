@@ -81,6 +81,7 @@ struct BatchDomain
 	const void* coef[3];
 	uint64_t coef_len[3];
 	uint64_t coef_comp_off[3]; // compressed tables (elements into coef)
+	uint64_t coef_blo_off[3];  // FP32: full tables of the multipliers' lo parts (elements into coef)
 	uint32_t coef_head[3];     // head points of the compressed tables
 	FaceArgs faces;
 	const uint64_t* dir_offsets;
@@ -91,6 +92,10 @@ struct BatchDomain
 	const void* bulk[3];
 	double dt;
 	CellArgs cells;
+	// per-step mass check of this domain (null when off): FP64 totals [before S |
+	// after S] added by the sweeps, and [before | after | worst | factor] x S
+	double* mc_tot;
+	double* mc_out;
 };
 
 // Entry k of a list covers units [base[k], base[k+1]) of domain dom[k].
@@ -162,10 +167,13 @@ __device__ __forceinline__ void fence_tensormap_acquire(const void* map)
 // coefficients are loaded together; there is no cross-group prefetch, which keeps
 // every substrate variant light enough to share one kernel (batched tiles are
 // small, so many CTAs per SM hide the latency instead).
-template <typename T, int ST>
+// MC adds substrate s's inputs / outputs to acc_in[s] / acc_out[s].
+template <typename T, int ST, int MC = 0>
 __device__ __forceinline__ void solve_row_lite(T* row, const T* __restrict__ cB, const T* __restrict__ cE,
-											   const T* __restrict__ cC, uint32_t n)
+											   const T* __restrict__ cC, const T* __restrict__ cBl, uint32_t n,
+											   MassAcc<T>* acc_in = nullptr, MassAcc<T>* acc_out = nullptr)
 {
+	constexpr bool kLo = sizeof(T) == 4;
 	using V = typename Vec16<T>::type;
 	constexpr int VN = Vec16<T>::N;
 	constexpr int GE = group_elems(ST, VN);
@@ -199,6 +207,8 @@ __device__ __forceinline__ void solve_row_lite(T* row, const T* __restrict__ cB,
 				const int s = (q * VN + u) % ST;
 				if (g * GE + q * VN + u < total)
 				{
+					if constexpr ((MC & kMcIn) != 0)
+						acc_in[s].add(vget<V, T>(x[q], u));
 					d[s] = dev::fmadd(vget<V, T>(e[q], u), d[s], vget<V, T>(x[q], u));
 					vset<V, T>(x[q], u, d[s]);
 				}
@@ -212,12 +222,14 @@ __device__ __forceinline__ void solve_row_lite(T* row, const T* __restrict__ cB,
 		d[s] = T(0);
 	for (int g = (int)groups - 1; g >= 0; g--)
 	{
-		V x[U], bb[U];
+		V x[U], bb[U], bl[U];
 #pragma unroll
 		for (int q = 0; q < U; q++)
 		{
 			x[q] = vrow[g * U + q];
 			bb[q] = __ldg(vB + g * U + q);
+			if constexpr (kLo)
+				bl[q] = __ldg(reinterpret_cast<const V*>(cBl) + g * U + q);
 		}
 #pragma unroll
 		for (int q = U - 1; q >= 0; q--)
@@ -227,8 +239,11 @@ __device__ __forceinline__ void solve_row_lite(T* row, const T* __restrict__ cB,
 				const int s = (q * VN + u) % ST;
 				if ((uint32_t)g * GE + q * VN + u < total)
 				{
-					d[s] = dev::fmadd(c[s], d[s], vget<V, T>(x[q], u)) * vget<V, T>(bb[q], u);
+					d[s] = bwd_step(c[s], d[s], vget<V, T>(x[q], u), vget<V, T>(bb[q], u),
+									kLo ? vget<V, T>(bl[q], u) : T(0));
 					vset<V, T>(x[q], u, d[s]);
+					if constexpr ((MC & kMcOut) != 0)
+						acc_out[s].add(d[s]);
 				}
 			}
 #pragma unroll
@@ -237,25 +252,61 @@ __device__ __forceinline__ void solve_row_lite(T* row, const T* __restrict__ cB,
 	}
 }
 
-template <typename T>
-__device__ __forceinline__ void solve_x_row(T* row, const T* cB, const T* cE, const T* cC, uint32_t n, uint32_t S)
+// One row per thread; `active` threads hold a row.  With MC every thread of the
+// warp calls it (the mass totals are summed across the warp): the rows' input
+// totals go to mc_in[s] and, when mc_out is given (x is the domain's last
+// sweep), their output totals to mc_out[s].
+template <typename T, int ST, int MC>
+__device__ __forceinline__ void solve_x_row_st(T* row, const T* cB, const T* cE, const T* cC, const T* cBl, uint32_t n,
+											   bool active, double* mc_in, double* mc_out)
+{
+	MassAcc<T> ai[ST], ao[ST];
+#pragma unroll
+	for (int s = 0; s < ST; s++)
+	{
+		ai[s].zero();
+		ao[s].zero();
+	}
+	if (active)
+		solve_row_lite<T, ST, MC>(row, cB, cE, cC, cBl, n, ai, ao);
+	if constexpr (MC != 0)
+	{
+#pragma unroll
+		for (int s = 0; s < ST; s++)
+		{
+			if (mc_in)
+				flush_classes(ai[s].value(), 1, kLanes, mc_in + s);
+			if (mc_out)
+				flush_classes(ao[s].value(), 1, kLanes, mc_out + s);
+		}
+	}
+}
+
+template <typename T, int MC>
+__device__ __forceinline__ void solve_x_row(T* row, const T* cB, const T* cE, const T* cC, const T* cBl, uint32_t n,
+											uint32_t S, bool active, double* mc_in, double* mc_out)
 {
 	switch (S)
 	{
-	case 1: solve_row_lite<T, 1>(row, cB, cE, cC, n); break;
-	case 2: solve_row_lite<T, 2>(row, cB, cE, cC, n); break;
-	case 3: solve_row_lite<T, 3>(row, cB, cE, cC, n); break;
-	case 4: solve_row_lite<T, 4>(row, cB, cE, cC, n); break;
-	case 5: solve_row_lite<T, 5>(row, cB, cE, cC, n); break;
-	case 6: solve_row_lite<T, 6>(row, cB, cE, cC, n); break;
-	case 7: solve_row_lite<T, 7>(row, cB, cE, cC, n); break;
-	case 8: solve_row_lite<T, 8>(row, cB, cE, cC, n); break;
-	default: solve_row_generic<T>(row, cB, cE, cC, n, S); break;
+	case 1: solve_x_row_st<T, 1, MC>(row, cB, cE, cC, cBl, n, active, mc_in, mc_out); break;
+	case 2: solve_x_row_st<T, 2, MC>(row, cB, cE, cC, cBl, n, active, mc_in, mc_out); break;
+	case 3: solve_x_row_st<T, 3, MC>(row, cB, cE, cC, cBl, n, active, mc_in, mc_out); break;
+	case 4: solve_x_row_st<T, 4, MC>(row, cB, cE, cC, cBl, n, active, mc_in, mc_out); break;
+	case 5: solve_x_row_st<T, 5, MC>(row, cB, cE, cC, cBl, n, active, mc_in, mc_out); break;
+	case 6: solve_x_row_st<T, 6, MC>(row, cB, cE, cC, cBl, n, active, mc_in, mc_out); break;
+	case 7: solve_x_row_st<T, 7, MC>(row, cB, cE, cC, cBl, n, active, mc_in, mc_out); break;
+	case 8: solve_x_row_st<T, 8, MC>(row, cB, cE, cC, cBl, n, active, mc_in, mc_out); break;
+	default:
+		if (active)
+			solve_row_generic<T, MC>(row, cB, cE, cC, cBl, n, S, mc_in, mc_out);
+		break;
 	}
 }
 
 // x: a tile is x_rows whole rows of one domain, bulk-copied into shared memory.
-template <typename T>
+// MC (mass check in this batch): for domains with the check on, the tile's input
+// totals (and output totals when x is the domain's last sweep) go to its mc_tot.
+template <typename T, int MC>
 __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 {
 	extern __shared__ __align__(128) unsigned char smem[];
@@ -305,6 +356,7 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 		const T* cB = static_cast<const T*>(D.coef[0]);
 		const T* cE = cB + D.coef_len[0];
 		const T* cC = cE + D.coef_len[0];
+		const T* cBl = sizeof(T) == 4 ? cB + D.coef_blo_off[0] : nullptr;
 		const uint32_t rl = tid / S, s = tid % S;
 		LineCoef<T> L {};
 		if (D.x_mode != kMapRow) // coefficient loads overlap the tile's arrival
@@ -316,13 +368,26 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 				report(b, DEV_ERR_WAIT_TIMEOUT, di);
 			return;
 		}
+		double* mc_in = MC != 0 ? D.mc_tot : nullptr;
+		double* mc_out = MC != 0 && D.mc_tot && D.dims == 1 ? D.mc_tot + S : nullptr;
 		if (D.x_mode == kMapRow)
+			solve_x_row<T, MC>(tile + tid * spitch, cB, cE, cC, cBl, n, S, tid < nrows, mc_in, mc_out);
+		else
 		{
-			if (tid < nrows)
-				solve_x_row<T>(tile + tid * spitch, cB, cE, cC, n, S);
+			MassAcc<T> ai, ao;
+			ai.zero();
+			ao.zero();
+			if (rl < nrows)
+				solve_line<T, 0, MC>(tile + rl * spitch + s, n, S, L, &ai, &ao);
+			if constexpr (MC != 0)
+			{
+				// lanes rl * S + s share substrate s (S <= 32 on this mapping)
+				if (mc_in)
+					flush_classes(ai.value(), S, kLanes, mc_in + s % S);
+				if (mc_out)
+					flush_classes(ao.value(), S, kLanes, mc_out + s % S);
+			}
 		}
-		else if (rl < nrows)
-			solve_line<T, 0>(tile + rl * spitch + s, n, S, L);
 		dev::fence_proxy_async_smem();
 		__syncthreads();
 		if (tid < nrows)
@@ -339,7 +404,9 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 // set of one domain; its boxes arrive through the domain's tensor map on one
 // mbarrier, the warp solves it in place, and the boxes are stored back before the
 // next tile is requested (several single-warp CTAs per SM overlap these phases).
-template <typename T, int AXIS>
+// MC (mass check in this batch): on the domain's last sweep, each tile's solved
+// totals (before its faces are written) go to the domain's mc_tot.
+template <typename T, int AXIS, int MC>
 __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 {
 	extern __shared__ __align__(128) unsigned char smem[];
@@ -419,7 +486,13 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 				L = line_coef<T>(comp, S, D.coef_head[AXIS], n,
 								 (uint64_t)(x0 + lane) < D.row_len ? (uint32_t)((x0 + lane) % S) : 0);
 			}
-			solve_line<T, kLanes>(base + j * tile_elems + lane, n, 0, L);
+			MassAcc<T> acc;
+			acc.zero();
+			solve_line<T, kLanes, MC>(base + j * tile_elems + lane, n, 0, L, nullptr, &acc);
+			if constexpr (MC != 0)
+				if (D.mc_tot && D.dims == AXIS + 1)
+					flush_classes(acc.value(), S < kLanes ? S : kLanes, kLanes,
+								  D.mc_tot + S + ((uint64_t)x0 + lane) % S);
 			// the last sweep of the domain writes its boundary faces (the batch's
 			// Dirichlet launch then covers interior nodes and 1-D domains only)
 			if (D.dims == AXIS + 1)
@@ -648,6 +721,30 @@ __global__ void batch_cells_internalize_kernel(BatchArgs b, const uint32_t* __re
 		agent_internalize<T>(a, __ldg(a.shared + j));
 }
 
+// After the sweeps of a step: for every domain with the mass check on that runs
+// this step, the masses before and after its sweeps, the worst residual of
+// after * factor = before, and its totals cleared for the next step.
+__global__ void batch_mass_finish_kernel(const BatchDomain* doms, const uint32_t* steps_left, uint32_t count)
+{
+	for (uint32_t d = blockIdx.x; d < count; d += gridDim.x)
+	{
+		const BatchDomain& D = doms[d];
+		if (!D.mc_tot || !steps_left[d])
+			continue;
+		const uint32_t S = D.S;
+		for (uint32_t s = threadIdx.x; s < S; s += blockDim.x)
+		{
+			const double bf = D.mc_tot[s], af = D.mc_tot[S + s];
+			D.mc_out[s] = bf;
+			D.mc_out[S + s] = af;
+			const double res = fabs(af * D.mc_out[3 * S + s] - bf) / fmax(fabs(bf), 1e-300);
+			D.mc_out[2 * S + s] = fmax(D.mc_out[2 * S + s], res);
+			D.mc_tot[s] = 0.0;
+			D.mc_tot[S + s] = 0.0;
+		}
+	}
+}
+
 // End of a step: one step fewer for every domain still running.
 __global__ void batch_count_step_kernel(uint32_t* steps_left, uint32_t count)
 {
@@ -782,6 +879,7 @@ struct pcg_batch
 	unsigned grid[3] = { 0, 0, 0 };
 	int max_dims = 0;
 	bool built = false;
+	bool any_mass_check = false; // some domain has the per-step mass check on
 
 	std::vector<uint8_t> h_recompute, dev_recompute;
 	bool dev_recompute_valid = false;
@@ -892,6 +990,7 @@ BatchDomain describe_domain(pcg_batch* b, size_t d)
 	for (int a = 0; a < c->dims; a++)
 	{
 		D.coef_comp_off[a] = c->coef_comp_off[a];
+		D.coef_blo_off[a] = c->coef_blo_off[a];
 		D.coef_head[a] = c->coef_head[a];
 	}
 	D.faces = make_face_args(c);
@@ -905,6 +1004,11 @@ BatchDomain describe_domain(pcg_batch* b, size_t d)
 	D.dt = c->dt;
 	D.cells = make_cell_args(c);
 	D.cells.err = static_cast<uint32_t*>(b->d_err.ptr);
+	if (c->mass_check && c->mc_tot.ptr && c->mc_out.ptr)
+	{
+		D.mc_tot = static_cast<double*>(c->mc_tot.ptr);
+		D.mc_out = static_cast<double*>(c->mc_out.ptr);
+	}
 	return D;
 }
 
@@ -1046,8 +1150,12 @@ int encode_maps(pcg_batch* b, size_t d)
 int upload_domains(pcg_batch* b)
 {
 	const size_t N = b->ctx.size();
+	b->any_mass_check = false;
 	for (size_t d = 0; d < N; d++)
+	{
 		b->h_doms[d] = describe_domain(b, d);
+		b->any_mass_check |= b->h_doms[d].mc_tot != nullptr;
+	}
 	// y/z: every CTA's buffer holds the batch's largest tile, so a short-line
 	// domain groups its tiles up to that size (at least kGroupBytes) instead of
 	// leaving most of the buffer empty
@@ -1110,13 +1218,16 @@ uint64_t sweep_smem(pcg_batch* b, int axis, const std::vector<size_t>& subset)
 }
 
 template <typename T>
-const void* sweep_kernel(int axis)
+const void* sweep_kernel(int axis, bool mass_check)
 {
 	if (axis == 0)
-		return reinterpret_cast<const void*>(batch_sweep_x_kernel<T>);
+		return mass_check ? reinterpret_cast<const void*>(batch_sweep_x_kernel<T, kMcIn | kMcOut>)
+						  : reinterpret_cast<const void*>(batch_sweep_x_kernel<T, 0>);
 	if (axis == 1)
-		return reinterpret_cast<const void*>(batch_sweep_yz_kernel<T, 1>);
-	return reinterpret_cast<const void*>(batch_sweep_yz_kernel<T, 2>);
+		return mass_check ? reinterpret_cast<const void*>(batch_sweep_yz_kernel<T, 1, kMcOut>)
+						  : reinterpret_cast<const void*>(batch_sweep_yz_kernel<T, 1, 0>);
+	return mass_check ? reinterpret_cast<const void*>(batch_sweep_yz_kernel<T, 2, kMcOut>)
+					  : reinterpret_cast<const void*>(batch_sweep_yz_kernel<T, 2, 0>);
 }
 
 // The dynamic shared-memory limit of a batched sweep kernel only ever grows, so
@@ -1139,12 +1250,13 @@ int raise_smem_limit(const void* k, int device, uint64_t smem)
 template <typename T>
 int sweep_grid(pcg_batch* b, int axis, uint64_t smem, uint64_t tiles, unsigned* grid)
 {
-	const void* k = sweep_kernel<T>(axis);
+	const void* k = sweep_kernel<T>(axis, b->any_mass_check);
 	if (smem > kMaxSmemBytes)
 		return fail(PCG_ERR_UNSUPPORTED, "a batched sweep tile exceeds shared memory");
-	int rc = raise_smem_limit(k, b->device, smem);
-	if (rc)
-		return rc;
+	int rc;
+	for (int mc = 0; mc < 2; mc++) // both variants: a later call may switch the check
+		if ((rc = raise_smem_limit(sweep_kernel<T>(axis, mc != 0), b->device, smem)))
+			return rc;
 	int per_sm = 0;
 	PCG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kLanes, smem));
 	if (per_sm < 1)
@@ -1218,6 +1330,8 @@ int build_t(pcg_batch* b)
 		b->step_bytes[K_DIRICHLET_INTERIOR] += (double)c->K * (8 + S * (2 * w + 1));
 		if (c->bulk_mode != PCG_BULK_NONE)
 			b->step_bytes[K_BULK] += V * S * w * (c->bulk_mode == PCG_BULK_PER_VOXEL ? 5.0 : 2.0);
+		if (b->h_doms[d].mc_tot)
+			b->step_bytes[K_MASS_CHECK] += 6 * S * 8;
 		if (c->A)
 		{
 			b->rebuild_bytes[d] = { 4.0 * V, A * (8.0 * c->dims + 1 + 5 * S * 8 + 8 + 6 * S * w + 4), A * 12,
@@ -1314,12 +1428,15 @@ template <typename T>
 int launch_sweep(pcg_batch* b, int axis, const BatchArgs& a, unsigned grid, uint64_t smem, double bytes)
 {
 	LaunchScope s(b, axis == 0 ? K_SWEEP_X : axis == 1 ? K_SWEEP_Y : K_SWEEP_Z, bytes);
+	const bool mc = b->any_mass_check;
 	if (axis == 0)
-		batch_sweep_x_kernel<T><<<grid, kLanes, smem, b->stream>>>(a);
+		(mc ? batch_sweep_x_kernel<T, kMcIn | kMcOut> : batch_sweep_x_kernel<T, 0>)<<<grid, kLanes, smem, b->stream>>>(a);
 	else if (axis == 1)
-		batch_sweep_yz_kernel<T, 1><<<grid, kLanes, smem, b->stream>>>(a);
+		(mc ? batch_sweep_yz_kernel<T, 1, kMcOut>
+			: batch_sweep_yz_kernel<T, 1, 0>)<<<grid, kLanes, smem, b->stream>>>(a);
 	else
-		batch_sweep_yz_kernel<T, 2><<<grid, kLanes, smem, b->stream>>>(a);
+		(mc ? batch_sweep_yz_kernel<T, 2, kMcOut>
+			: batch_sweep_yz_kernel<T, 2, 0>)<<<grid, kLanes, smem, b->stream>>>(a);
 	PCG_CUDA_TRY(cudaGetLastError());
 	return PCG_OK;
 }
@@ -1335,6 +1452,14 @@ int launch_step(pcg_batch* b)
 		if (b->lists[axis].total && (rc = launch_sweep<T>(b, axis, args_for(b, axis, axis), b->grid[axis],
 														   b->smem[axis], sb[K_SWEEP_X + axis])))
 			return rc;
+	if (b->any_mass_check)
+	{
+		LaunchScope s(b, K_MASS_CHECK, sb[K_MASS_CHECK]);
+		const uint32_t N = (uint32_t)b->ctx.size();
+		batch_mass_finish_kernel<<<std::min<uint32_t>(N, 1024), 32, 0, b->stream>>>(
+			static_cast<const BatchDomain*>(b->d_doms.ptr), static_cast<const uint32_t*>(b->d_steps_left.ptr), N);
+		PCG_CUDA_TRY(cudaGetLastError());
+	}
 	if (b->lists[L_FACES].total)
 	{
 		LaunchScope s(b, K_DIRICHLET_FACES, sb[K_DIRICHLET_FACES]);
@@ -1963,8 +2088,13 @@ int pcg_batch_solve_budgets(pcg_batch* b, uint64_t iterations, const uint64_t* b
 			return rc;
 	}
 	for (size_t d = 0; d < b->ctx.size(); d++)
+	{
+		Context* c = static_cast<Context*>(b->ctx[d]);
 		if (!budgets || budgets[d] > 0)
-			static_cast<Context*>(b->ctx[d])->recompute_cells = false;
+			c->recompute_cells = false;
+		if (b->h_doms[d].mc_tot)
+			c->mass_checked_steps += b->h_steps_left[d];
+	}
 	return pcg::sync_out(b);
 }
 

@@ -32,7 +32,7 @@ const char* kernel_name(int id)
 	static const char* names[K_COUNT] = { "sweep_x",	  "sweep_y",		"sweep_z",	   "dirichlet_faces",
 										  "dirichlet_interior", "bulk", "cells_locate", "cells_ballot",
 										  "cells_reduce", "cells_apply", "cells_internalize", "cells_release",
-										  "mass",		  "layout", "cells_clear", "mass_check" };
+										  "mass",		  "layout", "cells_clear", "mass_check", "cells_group" };
 	return (id >= 0 && id < K_COUNT) ? names[id] : "?";
 }
 
@@ -238,23 +238,32 @@ void launch_begin(Context* c, int kid, double bytes, cudaEvent_t* ev)
 	}
 }
 
-void launch_end(Context* c, int kid, cudaEvent_t ev)
+void launch_end(Context* c, int kid, cudaEvent_t ev, double per_shared)
 {
 	if (!c->timing || !ev)
 		return;
 	cudaEvent_t stop = get_event(c);
 	cudaEventRecord(stop, c->stream);
-	c->pending.push_back({ kid, ev, stop });
+	c->pending.push_back({ kid, ev, stop, per_shared });
 }
 
+// In timing mode the cell step copies the number of agents in shared voxels to a
+// pinned word after every ballot; launches whose work is those agents add their
+// bytes per agent times that number once their events have completed.
 void collect_timings(Context* c)
 {
+	if (!c->pending.empty() && c->h_words)
+	{
+		cudaEventSynchronize(c->pending.back().b);
+		c->shared_agents = c->h_words[2];
+	}
 	for (auto& p : c->pending)
 	{
 		cudaEventSynchronize(p.b);
 		float ms = 0;
 		cudaEventElapsedTime(&ms, p.a, p.b);
 		c->stats[p.kid].total_ms += ms;
+		c->stats[p.kid].bytes += p.per_shared * c->shared_agents;
 		c->event_pool.push_back(p.a);
 		c->event_pool.push_back(p.b);
 	}
@@ -332,22 +341,67 @@ static void precompute_axis(uint64_t n, uint64_t S, uint64_t shape, uint64_t dim
 		}
 }
 
+// FP32 backward multipliers that keep the sweep's mass exact.  The FP32 solve uses
+// E = e and C = c rounded to FP32; the tridiagonal matrix that this factorisation
+// inverts is then M' = L'U' with L'[i][i-1] = -E[i-1] and U' = diag(1/B) - C on the
+// superdiagonal, whose column j sums to (1 - E[j]) / B[j] + E[j-1] C - C (the last
+// two terms for j > 0; E[n-1] = 0).  Choosing B[j] (in FP64) so that every column
+// sums exactly to the reference matrix's column sum (diffusion_solver.cpp:29-86:
+// the diagonal minus r for each neighbour) makes M' conserve mass exactly as the
+// reference does; with the exact e and c it gives b'[j] itself.  FP32 rounding of
+// b', e and c otherwise biases every step the same way, and over hundreds of steps
+// that drift dominates the FP32 error.  B is applied as a pair hi + lo with one
+// rounding (d = fma(t, hi, t * lo)).
+static void colsum_multipliers(uint64_t n, uint64_t S, uint64_t shape, uint64_t dims, double dt, const double* D,
+							   const double* decay, const std::vector<double>& e, const std::vector<double>& cc,
+							   std::vector<double>& B)
+{
+	const double h2 = (double)(shape * shape);
+	B.assign(n * S, 0.0);
+	for (uint64_t s = 0; s < S; s++)
+	{
+		const double r = dt * D[s] / h2;
+		const double C = (double)(float)cc[s];
+		for (uint64_t j = 0; j < n; j++)
+		{
+			double diag = 1 + decay[s] * dt / (double)dims + 2 * dt * D[s] / h2;
+			if (j == 0 || j == n - 1)
+				diag -= dt * D[s] / h2;
+			const double kappa = diag - (j > 0 ? r : 0.0) - (j + 1 < n ? r : 0.0);
+			const double Ej = j + 1 < n ? (double)(float)e[j * S + s] : 0.0;
+			const double Em = j > 0 ? (double)(float)e[(j - 1) * S + s] : 0.0;
+			B[j * S + s] = (1.0 - Ej) / (kappa - Em * C + (j > 0 ? C : 0.0));
+		}
+	}
+}
+
 // Device coefficient table of one axis: [B | E | C], C[s] = c.  For x, B and E are
 // flat in the field's (i, s) order, B[i*S+s] = b'_i, E[i*S+s] = e_{i-1} (0 at i = 0),
 // so a 16-byte chunk of coefficients matches a chunk of a row.  For y and z they are
 // per-substrate rows, B[s*cp + i], padded to cp = a multiple of the solver block.
+// FP32 tables hold the column-sum-exact multipliers as hi + lo (colsum_multipliers):
+// B is the hi part and a B_lo table of the same layout follows C.
 template <typename T>
 static int upload_coefficients(Context* c)
 {
 	const uint64_t S = c->S;
+	constexpr bool kLo = sizeof(T) == 4;
 	for (int axis = 0; axis < c->dims; axis++)
 	{
 		const uint64_t n = c->n[axis];
-		std::vector<double> b, e, cc;
+		std::vector<double> b, e, cc, B;
 		precompute_axis(n, S, c->voxel[axis], (uint64_t)c->dims, c->dt, c->D.data(), c->decay.data(), b, e, cc);
+		if (kLo)
+		{
+			colsum_multipliers(n, S, c->voxel[axis], (uint64_t)c->dims, c->dt, c->D.data(), c->decay.data(), e, cc,
+							   B);
+			b = B;
+		}
+		auto lo = [&](uint64_t k) { return kLo ? (T)(b[k] - (double)(T)b[k]) : T(0); };
 		const uint64_t cp = coef_row_pitch(n);
 		const uint64_t len = axis == 0 ? coef_table_len(n, S, sizeof(T)) : S * cp;
-		const uint64_t total = 2 * len + round_up(S, 16 / sizeof(T));
+		const uint64_t blo_off = 2 * len + round_up(S, 16 / sizeof(T));
+		const uint64_t total = blo_off + (kLo ? len : 0);
 		// Compressed tables.  b'_i and e_i converge to a constant within a few
 		// points, so a line needs only a head of H points (the first index from which
 		// every stored value up to n-2 equals the value at n-2, rounded up to the solver
@@ -364,12 +418,13 @@ static int upload_coefficients(Context* c)
 					const T bm = (T)b[(n - 2) * S + sub];
 					const T em = n >= 3 ? (T)e[(n - 3) * S + sub] : T(0);
 					h = n - 2;
+					const T blm = lo((n - 2) * S + sub);
 					while (h > 0)
 					{
 						const uint64_t i = h - 1;
 						const T bi = (T)b[i * S + sub];
 						const T ei = i == 0 ? T(0) : (T)e[(i - 1) * S + sub];
-						if (bi != bm || ei != em)
+						if (bi != bm || ei != em || lo(i * S + sub) != blm)
 							break;
 						h = i;
 					}
@@ -381,10 +436,11 @@ static int upload_coefficients(Context* c)
 				H = round_up(n, kBlockPoints); // the whole line lives in the head
 		}
 		const uint64_t kS = round_up(S, vn);
-		const uint64_t comp_total = 2 * S * H + 5 * kS;
+		const uint64_t comp_total = 2 * S * H + 5 * kS + (kLo ? S * H + 2 * kS : 0);
 		c->coef_len[axis] = len;
 		c->coef_elems[axis] = total;
 		c->coef_comp_off[axis] = total;
+		c->coef_blo_off[axis] = kLo ? blo_off : 0;
 		c->coef_head[axis] = (uint32_t)H;
 		std::vector<T> tab(total + comp_total, T(0));
 		for (uint64_t i = 0; i < n; i++)
@@ -393,6 +449,8 @@ static int upload_coefficients(Context* c)
 				const uint64_t at = axis == 0 ? i * S + s : s * cp + i;
 				tab[at] = (T)b[i * S + s];
 				tab[len + at] = i == 0 ? T(0) : (T)e[(i - 1) * S + s];
+				if (kLo)
+					tab[blo_off + at] = lo(i * S + s);
 			}
 		for (uint64_t s = 0; s < S; s++)
 			tab[2 * len + s] = (T)cc[s];
@@ -400,12 +458,16 @@ static int upload_coefficients(Context* c)
 			T* hB = tab.data() + total;
 			T* hE = hB + S * H;
 			T* k = hE + S * H; // [mid b' | mid e | last b' | last e | c], each kS long
+			T* hBl = k + 5 * kS; // FP32: [head b' lo | mid b' lo | last b' lo]
+			T* kl = hBl + S * H;
 			for (uint64_t sub = 0; sub < S; sub++)
 			{
 				for (uint64_t i = 0; i < std::min(H, n); i++)
 				{
 					hB[sub * H + i] = (T)b[i * S + sub];
 					hE[sub * H + i] = i == 0 ? T(0) : (T)e[(i - 1) * S + sub];
+					if (kLo)
+						hBl[sub * H + i] = lo(i * S + sub);
 				}
 				const uint64_t m = n >= 2 ? n - 2 : 0;
 				k[sub] = (T)b[m * S + sub];
@@ -413,6 +475,11 @@ static int upload_coefficients(Context* c)
 				k[2 * kS + sub] = (T)b[(n - 1) * S + sub];
 				k[3 * kS + sub] = n == 1 ? T(0) : (T)e[(n - 2) * S + sub];
 				k[4 * kS + sub] = (T)cc[sub];
+				if (kLo)
+				{
+					kl[sub] = lo(m * S + sub);
+					kl[kS + sub] = lo((n - 1) * S + sub);
+				}
 			}
 		}
 		int rc = dalloc(c, c->coef[axis], tab.size() * sizeof(T));
@@ -703,6 +770,10 @@ static int alloc_agents(Context* c, uint64_t A)
 		return rc;
 	if ((rc = dalloc(c, c->a_shared, std::max<uint64_t>(A, 1) * sizeof(uint32_t))))
 		return rc;
+	if ((rc = dalloc(c, c->a_rank, std::max<uint64_t>(A, 1) * sizeof(uint32_t))))
+		return rc;
+	if ((rc = dalloc(c, c->a_sorted, std::max<uint64_t>(A, 1) * sizeof(uint32_t))))
+		return rc;
 	DeviceBuffer* rs[] = { &c->a_num, &c->a_den, &c->a_fac, &c->a_rnum, &c->a_rden, &c->a_rfac };
 	for (DeviceBuffer* b : rs)
 		if ((rc = dalloc(c, *b, std::max<uint64_t>(A * S, 1) * w)))
@@ -796,8 +867,8 @@ uint64_t estimate_device_bytes(const Context* c)
 	const uint64_t row_len = c->n[0] * S, pitch = round_up(row_len, 32 / w), rows = c->n[1] * c->n[2];
 	uint64_t b = rows * pitch * w;               // field
 	b += V * S * w;                              // staging of pcg_get_field / pcg_set_field
-	for (int a = 0; a < c->dims; a++)            // coefficient tables (full and compressed)
-		b += (4 * c->n[a] * S + 64 * S + 64) * w;
+	for (int a = 0; a < c->dims; a++)            // coefficient tables (full and compressed; FP32: with lo parts)
+		b += (7 * c->n[a] * S + 96 * S + 64) * w;
 	b += 3 * 256 + 2 * S * 8;                    // words, mass
 	b += c->K * (8 + S * (w + 1)) + 12 * S * (w + 1);
 	if (c->bulk_mode == PCG_BULK_UNIFORM)
@@ -805,7 +876,7 @@ uint64_t estimate_device_bytes(const Context* c)
 	else if (c->bulk_mode == PCG_BULK_PER_VOXEL)
 		b += 3 * rows * pitch * w;
 	if (A)
-		b += A * (c->dims * 8 + 6 * S * 8 + 8 + 1 + 8 + 5 + 6 * S * w) + V * 8;
+		b += A * (c->dims * 8 + 6 * S * 8 + 8 + 1 + 8 + 5 + 8 + 6 * S * w) + V * 8;
 	return b;
 }
 
@@ -893,7 +964,7 @@ int pcg_destroy(pcg_context* c)
 								 &c->a_active,	 &c->a_internal, &c->a_frac,	&c->a_foff,		 &c->a_num,
 								 &c->a_den,		 &c->a_fac,		&c->a_rnum,		&c->a_rden,		 &c->a_rfac,
 								 &c->owner,		 &c->counts,	&c->a_role,		&c->a_shared,	 &c->rb_staging[0],
-								 &c->rb_staging[1] };
+								 &c->rb_staging[1], &c->a_rank,	&c->a_sorted };
 	for (auto* b : all)
 		pcg::dfree(*b);
 	pcg::dfree(c->slab); // after the pieces carved from it
@@ -1493,6 +1564,8 @@ int pcg_set_mass_check(pcg_context* c, int enable)
 		return rc;
 	if (enable && (rc = prepare_mass_check(c)))
 		return rc;
+	if (c->mass_check != (enable != 0))
+		c->generation++; // a batch holding this context rebuilds its descriptors
 	c->mass_check = enable != 0;
 	return PCG_OK;
 }

@@ -9,22 +9,24 @@
 //   release      (274-289)  D += I F / Vv, I = 0
 //
 // GB300 design:
-//  * locate: one thread per agent computes its voxel index in FP64 exactly as
-//    cartesian_mesh::voxel_position does (mesh.cpp:37-61), so agent->voxel maps
-//    and therefore the per-voxel counts are bit-exact with the reference.
-//  * ballot: lanes holding the same voxel are grouped with __match_any_sync; the
-//    group leader issues one atomicMin (the winner is the lowest agent index,
-//    which canonicalises the reference's first-CAS-wins race) and one atomicAdd
-//    of the group's population.
-//  * reduce: each agent adds its terms into its winner's row with atomics (the
-//    winner also adds the 1 of the denominator); any agent that is not its
-//    voxel's winner raises the conflict flag, which stays on the device, so the
-//    step never waits on the host (the Thrust backend copies it back every step,
+//  * place: one thread per agent computes its voxel index exactly as
+//    cartesian_mesh::voxel_position does (mesh.cpp:37-61; locate in
+//    cells_device.cuh: an FP32 estimate decides unless it lies within its error
+//    bound of a voxel boundary, where the FP64 division decides), so the
+//    agent->voxel maps and the per-voxel counts are bit-exact with the reference;
+//    lanes of one voxel count with one atomic (__match_any_sync), whose returned
+//    offset ranks the agents of the voxel.
+//  * ballot: rank 0 wins the voxel (the reference's first compare-and-swap wins,
+//    cell_solver.cpp:79-101); the agents of shared voxels are grouped by voxel and
+//    each group is summed by a segmented warp reduction instead of every agent
+//    adding its terms to the winner's row with contended atomics
+//    (cell_solver.cpp:102-127); the conflict flag stays on the device, so the step
+//    never waits on the host (the Thrust backend copies it back every step,
 //    thrust_solver/src/cell_solver.cpp:251-252).
 //  * apply/internalize read the flag on the device and take the reference's
 //    fused or two-pass branch.  A voxel's substrates are adjacent in the field, so
 //    each agent touches one 32-byte sector of densities (S <= 8, FP32).
-//  Internalized substrates are kept in FP64 in both builds.
+//  Batches keep the per-warp ballot with atomics (batch.cu).
 #include "cells_device.cuh"
 
 namespace pcg {
@@ -33,32 +35,208 @@ namespace {
 
 using namespace cellsdev;
 
+// place: terms (after new agent data), voxel, count and rank; the step's words
+// (conflict flag, list length, reserved group slots) start at zero.
 template <typename T>
-__global__ void cells_locate_kernel(CellArgs a)
+__global__ void cells_place_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	if (i == 0)
-		a.flags[0] = a.flags[1] = 0;
+		a.flags[0] = a.flags[1] = a.flags[2] = 0;
+	uint32_t v = kNoAgent;
 	if (i < a.A)
-		agent_locate<T>(a, i);
+	{
+		if (a.terms)
+			agent_terms<T>(a, i);
+		v = agent_place(a, i);
+	}
+	count_rank(a, i, v);
 }
 
-__global__ void cells_ballot_kernel(CellArgs a)
-{
-	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-	const uint32_t key = i < a.A ? a.vox[i] : kNoAgent;
-	// lanes of a warp hold consecutive agent indices, so a group's leader is its minimum
-	warp_ballot(&a, i, key, key);
-}
+constexpr unsigned kClassifyBlock = 512;
 
+// classify: roles from count and rank (cell_solver.cpp:102-127: every agent but
+// the winner of a shared voxel is a conflict); the agents of shared voxels listed
+// in agent order (flags[1]); each winner reserves its voxel's group of slots
+// (owner[v] = first slot, flags[2] counts slots) and clears its reduced row.  One
+// atomic per block for each counter (block-wide scans).
 template <typename T>
-__global__ void cells_reduce_kernel(CellArgs a)
+__global__ void __launch_bounds__(kClassifyBlock) cells_classify_kernel(CellArgs a)
 {
+	__shared__ uint32_t part[2][kClassifyBlock / 32];
+	__shared__ uint32_t base[2];
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-	const uint8_t role = i < a.A ? agent_reduce<T>(a, i) : kRoleNone;
-	if (__any_sync(0xffffffffu, role == kRoleLoser) && (threadIdx.x & 31) == 0)
+	const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	uint32_t v = kNoAgent, cnt = 0;
+	uint8_t role = kRoleNone;
+	if (i < a.A)
+	{
+		v = a.vox[i];
+		if (v != kNoAgent)
+		{
+			cnt = a.counts[v];
+			role = cnt == 1 ? kRoleAlone : (a.rank[i] == 0 ? kRoleWinner : kRoleLoser);
+		}
+		a.role[i] = role;
+	}
+	if (__any_sync(0xffffffffu, role == kRoleLoser) && lane == 0)
 		atomicOr(a.flags, 1u);
-	list_shared(a, i, role == kRoleWinner || role == kRoleLoser, 0);
+	const uint32_t sh = (role == kRoleWinner || role == kRoleLoser) ? 1u : 0u;
+	const uint32_t seg = role == kRoleWinner ? cnt : 0u;
+	uint32_t sh_inc = sh, seg_inc = seg;
+	for (uint32_t o = 1; o < 32; o <<= 1)
+	{
+		const uint32_t t0 = __shfl_up_sync(0xffffffffu, sh_inc, o), t1 = __shfl_up_sync(0xffffffffu, seg_inc, o);
+		if (lane >= o)
+			sh_inc += t0, seg_inc += t1;
+	}
+	if (lane == 31)
+		part[0][warp] = sh_inc, part[1][warp] = seg_inc;
+	__syncthreads();
+	if (warp == 0)
+	{
+		uint32_t p0 = lane < nw ? part[0][lane] : 0u, p1 = lane < nw ? part[1][lane] : 0u;
+		for (uint32_t o = 1; o < 32; o <<= 1)
+		{
+			const uint32_t t0 = __shfl_up_sync(0xffffffffu, p0, o), t1 = __shfl_up_sync(0xffffffffu, p1, o);
+			if (lane >= o)
+				p0 += t0, p1 += t1;
+		}
+		if (lane == 31)
+		{
+			base[0] = p0 ? atomicAdd(a.flags + 1, p0) : 0u;
+			base[1] = p1 ? atomicAdd(a.flags + 2, p1) : 0u;
+		}
+		uint32_t e0 = __shfl_up_sync(0xffffffffu, p0, 1), e1 = __shfl_up_sync(0xffffffffu, p1, 1);
+		if (lane == 0)
+			e0 = e1 = 0u;
+		if (lane < nw)
+			part[0][lane] = e0, part[1][lane] = e1;
+	}
+	__syncthreads();
+	if (sh)
+		a.shared[base[0] + part[0][warp] + sh_inc - 1] = (uint32_t)i;
+	if (role == kRoleWinner)
+	{
+		a.owner[v] = base[1] + part[1][warp] + seg_inc - seg;
+		T* rn = static_cast<T*>(a.rnum) + i * a.S;
+		T* rd = static_cast<T*>(a.rden) + i * a.S;
+		T* rf = static_cast<T*>(a.rfac) + i * a.S;
+		for (uint64_t s = 0; s < a.S; s++)
+			rn[s] = rd[s] = rf[s] = T(0);
+	}
+}
+
+// group: every agent of a shared voxel writes its index into its voxel's group.
+__global__ void cells_group_kernel(CellArgs a)
+{
+	const uint32_t count = __ldg(a.flags + 1);
+	for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < count; j += (uint64_t)gridDim.x * blockDim.x)
+	{
+		const uint32_t i = __ldg(a.shared + j);
+		const uint32_t v = __ldg(a.vox + i);
+		a.sorted[__ldg(a.owner + v) + __ldg(a.rank + i)] = i;
+	}
+}
+
+// group sum: a warp takes 32 consecutive slots and sums each voxel's terms with a
+// segmented scan (lanes of one voxel are consecutive); the last lane of each
+// voxel's run writes the winner's row: sum num, 1 + sum den, sum fac -- stored
+// when the run is the voxel's whole group, else added with atomics (the part
+// holding the group's first slot adds the 1).
+template <typename T>
+__global__ void cells_group_sum_kernel(CellArgs a)
+{
+	const uint32_t count = __ldg(a.flags + 1);
+	const uint32_t lane = threadIdx.x & 31;
+	const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+	const uint32_t S = (uint32_t)a.S;
+	const bool vec = a.vec;
+	const T* num = static_cast<const T*>(a.num);
+	const T* den = static_cast<const T*>(a.den);
+	const T* fac = static_cast<const T*>(a.fac);
+	T* rnum = static_cast<T*>(a.rnum);
+	T* rden = static_cast<T*>(a.rden);
+	T* rfac = static_cast<T*>(a.rfac);
+	for (uint64_t j0 = gw * 32; j0 < count; j0 += nwarps * 32)
+	{
+		const uint64_t j = j0 + lane;
+		uint32_t i = 0, v = kNoAgent;
+		if (j < count)
+		{
+			i = __ldg(a.sorted + j);
+			v = __ldg(a.vox + i);
+		}
+		const uint32_t group = __match_any_sync(0xffffffffu, v);
+		const uint32_t first = __ffs(group) - 1, last = 31 - __clz(group);
+		const bool writer = v != kNoAgent && lane == last;
+		uint32_t w = 0;
+		bool head = false, whole = false;
+		if (writer)
+		{
+			const uint32_t seg0 = __ldg(a.owner + v), cnt = __ldg(a.counts + v);
+			w = __ldg(a.sorted + seg0);
+			head = j0 + first == seg0;
+			whole = head && j0 + last == (uint64_t)seg0 + cnt - 1;
+		}
+		uint32_t kup[5];
+#pragma unroll
+		for (int k = 0; k < 5; k++)
+			kup[k] = __shfl_up_sync(0xffffffffu, v, 1u << k);
+		for (uint32_t s0 = 0; s0 < S; s0 += kSubBatch)
+		{
+			T n_[kSubBatch], d_[kSubBatch], f_[kSubBatch];
+#pragma unroll
+			for (int q = 0; q < kSubBatch; q++)
+				n_[q] = d_[q] = f_[q] = T(0);
+			if (v != kNoAgent)
+			{
+				row_load(num + (uint64_t)i * S, s0, S, vec, n_);
+				row_load(den + (uint64_t)i * S, s0, S, vec, d_);
+				row_load(fac + (uint64_t)i * S, s0, S, vec, f_);
+			}
+#pragma unroll
+			for (int k = 0; k < 5; k++)
+			{
+				const uint32_t o = 1u << k;
+				const bool take = lane >= o && kup[k] == v;
+#pragma unroll
+				for (int q = 0; q < kSubBatch; q++)
+					if (s0 + q < S) // uniform across the warp
+					{
+						const T tn = __shfl_up_sync(0xffffffffu, n_[q], o);
+						const T td = __shfl_up_sync(0xffffffffu, d_[q], o);
+						const T tf = __shfl_up_sync(0xffffffffu, f_[q], o);
+						if (take)
+							n_[q] += tn, d_[q] += td, f_[q] += tf;
+					}
+			}
+			if (writer)
+			{
+				if (head)
+#pragma unroll
+					for (int q = 0; q < kSubBatch; q++)
+						d_[q] += T(1);
+				const uint64_t r = (uint64_t)w * S;
+				if (whole)
+				{
+					row_store(rnum + r, s0, S, vec, n_);
+					row_store(rden + r, s0, S, vec, d_);
+					row_store(rfac + r, s0, S, vec, f_);
+				}
+				else
+#pragma unroll
+					for (int q = 0; q < kSubBatch; q++)
+						if (s0 + q < S)
+						{
+							atomicAdd(rnum + r + s0 + q, n_[q]);
+							atomicAdd(rden + r + s0 + q, d_[q]);
+							atomicAdd(rfac + r + s0 + q, f_[q]);
+						}
+			}
+		}
+	}
 }
 
 // FP32: registers capped for 3 blocks of 256 per SM (a latency-bound gather:
@@ -147,10 +325,55 @@ CellArgs make_cell_args(const Context* c)
 	a.vec = rows_vectorizable(a, c->wsize);
 	a.terms = 1;
 	a.pairs = c->wsize == 4 ? 1 : 0; // FP32 contexts store internalized amounts as float pairs
+	a.rank = static_cast<uint32_t*>(c->a_rank.ptr);
+	a.sorted = static_cast<uint32_t*>(c->a_sorted.ptr);
+	set_fast_locate(a);
 	return a;
 }
 
 } // namespace cellsdev
+
+// The voxel-grouped ballot (cells_device.cuh) on `stream`; launch bookkeeping
+// through `c` when given.
+template <typename T>
+static int run_ballot(Context* c, const CellArgs& a, cudaStream_t stream, int sm_count)
+{
+	const unsigned block = 256;
+	const unsigned grid = (unsigned)((a.A + block - 1) / block);
+	const unsigned cgrid = (unsigned)((a.A + kClassifyBlock - 1) / kClassifyBlock);
+	// the list of shared-voxel agents is only known on the device: grid-stride
+	const unsigned lgrid = std::min<unsigned>(grid, 16 * std::max(sm_count, 1));
+	const double S = (double)a.S, A = (double)a.A, w = (double)sizeof(T);
+	cudaEvent_t ev = nullptr;
+	if (c)
+		launch_begin(c, K_CELLS_LOCATE,
+					 A * (8.0 * a.dims + 1 + 4 + 4 + 4 + 4) + (a.terms ? A * (5 * S * 8 + 8 + 3 * S * w) : 0), &ev);
+	cells_place_kernel<T><<<grid, block, 0, stream>>>(a);
+	if (c)
+		launch_end(c, K_CELLS_LOCATE, ev);
+	PCG_CUDA_TRY(cudaGetLastError());
+	if (c)
+		launch_begin(c, K_CELLS_BALLOT, A * (4 + 4 + 4 + 1), &ev);
+	cells_classify_kernel<T><<<cgrid, kClassifyBlock, 0, stream>>>(a);
+	if (c && c->timing && c->h_words) // list length for the per-agent byte counts
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->h_words + 2, a.flags + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	if (c)
+		launch_end(c, K_CELLS_BALLOT, ev, 4.0 + 3 * S * w);
+	PCG_CUDA_TRY(cudaGetLastError());
+	if (c)
+		launch_begin(c, K_CELLS_GROUP, 0.0, &ev);
+	cells_group_kernel<<<lgrid, block, 0, stream>>>(a);
+	if (c)
+		launch_end(c, K_CELLS_GROUP, ev, 20.0);
+	PCG_CUDA_TRY(cudaGetLastError());
+	if (c)
+		launch_begin(c, K_CELLS_REDUCE, 0.0, &ev);
+	cells_group_sum_kernel<T><<<lgrid, block, 0, stream>>>(a);
+	if (c)
+		launch_end(c, K_CELLS_REDUCE, ev, 8.0 + 3 * S * w);
+	PCG_CUDA_TRY(cudaGetLastError());
+	return PCG_OK;
+}
 
 template <typename T>
 static int run_cells(Context* c, bool recompute)
@@ -165,23 +388,14 @@ static int run_cells(Context* c, bool recompute)
 	if (recompute)
 	{
 		PCG_CUDA_TRY(cudaMemsetAsync(c->counts.ptr, 0, c->V * sizeof(uint32_t), c->stream));
-		// positions, activity, voxel index/offset, ballot slot, cleared sums; the terms
-		// (rates, volume in; three FP32/FP64 rows out) only after new agent data
+		// the terms (rates, volume in; three rows out) only after new agent data
 		a.terms = c->terms_dirty ? 1 : 0;
-		launch_begin(c, K_CELLS_LOCATE,
-					 A * (8.0 * c->dims + 1 + 8 + 4 + 3 * S * w + (a.terms ? 5 * S * 8 + 8 + 3 * S * w : 0)), &ev);
-		cells_locate_kernel<T><<<grid, block, 0, c->stream>>>(a);
+		if (c->timing && !c->h_words && !(c->h_words = pinned_words_get()))
+			return fail(PCG_ERR_NOMEM, "pinned host memory for the device words");
+		const int rc = run_ballot<T>(c, a, c->stream, c->sm_count);
+		if (rc)
+			return rc;
 		c->terms_dirty = false;
-		launch_end(c, K_CELLS_LOCATE, ev);
-		PCG_CUDA_TRY(cudaGetLastError());
-		launch_begin(c, K_CELLS_BALLOT, A * (4 + 8), &ev);
-		cells_ballot_kernel<<<grid, block, 0, c->stream>>>(a);
-		launch_end(c, K_CELLS_BALLOT, ev);
-		PCG_CUDA_TRY(cudaGetLastError());
-		launch_begin(c, K_CELLS_REDUCE, A * (8 + 6 * S * w), &ev);
-		cells_reduce_kernel<T><<<grid, block, 0, c->stream>>>(a);
-		launch_end(c, K_CELLS_REDUCE, ev);
-		PCG_CUDA_TRY(cudaGetLastError());
 	}
 	// per agent: role, offset, summed (or own) terms, density read+write
 	launch_begin(c, K_CELLS_APPLY, A * (5 + 3 * S * w + 2 * S * w + (c->compute_internalized ? 16 * S : 0)), &ev);
@@ -190,12 +404,11 @@ static int run_cells(Context* c, bool recompute)
 	PCG_CUDA_TRY(cudaGetLastError());
 	if (c->compute_internalized)
 	{
-		// the agents that share a voxel (a few percent at 1e6 agents in 320^3 voxels)
-		// read their own terms and density and rewrite their internalized amounts:
-		// not counted, only the list length is
-		launch_begin(c, K_CELLS_INTERNALIZE, 4, &ev);
+		// the agents that share a voxel (a few percent at 1e6 agents in 320^3 voxels):
+		// list entry, offset, density, own terms, internalized read and write each
+		launch_begin(c, K_CELLS_INTERNALIZE, 0.0, &ev);
 		cells_internalize_kernel<T><<<std::min<unsigned>(grid, 8 * std::max(c->sm_count, 1)), block, 0, c->stream>>>(a);
-		launch_end(c, K_CELLS_INTERNALIZE, ev);
+		launch_end(c, K_CELLS_INTERNALIZE, ev, 8.0 + 4 * S * w + 16 * S);
 		PCG_CUDA_TRY(cudaGetLastError());
 	}
 	return PCG_OK;
@@ -253,13 +466,20 @@ int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream)
 	a.vec = rows_vectorizable(a, sizeof(float));
 	a.terms = 1;
 	a.pairs = 0; // the caller's FP64 amounts
+	a.rank = b.rank;
+	a.sorted = b.sorted;
+	set_fast_locate(a);
 	const uint64_t V = b.n[0] * b.n[1] * b.n[2];
 	const unsigned block = 256;
 	const unsigned grid = (unsigned)((b.A + block - 1) / block);
+	int sm_count = 0, dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev) !=
+												   cudaSuccess)
+		sm_count = 0;
 	PCG_CUDA_TRY(cudaMemsetAsync(b.counts, 0, V * sizeof(uint32_t), stream));
-	cells_locate_kernel<float><<<grid, block, 0, stream>>>(a);
-	cells_ballot_kernel<<<grid, block, 0, stream>>>(a);
-	cells_reduce_kernel<float><<<grid, block, 0, stream>>>(a);
+	int rc = run_ballot<float>(nullptr, a, stream, sm_count);
+	if (rc)
+		return rc;
 	cells_apply_kernel<float><<<grid, block, 0, stream>>>(a);
 	if (b.internalized)
 		cells_internalize_kernel<float><<<grid, block, 0, stream>>>(a);

@@ -53,7 +53,31 @@ struct CellArgs
 	int vec;   // rows of S values start on 16-byte boundaries and S is a multiple of 16 / sizeof(T)
 	int pairs; // internalized amounts stored as float pairs (FP32 contexts; see pair_add)
 	int terms; // recompute the agent terms (their rates or volumes changed), not only positions
+	// fast voxel location (locate): bbmin and 1/voxel as floats; fast == 0 when the
+	// mesh's bounds or voxel edges are not exactly representable in FP32
+	float mf[3], rf[3];
+	int fast;
+	// voxel-grouped ballot (cells.cu): rank of each agent in its voxel, and the
+	// agents of shared voxels grouped by voxel (slot order)
+	uint32_t* rank;   // [A]
+	uint32_t* sorted; // [A]
 };
+
+// The fast-location constants of a mesh: float bounds and reciprocal voxel edges,
+// usable when every bound and edge is an integer of at most 24 bits.
+inline void set_fast_locate(CellArgs& a)
+{
+	a.fast = 1;
+	for (int d = 0; d < a.dims; d++)
+	{
+		const double m = a.bbmin[d], h = a.voxel[d];
+		if (!(fabs(m) <= 16777216.0) || !(h >= 1.0 && h <= 16777216.0) || (double)(float)m != m ||
+			(double)(float)h != h || a.n[d] > (1u << 22))
+			a.fast = 0;
+		a.mf[d] = (float)m;
+		a.rf[d] = (float)(1.0 / h);
+	}
+}
 
 // Cell arguments of a context's own buffers (cells.cu).
 CellArgs make_cell_args(const Context* c);
@@ -67,16 +91,48 @@ inline int rows_vectorizable(const CellArgs& a, size_t wsize)
 		   al(a.den) && al(a.fac) && al(a.rnum) && al(a.rden) && al(a.rfac);
 }
 
-// cartesian_mesh::voxel_position (mesh.cpp:37-61) in FP64; false when outside the grid.
+// cartesian_mesh::voxel_position (mesh.cpp:37-61): idx = trunc(q) with the FP64
+// quotient q = (p - bbmin) / voxel, outside the grid when !(q >= 0) or q >= n;
+// false when outside.  The result is exactly the FP64 expression's, but the
+// division (a long sequence on this GPU's slow FP64 pipe) runs only near a voxel
+// boundary: qf = (float(p) - float(bbmin)) * float(1/voxel) is within
+// 2^-24 (3|q| + |p|/voxel) of q (one rounding each of p, the difference, the
+// reciprocal and the product; bbmin and voxel are exact as floats), so when qf
+// lies more than 2^-21 (|qf| + |p|/voxel) + 2^-40 from every integer, q lies
+// strictly inside the same unit interval and trunc(q), and the bounds test, are
+// decided by qf.  Otherwise (and for NaN or huge positions) the FP64 division
+// decides.
+__device__ __forceinline__ bool locate_exact_axis(const CellArgs& a, double p, int d, uint64_t& idx)
+{
+	const double q = (p - a.bbmin[d]) / a.voxel[d];
+	if (!(q >= 0.0) || q >= (double)a.n[d])
+		return false;
+	idx = (uint64_t)q;
+	return true;
+}
+
 __device__ __forceinline__ bool locate(const CellArgs& a, uint64_t i, uint64_t idx[3])
 {
 	idx[0] = idx[1] = idx[2] = 0;
 	for (int d = 0; d < a.dims; d++)
 	{
-		const double q = (a.pos[i * a.dims + d] - a.bbmin[d]) / a.voxel[d];
-		if (!(q >= 0.0) || q >= (double)a.n[d])
+		const double p = a.pos[i * a.dims + d];
+		if (a.fast)
+		{
+			const float pf = (float)p;
+			const float qf = __fmul_rn(__fsub_rn(pf, a.mf[d]), a.rf[d]);
+			const float fl = floorf(qf);
+			const float tol = fmaf(fabsf(qf) + fabsf(pf) * a.rf[d], 4.76837158e-7f, 9.09494702e-13f); // 2^-21, 2^-40
+			if (qf - fl > tol && (fl + 1.0f) - qf > tol)
+			{
+				if (fl < 0.0f || fl >= (float)a.n[d])
+					return false;
+				idx[d] = (uint64_t)fl;
+				continue;
+			}
+		}
+		if (!locate_exact_axis(a, p, d, idx[d]))
 			return false;
-		idx[d] = (uint64_t)q;
 	}
 	return true;
 }
@@ -87,12 +143,11 @@ __device__ __forceinline__ bool locate(const CellArgs& a, uint64_t i, uint64_t i
 // recomputes.  With a.terms they are computed for inactive agents too, so that an
 // agent activated later finds its terms.
 template <typename T>
-__device__ __forceinline__ void agent_locate(const CellArgs& a, uint64_t i)
+__device__ __forceinline__ void agent_terms(const CellArgs& a, uint64_t i)
 {
 	T* num = static_cast<T*>(a.num);
 	T* den = static_cast<T*>(a.den);
 	T* fac = static_cast<T*>(a.fac);
-	if (a.terms)
 	{
 		const double vol = a.vol[i];
 		// FP32 build: the agent's dt Vc / Vv and dt / Vv once, products per
@@ -118,21 +173,38 @@ __device__ __forceinline__ void agent_locate(const CellArgs& a, uint64_t i)
 			}
 		}
 	}
+}
+
+// The voxel of agent i < A (vox, foff), or kNoAgent when it is inactive or outside
+// the grid (a device error then); returns it.
+__device__ __forceinline__ uint32_t agent_place(const CellArgs& a, uint64_t i)
+{
 	uint64_t idx[3];
 	if (!a.active[i])
 	{
 		a.vox[i] = kNoAgent;
-		return;
+		return kNoAgent;
 	}
 	if (!locate(a, i, idx))
 	{
 		atomicOr(a.err, DEV_ERR_AGENT_OUTSIDE);
 		a.vox[i] = kNoAgent;
-		return;
+		return kNoAgent;
 	}
 	const uint32_t v = (uint32_t)(idx[0] + a.n[0] * (idx[1] + a.n[1] * idx[2]));
 	a.vox[i] = v;
 	a.foff[i] = (uint32_t)((idx[2] * a.n[1] + idx[1]) * a.pitch + idx[0] * a.S);
+	return v;
+}
+
+template <typename T>
+__device__ __forceinline__ void agent_locate(const CellArgs& a, uint64_t i)
+{
+	if (a.terms)
+		agent_terms<T>(a, i);
+	const uint32_t v = agent_place(a, i);
+	if (v == kNoAgent)
+		return;
 	a.owner[v] = kNoAgent;
 	T* rnum = static_cast<T*>(a.rnum);
 	T* rden = static_cast<T*>(a.rden);
@@ -213,6 +285,39 @@ __device__ __forceinline__ void list_shared(const CellArgs& a, uint64_t i, bool 
 		base = atomicAdd(a.flags + 1, (uint32_t)__popc(group));
 	base = __shfl_sync(group, base, leader);
 	a.shared[base + __popc(group & ((1u << lane) - 1))] = (uint32_t)i;
+}
+
+// ---- voxel-grouped ballot (single-domain contexts)
+//
+// The reference sums every agent's terms into its voxel's winner with atomics
+// (cell_solver.cpp:79-129).  When tens of agents share a voxel those atomics
+// serialise on the winner's row, so here the ballot groups the agents of shared
+// voxels by voxel instead and sums each group with a segmented warp reduction:
+//   place:     voxel of each agent; a warp-aggregated count per voxel whose
+//              returned offset gives the agent's rank in its voxel (rank 0, the
+//              agent whose atomic landed first, is the winner, as the first
+//              compare-and-swap wins in the reference)
+//   classify:  roles from count and rank; the agents of shared voxels are listed
+//              in agent order (for the internalized pass) and each winner
+//              reserves its voxel's group of slots
+//   group:     every listed agent writes its index into its voxel's group
+//   group sum: warps reduce consecutive slots by voxel; a group that lies within
+//              one warp is stored once, a group split across warps adds its parts
+//              to the winner's row (cleared by classify) with atomics
+
+// Counts agent i into voxel v (one atomic per voxel and warp) and records its rank
+// in the voxel.  All lanes of the warp call it (v = kNoAgent for none).
+__device__ __forceinline__ void count_rank(const CellArgs& a, uint64_t i, uint32_t v)
+{
+	const uint32_t group = __match_any_sync(0xffffffffu, v);
+	if (v == kNoAgent)
+		return;
+	const uint32_t lane = threadIdx.x & 31, leader = __ffs(group) - 1;
+	uint32_t base = 0;
+	if (lane == leader)
+		base = atomicAdd(a.counts + v, (uint32_t)__popc(group));
+	base = __shfl_sync(group, base, leader);
+	a.rank[i] = base + __popc(group & ((1u << lane) - 1));
 }
 
 // Change of an internalized amount.  The FP64 build evaluates the reference's

@@ -63,6 +63,7 @@ enum KernelId : int
 	K_LAYOUT,
 	K_CELLS_CLEAR,
 	K_MASS_CHECK,
+	K_CELLS_GROUP,
 	K_COUNT
 };
 
@@ -105,6 +106,7 @@ struct SweepArgs
 	uint32_t box_rows;    // line points per TMA box (<= 256)
 	uint32_t boxes;       // boxes per tile (boxes * box_rows >= n)
 	uint64_t comp_off;    // compressed coefficient tables (elements into coef)
+	uint64_t blo_off;     // FP32: full table of the multipliers' lo parts (elements into coef)
 	uint32_t head;        // head points of the compressed tables
 	// x sweep: a tile is rows_per_tile whole rows
 	uint64_t rows;        // ny*nz
@@ -121,7 +123,7 @@ struct SweepArgs
 	uint64_t nx, ny, nz;
 	// mass check (kernels instantiated with it): FP64 totals [before S | after S];
 	// the x sweep adds its inputs, the last sweep its outputs (x as well when the
-	// mesh is 1-D: mc_x_out)
+	// mesh is 1-D)
 	double* mc_tot;
 	uint32_t mc_x_out;
 };
@@ -211,6 +213,7 @@ struct Context
 	uint64_t coef_len[3] = { 0, 0, 0 };
 	uint64_t coef_elems[3] = { 0, 0, 0 };
 	uint64_t coef_comp_off[3] = { 0, 0, 0 }; // compressed tables (head rows, constants)
+	uint64_t coef_blo_off[3] = { 0, 0, 0 };  // FP32: the full table of the multipliers' lo parts
 	uint32_t coef_head[3] = { 0, 0, 0 };     // head points per substrate of the compressed tables
 	// One allocation at initialisation sized by estimate_device_bytes, from which
 	// the context's buffers are carved in turn (dozens of pool allocations per
@@ -277,9 +280,12 @@ struct Context
 	DeviceBuffer a_foff;                  // uint32 [A]: field offset of the voxel's first substrate
 	DeviceBuffer a_role;                  // uint8 [A]: ballot role (cells_device.cuh)
 	DeviceBuffer a_shared;                // uint32 [A]: agents of voxels that hold several
+	DeviceBuffer a_rank;                  // uint32 [A]: rank of the agent in its voxel
+	DeviceBuffer a_sorted;                // uint32 [A]: agents of shared voxels grouped by voxel
 	DeviceBuffer a_num, a_den, a_fac;     // real [A*S]
 	DeviceBuffer a_rnum, a_rden, a_rfac;  // real [A*S]
-	DeviceBuffer owner;                   // uint32 [V]: winning agent per voxel
+	DeviceBuffer owner;                   // uint32 [V]: winning agent per voxel (batches), or the first
+										  // slot of the voxel's group in a_sorted (single domain)
 	DeviceBuffer counts;                  // uint32 [V]: active agents per voxel
 
 	// measurement
@@ -291,14 +297,16 @@ struct Context
 	{
 		int kid;
 		cudaEvent_t a, b;
+		double per_shared; // algorithmic bytes per agent in a shared voxel (a count known on the device)
 	};
+	uint32_t shared_agents = 0; // agents in shared voxels after the last timed ballot (timing mode)
 	std::vector<PendingTiming> pending;
 };
 
 // Launch bookkeeping: every kernel launch goes through begin/end so that the
 // context can count launches and (optionally) time them with CUDA events.
 void launch_begin(Context* c, int kid, double bytes, cudaEvent_t* ev);
-void launch_end(Context* c, int kid, cudaEvent_t ev);
+void launch_end(Context* c, int kid, cudaEvent_t ev, double per_shared = 0.0);
 void collect_timings(Context* c);
 
 // ------------------------------------------------------------------ kernel launchers (defined in .cu files)
@@ -338,8 +346,8 @@ struct CellStepBuffers
 	double* internal;
 	int internalized;
 	float* field;
-	// scratch: vox/foff/shared/role [A], owner/counts [V], flags/err [4] each, terms [A*S] each
-	uint32_t *vox, *foff, *shared, *owner, *counts, *flags, *err;
+	// scratch: vox/foff/shared/rank/sorted/role [A], owner/counts [V], flags/err [4] each, terms [A*S] each
+	uint32_t *vox, *foff, *shared, *rank, *sorted, *owner, *counts, *flags, *err;
 	uint8_t* role;
 	float *num, *den, *fac, *rnum, *rden, *rfac;
 };

@@ -127,12 +127,28 @@ struct LineCoef
 {
 	const T* hB;
 	const T* hE;
+	const T* hBl; // FP32: lo parts of the multipliers (head rows), null for FP64
 	uint32_t H, n;
 	T mB, mE, lB, lE, c;
+	T mBl, lBl; // FP32: lo parts of the middle and last multipliers
 };
 
+// One backward step d = (x + c d) b'.  FP32 tables give the multiplier as a pair
+// hi + lo (the column-sum-exact multiplier of the host tables), applied with one
+// rounding; FP64 tables hold b' itself (lo unused).
+__device__ __forceinline__ float bwd_step(float c, float d, float x, float bh, float bl)
+{
+	const float t = dev::fmadd(c, d, x);
+	return dev::fmadd(t, bh, t * bl);
+}
+__device__ __forceinline__ double bwd_step(double c, double d, double x, double bh, double)
+{
+	return dev::fmadd(c, d, x) * bh;
+}
+
 // Compressed table of an axis: [head b' (S x H) | head e (S x H) | mid b' | mid e |
-// last b' | last e | c], the five constant arrays kS = S rounded up to 16 bytes long.
+// last b' | last e | c], the five constant arrays kS = S rounded up to 16 bytes long;
+// FP32 tables continue with [head b' lo (S x H) | mid b' lo | last b' lo].
 template <typename T>
 __device__ __forceinline__ LineCoef<T> line_coef(const T* comp, uint32_t S, uint32_t H, uint32_t n, uint32_t s)
 {
@@ -149,6 +165,18 @@ __device__ __forceinline__ LineCoef<T> line_coef(const T* comp, uint32_t S, uint
 	L.lB = __ldg(k + 2 * kS + s);
 	L.lE = __ldg(k + 3 * kS + s);
 	L.c = __ldg(k + 4 * kS + s);
+	if constexpr (sizeof(T) == 4)
+	{
+		const T* lo = k + 5 * kS;
+		L.hBl = lo + (uint64_t)s * H;
+		L.mBl = __ldg(lo + (uint64_t)S * H + s);
+		L.lBl = __ldg(lo + (uint64_t)S * H + kS + s);
+	}
+	else
+	{
+		L.hBl = nullptr;
+		L.mBl = L.lBl = T(0);
+	}
 	return L;
 }
 
@@ -243,16 +271,18 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 		}
 	}
 	d = T(0);
+	constexpr bool kLo = sizeof(T) == 4;
 	for (int j = (int)n - 1; j >= (int)(nb * P); j--)
 	{
-		d = dev::fmadd(c, d, col[(uint64_t)j * st]) * coef_at(L.hB, L.H, L.mB, L.lB, n, (uint32_t)j);
+		const T bl = kLo ? coef_at(L.hBl, L.H, L.mBl, L.lBl, n, (uint32_t)j) : T(0);
+		d = bwd_step(c, d, col[(uint64_t)j * st], coef_at(L.hB, L.H, L.mB, L.lB, n, (uint32_t)j), bl);
 		col[(uint64_t)j * st] = d;
 		if constexpr ((MC & kMcOut) != 0)
 			acc_out->add(d);
 	}
 	{
 		T x[P], xn[P];
-		V bb[NV], bn[NV];
+		V bb[NV], bn[NV], bl[NV], bln[NV];
 		if (nb)
 		{
 			const T* blk = col + (uint64_t)(nb - 1) * P * st;
@@ -260,6 +290,8 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 			for (int q = 0; q < P; q++)
 				x[q] = blk[q * st];
 			fetch_block<T, V, NV>(L.hB, L.H, L.mB, L.lB, n, (nb - 1) * P, bb);
+			if constexpr (kLo)
+				fetch_block<T, V, NV>(L.hBl, L.H, L.mBl, L.lBl, n, (nb - 1) * P, bl);
 		}
 		for (int b = (int)nb - 1; b >= 0; b--)
 		{
@@ -270,12 +302,14 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 				for (int q = 0; q < P; q++)
 					xn[q] = blk[(q - P) * (int)st];
 				fetch_block<T, V, NV>(L.hB, L.H, L.mB, L.lB, n, (uint32_t)(b - 1) * P, bn);
+				if constexpr (kLo)
+					fetch_block<T, V, NV>(L.hBl, L.H, L.mBl, L.lBl, n, (uint32_t)(b - 1) * P, bln);
 			}
 			T y[P];
 #pragma unroll
 			for (int q = P - 1; q >= 0; q--)
 			{
-				d = dev::fmadd(c, d, x[q]) * vget<V, T>(bb[q / VN], q % VN);
+				d = bwd_step(c, d, x[q], vget<V, T>(bb[q / VN], q % VN), kLo ? vget<V, T>(bl[q / VN], q % VN) : T(0));
 				blk[q * st] = d;
 				y[q] = d;
 			}
@@ -286,7 +320,11 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 				x[q] = xn[q];
 #pragma unroll
 			for (int v = 0; v < NV; v++)
+			{
 				bb[v] = bn[v];
+				if constexpr (kLo)
+					bl[v] = bln[v];
+			}
 		}
 	}
 }
@@ -295,16 +333,19 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 // S*sizeof(T) a multiple of 16 bytes: thread h of a row's TPR threads owns chunk
 // slot h of every x position (VN substrates, VN independent recurrences).
 // MC adds element u's inputs / outputs to acc_in[u] / acc_out[u] (substrate h*VN + u).
+// cBl: the FP32 multipliers' lo parts (same layout as cB), null for FP64.
 template <typename T, int TPR, int MC = 0>
 __device__ __forceinline__ void solve_row_chunks(T* row, const T* __restrict__ cB, const T* __restrict__ cE,
-												 const T* __restrict__ cC, uint32_t n, int h,
+												 const T* __restrict__ cC, const T* __restrict__ cBl, uint32_t n, int h,
 												 MassAcc<T>* acc_in = nullptr, MassAcc<T>* acc_out = nullptr)
 {
 	using V = typename Vec16<T>::type;
 	constexpr int VN = Vec16<T>::N, P = kChunkBlock;
+	constexpr bool kLo = sizeof(T) == 4;
 	V* __restrict__ vrow = reinterpret_cast<V*>(row) + h;
 	const V* vE = reinterpret_cast<const V*>(cE) + h;
 	const V* vB = reinterpret_cast<const V*>(cB) + h;
+	const V* vBl = kLo ? reinterpret_cast<const V*>(cBl) + h : nullptr;
 	const uint32_t nb = n / P;
 	T d[VN], c[VN];
 #pragma unroll
@@ -323,15 +364,21 @@ __device__ __forceinline__ void solve_row_chunks(T* row, const T* __restrict__ c
 			vset<V, T>(v, u, d[u]);
 		}
 	};
-	auto step_bwd = [&](V& v, const V& b) {
+	auto step_bwd = [&](V& v, const V& b, const V& bl) {
 #pragma unroll
 		for (int u = 0; u < VN; u++)
 		{
-			d[u] = dev::fmadd(c[u], d[u], vget<V, T>(v, u)) * vget<V, T>(b, u);
+			d[u] = bwd_step(c[u], d[u], vget<V, T>(v, u), vget<V, T>(b, u), kLo ? vget<V, T>(bl, u) : T(0));
 			vset<V, T>(v, u, d[u]);
 			if constexpr ((MC & kMcOut) != 0)
 				acc_out[u].add(d[u]);
 		}
+	};
+	auto ldg_lo = [&](uint32_t k) {
+		V z {};
+		if constexpr (kLo)
+			z = ldg_vec(vBl + k);
+		return z;
 	};
 	{
 		V x[P], xn[P], e[P], en[P];
@@ -378,17 +425,18 @@ __device__ __forceinline__ void solve_row_chunks(T* row, const T* __restrict__ c
 	for (int i = (int)n - 1; i >= (int)(nb * P); i--)
 	{
 		V v = vrow[i * TPR];
-		step_bwd(v, ldg_vec(vB + i * TPR));
+		step_bwd(v, ldg_vec(vB + i * TPR), ldg_lo(i * TPR));
 		vrow[i * TPR] = v;
 	}
 	{
-		V x[P], xn[P], bb[P], bn[P];
+		V x[P], xn[P], bb[P], bn[P], bl[P], bln[P];
 		if (nb)
 #pragma unroll
 			for (int q = 0; q < P; q++)
 			{
 				x[q] = vrow[((nb - 1) * P + q) * TPR];
 				bb[q] = ldg_vec(vB + ((nb - 1) * P + q) * TPR);
+				bl[q] = ldg_lo(((nb - 1) * P + q) * TPR);
 			}
 		for (int b = (int)nb - 1; b >= 0; b--)
 		{
@@ -399,11 +447,12 @@ __device__ __forceinline__ void solve_row_chunks(T* row, const T* __restrict__ c
 				{
 					xn[q] = vrow[(i0 - P + q) * TPR];
 					bn[q] = ldg_vec(vB + (i0 - P + q) * TPR);
+					bln[q] = ldg_lo((i0 - P + q) * TPR);
 				}
 #pragma unroll
 			for (int q = P - 1; q >= 0; q--)
 			{
-				step_bwd(x[q], bb[q]);
+				step_bwd(x[q], bb[q], bl[q]);
 				vrow[(i0 + q) * TPR] = x[q];
 			}
 #pragma unroll
@@ -411,6 +460,7 @@ __device__ __forceinline__ void solve_row_chunks(T* row, const T* __restrict__ c
 			{
 				x[q] = xn[q];
 				bb[q] = bn[q];
+				bl[q] = bln[q];
 			}
 		}
 	}
@@ -422,8 +472,8 @@ __device__ __forceinline__ void solve_row_chunks(T* row, const T* __restrict__ c
 // MC adds substrate s's inputs / outputs to acc_in[s] / acc_out[s].
 template <typename T, int ST, int MC = 0>
 __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, const T* __restrict__ cE,
-											  const T* __restrict__ cC, uint32_t n, MassAcc<T>* acc_in = nullptr,
-											  MassAcc<T>* acc_out = nullptr)
+											  const T* __restrict__ cC, const T* __restrict__ cBl, uint32_t n,
+											  MassAcc<T>* acc_in = nullptr, MassAcc<T>* acc_out = nullptr)
 {
 	using V = typename Vec16<T>::type;
 	constexpr int VN = Vec16<T>::N;
@@ -432,9 +482,17 @@ __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, 
 	constexpr int NB = U * ((kChunkBlock + U - 1) / U); // chunks per block
 	const uint32_t total = n * ST;
 	const uint32_t nchunks = (total + GE - 1) / GE * U; // whole groups (tail elements predicated)
+	constexpr bool kLo = sizeof(T) == 4;
 	V* __restrict__ vrow = reinterpret_cast<V*>(row);
 	const V* vE = reinterpret_cast<const V*>(cE);
 	const V* vB = reinterpret_cast<const V*>(cB);
+	const V* vBl = reinterpret_cast<const V*>(cBl);
+	auto ldg_lo = [&](uint32_t k) {
+		V z {};
+		if constexpr (kLo)
+			z = ldg_vec(vBl + k);
+		return z;
+	};
 	T d[ST], c[ST];
 #pragma unroll
 	for (int s = 0; s < ST; s++)
@@ -458,14 +516,14 @@ __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, 
 			}
 		}
 	};
-	auto bwd_chunk = [&](V& v, const V& b, int q, uint32_t k) {
+	auto bwd_chunk = [&](V& v, const V& b, const V& bl, int q, uint32_t k) {
 #pragma unroll
 		for (int u = VN - 1; u >= 0; u--)
 		{
 			const int s = (q * VN + u) % ST;
 			if (k * VN + u < total)
 			{
-				d[s] = dev::fmadd(c[s], d[s], vget<V, T>(v, u)) * vget<V, T>(b, u);
+				d[s] = bwd_step(c[s], d[s], vget<V, T>(v, u), vget<V, T>(b, u), kLo ? vget<V, T>(bl, u) : T(0));
 				vset<V, T>(v, u, d[s]);
 				if constexpr ((MC & kMcOut) != 0)
 					acc_out[s].add(d[s]);
@@ -526,18 +584,19 @@ __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, 
 		for (int q = U - 1; q >= 0; q--)
 		{
 			V v = vrow[k0 + q];
-			bwd_chunk(v, ldg_vec(vB + k0 + q), q, (uint32_t)(k0 + q));
+			bwd_chunk(v, ldg_vec(vB + k0 + q), ldg_lo(k0 + q), q, (uint32_t)(k0 + q));
 			vrow[k0 + q] = v;
 		}
 	}
 	{
-		V x[NB], xn[NB], bb[NB], bn[NB];
+		V x[NB], xn[NB], bb[NB], bn[NB], bl[NB], bln[NB];
 		if (nb)
 #pragma unroll
 			for (int q = 0; q < NB; q++)
 			{
 				x[q] = vrow[(nb - 1) * NB + q];
 				bb[q] = ldg_vec(vB + (nb - 1) * NB + q);
+				bl[q] = ldg_lo((nb - 1) * NB + q);
 			}
 		for (int b = (int)nb - 1; b >= 0; b--)
 		{
@@ -548,11 +607,12 @@ __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, 
 				{
 					xn[q] = vrow[k0 - NB + q];
 					bn[q] = ldg_vec(vB + k0 - NB + q);
+					bln[q] = ldg_lo(k0 - NB + q);
 				}
 #pragma unroll
 			for (int q = NB - 1; q >= 0; q--)
 			{
-				bwd_chunk(x[q], bb[q], q, k0 + q);
+				bwd_chunk(x[q], bb[q], bl[q], q, k0 + q);
 				vrow[k0 + q] = x[q];
 			}
 #pragma unroll
@@ -560,6 +620,7 @@ __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, 
 			{
 				x[q] = xn[q];
 				bb[q] = bn[q];
+				bl[q] = bln[q];
 			}
 		}
 	}
@@ -569,8 +630,9 @@ __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, 
 // substrate s's input / output total of the row to mc_in[s] / mc_out[s] (FP64
 // atomics per row; a path for rare substrate counts).
 template <typename T, int MC = 0>
-__device__ __forceinline__ void solve_row_generic(T* row, const T* cB, const T* cE, const T* cC, uint32_t n,
-												  uint32_t S, double* mc_in = nullptr, double* mc_out = nullptr)
+__device__ __forceinline__ void solve_row_generic(T* row, const T* cB, const T* cE, const T* cC, const T* cBl,
+												  uint32_t n, uint32_t S, double* mc_in = nullptr,
+												  double* mc_out = nullptr)
 {
 	for (uint32_t s = 0; s < S; s++)
 	{
@@ -589,7 +651,7 @@ __device__ __forceinline__ void solve_row_generic(T* row, const T* cB, const T* 
 		d = T(0);
 		for (int i = (int)n - 1; i >= 0; i--)
 		{
-			d = dev::fmadd(c, d, row[i * S + s]) * __ldg(cB + i * S + s);
+			d = bwd_step(c, d, row[i * S + s], __ldg(cB + i * S + s), sizeof(T) == 4 ? __ldg(cBl + i * S + s) : T(0));
 			row[i * S + s] = d;
 			if constexpr ((MC & kMcOut) != 0)
 				ao.add(d);
@@ -612,14 +674,15 @@ constexpr int x_tpr()
 
 // Solves one x row of substrate count S at compile time when S <= 8.
 template <typename T, int ST>
-__device__ __forceinline__ void solve_row(T* row, const T* cB, const T* cE, const T* cC, uint32_t n, uint32_t S, int h)
+__device__ __forceinline__ void solve_row(T* row, const T* cB, const T* cE, const T* cC, const T* cBl, uint32_t n,
+										  uint32_t S, int h)
 {
 	if constexpr (ST == 0)
-		solve_row_generic<T>(row, cB, cE, cC, n, S);
+		solve_row_generic<T>(row, cB, cE, cC, cBl, n, S);
 	else if constexpr ((ST * (int)sizeof(T)) % 16 == 0)
-		solve_row_chunks<T, x_tpr<T, ST>()>(row, cB, cE, cC, n, h);
+		solve_row_chunks<T, x_tpr<T, ST>()>(row, cB, cE, cC, cBl, n, h);
 	else
-		solve_row_vec<T, ST>(row, cB, cE, cC, n);
+		solve_row_vec<T, ST>(row, cB, cE, cC, cBl, n);
 }
 
 } // namespace solvers

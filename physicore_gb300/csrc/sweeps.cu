@@ -152,8 +152,8 @@ __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __g
 // Row-per-thread mapping: a tile is rows_per_tile consecutive rows and the CTA has
 // rows_per_tile * TPR threads (<= 32); TPR threads share a row when its substrates
 // fill whole 16-byte chunks.
-// MC = kMcIn | kMcOut (the mass check on): the threads also sum their rows'
-// inputs (and outputs on a 1-D mesh, where x is the last sweep) per substrate.
+// MC (the mass check on): the threads also sum their rows' inputs (kMcIn) and, on
+// a 1-D mesh where x is the last sweep, their outputs (kMcOut) per substrate.
 template <typename T, int ST, int MC>
 __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 {
@@ -179,6 +179,7 @@ __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 	const T* cB = static_cast<const T*>(a.coef);
 	const T* cE = cB + a.coef_len;
 	const T* cC = cE + a.coef_len;
+	const T* cBl = sizeof(T) == 4 ? cB + a.blo_off : nullptr;
 	if (tid == 0)
 	{
 		dev::mbar_init(bar, 1);
@@ -212,11 +213,11 @@ __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 		{
 			T* row = tile + r_local * a.smem_pitch;
 			if constexpr (ST == 0)
-				solve_row_generic<T, MC>(row, cB, cE, cC, n, a.S, a.mc_tot, a.mc_x_out ? a.mc_tot + a.S : nullptr);
+				solve_row_generic<T, MC>(row, cB, cE, cC, cBl, n, a.S, a.mc_tot, a.mc_tot + a.S);
 			else if constexpr (kChunks)
-				solve_row_chunks<T, TPR, MC>(row, cB, cE, cC, n, h, ai, ao);
+				solve_row_chunks<T, TPR, MC>(row, cB, cE, cC, cBl, n, h, ai, ao);
 			else
-				solve_row_vec<T, ST, MC>(row, cB, cE, cC, n, ai, ao);
+				solve_row_vec<T, ST, MC>(row, cB, cE, cC, cBl, n, ai, ao);
 		}
 		dev::fence_proxy_async_smem();
 		__syncthreads();
@@ -234,7 +235,7 @@ __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 		{
 			const uint32_t sub = kChunks ? (uint32_t)(h * Vec16<T>::N + u) : (uint32_t)u;
 			flush_classes(ai[u].value(), TPR, blockDim.x, a.mc_tot + sub);
-			if (a.mc_x_out)
+			if constexpr ((MC & kMcOut) != 0)
 				flush_classes(ao[u].value(), TPR, blockDim.x, a.mc_tot + a.S + sub);
 		}
 	}
@@ -247,8 +248,8 @@ __global__ void __launch_bounds__(kLanes) sweep_x_kernel(SweepArgs a)
 // points need no coefficient load).  Row pitches are chosen so that the lanes of
 // a warp touch distinct banks.
 // ST = S when it is a compile-time constant (stride-S shared-memory accesses with
-// immediate offsets), 0 for the run-time path.  MC = kMcIn | kMcOut (the mass
-// check on): lane (r, s) also sums its lines' inputs (and outputs on a 1-D mesh)
+// immediate offsets), 0 for the run-time path.  MC (the mass check on): lane
+// (r, s) also sums its lines' inputs (kMcIn) and, on a 1-D mesh, outputs (kMcOut)
 // over all its tiles, added once at the end.
 template <typename T, int ST, int MC>
 __global__ void __launch_bounds__(kLanes) sweep_x_sub_kernel(SweepArgs a)
@@ -307,7 +308,7 @@ __global__ void __launch_bounds__(kLanes) sweep_x_sub_kernel(SweepArgs a)
 	{
 		// lanes r * S + s share substrate s (S <= 32 on this mapping)
 		flush_classes(ai.value(), S, kLanes, a.mc_tot + s);
-		if (a.mc_x_out)
+		if constexpr ((MC & kMcOut) != 0)
 			flush_classes(ao.value(), S, kLanes, a.mc_tot + S + s);
 	}
 	dev::bulk_wait_all();
@@ -389,6 +390,7 @@ SweepArgs base_args(const Context* c, int axis)
 	a.rows = c->rows;
 	a.err = static_cast<uint32_t*>(c->err.ptr);
 	a.ticket = static_cast<uint32_t*>(c->tickets.ptr) + axis;
+	a.blo_off = c->coef_blo_off[axis];
 	return a;
 }
 
@@ -438,7 +440,8 @@ int run_sweep_x(Context* c, bool mass_check)
 		return dispatch_sweep_x<T, 0>(c, a, p, sub);
 	a.mc_tot = static_cast<double*>(c->mc_tot.ptr);
 	a.mc_x_out = c->dims == 1 ? 1u : 0u;
-	return dispatch_sweep_x<T, kMcIn | kMcOut>(c, a, p, sub);
+	// on a 1-D mesh x is also the last sweep: it sums its outputs as well
+	return c->dims == 1 ? dispatch_sweep_x<T, kMcIn | kMcOut>(c, a, p, sub) : dispatch_sweep_x<T, kMcIn>(c, a, p, sub);
 }
 
 template <typename T>

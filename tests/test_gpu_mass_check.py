@@ -89,3 +89,45 @@ def test_mass_check_many_substrates(pcg, oracle_mod, precision):
     after = o.mass()
     assert np.all(np.abs(chk["before"] - before) <= tol * np.abs(before))
     assert np.all(np.abs(chk["after"] - after) <= tol * np.abs(before))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("graph", [True, False])
+def test_mass_check_in_batches(pcg, oracle_mod, precision, graph):
+    """Contexts stepped by a batch keep their own per-step check: every other
+    domain has it on, domains run different step budgets, and each checked
+    domain's worst residual, step count and last totals match a single-domain
+    checked run of the same problem (and its totals the oracle's)."""
+    problems = [W.random_small(100 + k) for k in range(10)]
+    budgets = [STEPS - (k % 3) for k in range(10)]
+    batched = [W.apply(pcg.Solver(precision), p) for p in problems]
+    for k, s in enumerate(batched):
+        if k % 2 == 0:
+            s.set_mass_check(True)
+    b = pcg.Batch(batched)
+    b.set_graph(graph)
+    b.solve(STEPS, budgets=budgets)
+    b.synchronize()
+    tol = 1e-12 if precision == 1 else 1e-5
+    for k, (p, s) in enumerate(zip(problems, batched)):
+        if k % 2:
+            with pytest.raises(pcg.PcgError):
+                s.get_mass_check()
+            continue
+        chk = s.get_mass_check()
+        assert chk["steps"] == budgets[k], (k, chk["steps"])
+        assert np.all(chk["worst"] <= tol), (k, chk["worst"])
+        single = W.apply(pcg.Solver(precision), p)
+        single.set_mass_check(True)
+        single.solve(budgets[k])
+        ref = single.get_mass_check()
+        scale = np.maximum(np.abs(ref["before"]), 1e-300)
+        assert np.all(np.abs(chk["before"] - ref["before"]) <= tol * scale), k
+        assert np.all(np.abs(chk["after"] - ref["after"]) <= tol * scale), k
+        o = W.apply(oracle_mod.OracleSolver(threads=2), p)
+        o.solve(budgets[k] - 1)
+        before = o.mass()
+        o.run_phases(oracle_mod.PHASE_DIFFUSION, False)
+        assert np.all(np.abs(chk["before"] - before) <= tol * np.maximum(np.abs(before), 1e-300)), k
+        assert np.all(np.abs(chk["after"] - o.mass()) <= tol * np.maximum(np.abs(before), 1e-300)), k
+    b.close()
