@@ -186,11 +186,19 @@ int pcg_mass(pcg_context* ctx, double* host);
  * diagonal entry having r subtracted once), so every step's sweeps must divide
  * each substrate's total by f, the product of those sums over the axes, whatever
  * Dirichlet, bulk and agents then add.  When enabled, every step that runs the diffusion
- * phase sums the field in FP64 before the x sweep and after the last sweep (two
- * extra passes over the field, and the boundary faces are then written by their
- * own kernel) and keeps, per substrate, the worst |after*f - before| / |before|.
- * Enabling resets the record; contexts stepped by a batch are not checked. */
+ * phase totals the field in FP64 before the x sweep and after the last sweep --
+ * the sweeps add up the values they read and write, so the check reads no extra
+ * pass of the field -- and keeps, per substrate, the worst
+ * |after*f - before| / |before|.  Enabling resets the record.  Contexts stepped by
+ * a batch keep their check (pcg_batch_solve checks every domain that has it on). */
 int pcg_set_mass_check(pcg_context* ctx, int enable);
+/* Tuning of the x and y sweeps of 3-D meshes (3 to 32 substrates), which by
+ * default run as one launch over z-slabs of about slab_bytes of field, the y
+ * sweep of a slab starting `lag` slabs after its x sweep, so that the y sweep
+ * reads the x sweep's output from L2 (the arithmetic is unchanged).  enable = 0
+ * runs them as two launches; slab_bytes / lag of 0 keep the current values
+ * (defaults 8 MiB and 2). */
+int pcg_set_sweep_fusion(pcg_context* ctx, int enable, uint64_t slab_bytes, uint32_t lag);
 /* The last checked step's totals before and after its sweeps, the worst residual
  * since the check was enabled (each [S], NULL to skip) and the steps checked. */
 int pcg_get_mass_check(pcg_context* ctx, double* mass_before, double* mass_after, double* worst_residual,

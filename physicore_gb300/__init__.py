@@ -70,6 +70,7 @@ SIGNATURES = {
     "pcg_get_conflict": [_P, _P],
     "pcg_mass": [_P, _P],
     "pcg_set_mass_check": [_P, ctypes.c_int],
+    "pcg_set_sweep_fusion": [_P, ctypes.c_int, _u64, _u32],
     "pcg_get_mass_check": [_P, _P, _P, _P, _P],
     "pcg_synchronize": [_P],
     "pcg_get_field_device": [_P, _P, _P, _P],
@@ -327,6 +328,10 @@ class Solver:
     def set_mass_check(self, enable=True):
         """Per-step FP64 check of the sweeps' mass identity (pcg_set_mass_check)."""
         self._check(self._L.pcg_set_mass_check(self._h, int(bool(enable))))
+
+    def set_sweep_fusion(self, enable=True, slab_bytes=0, lag=0):
+        """x and y sweeps of 3-D meshes in one launch over z-slabs (pcg_set_sweep_fusion)."""
+        self._check(self._L.pcg_set_sweep_fusion(self._h, int(bool(enable)), int(slab_bytes), int(lag)))
 
     def get_mass_check(self):
         """dict(before, after, worst, steps): the last checked step's totals before

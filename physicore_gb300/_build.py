@@ -49,7 +49,7 @@ def _compile(src: str, extra: list[str]) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     if not _stale(obj, [src] + headers() + [__file__]):
         return obj
-    cmd = [nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+    cmd = [nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
            "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), *extra, "-c", src, "-o", obj + ".tmp"]
     subprocess.run(cmd, check=True)
     os.replace(obj + ".tmp", obj)

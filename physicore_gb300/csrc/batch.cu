@@ -745,6 +745,34 @@ __global__ void batch_mass_finish_kernel(const BatchDomain* doms, const uint32_t
 	}
 }
 
+// Timing mode only: the algorithmic bytes of this step's internalize pass, which
+// reads and rewrites the rows of the agents in shared voxels (their number is on
+// the device): list entry, offset, density, own terms, internalized amount.
+__global__ void batch_shared_bytes_kernel(const BatchDomain* doms, const uint32_t* steps_left, uint32_t count,
+										  uint32_t wsize, double* out)
+{
+	double acc = 0.0;
+	for (uint32_t d = threadIdx.x; d < count; d += blockDim.x)
+	{
+		const CellArgs& a = doms[d].cells;
+		if (steps_left[d] && a.internalized && a.A)
+			acc += (double)__ldg(a.flags + 1) * (8.0 + 4.0 * a.S * wsize + 16.0 * a.S);
+	}
+	for (int o = 16; o > 0; o >>= 1)
+		acc += __shfl_xor_sync(0xffffffffu, acc, o);
+	__shared__ double part[32];
+	if ((threadIdx.x & 31) == 0)
+		part[threadIdx.x >> 5] = acc;
+	__syncthreads();
+	if (threadIdx.x == 0)
+	{
+		double t = 0.0;
+		for (uint32_t w = 0; w < blockDim.x / 32; w++)
+			t += part[w];
+		*out = t;
+	}
+}
+
 // End of a step: one step fewer for every domain still running.
 __global__ void batch_count_step_kernel(uint32_t* steps_left, uint32_t count)
 {
@@ -903,7 +931,10 @@ struct pcg_batch
 	{
 		int kid;
 		cudaEvent_t a, b;
+		bool shared_bytes; // add the step's shared-voxel agent bytes (timing mode)
 	};
+	pcg::DeviceBuffer d_shared_bytes; // timing mode: bytes of the last internalize pass
+	double* h_shared_bytes = nullptr;  // pinned copy
 	std::vector<Pending> pending;
 	std::vector<cudaEvent_t> event_pool;
 
@@ -1337,8 +1368,8 @@ int build_t(pcg_batch* b)
 			b->rebuild_bytes[d] = { 4.0 * V, A * (8.0 * c->dims + 1 + 5 * S * 8 + 8 + 6 * S * w + 4), A * 12,
 									A * (8 + 6 * S * w) };
 			b->step_bytes[K_CELLS_APPLY] += A * (5 + 5 * S * w + (c->compute_internalized ? 16 * S : 0));
-			if (c->compute_internalized)
-				b->step_bytes[K_CELLS_INTERNALIZE] += 4; // agents sharing a voxel not counted
+			// internalize: counted per agent of a shared voxel in timing mode (the
+			// lists' lengths are on the device), not in replayed steps
 		}
 	}
 	b->built = true;
@@ -1384,7 +1415,7 @@ struct LaunchScope
 		{
 			cudaEvent_t e = get_event(b);
 			cudaEventRecord(e, b->stream);
-			b->pending.push_back({ kid, a, e });
+			b->pending.push_back({ kid, a, e, kid == K_CELLS_INTERNALIZE });
 		}
 	}
 };
@@ -1396,6 +1427,8 @@ void collect(pcg_batch* b)
 		float ms = 0;
 		if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess)
 			b->stats[p.kid].total_ms += ms;
+		if (p.shared_bytes && b->h_shared_bytes)
+			b->stats[p.kid].bytes += *b->h_shared_bytes;
 		b->event_pool.push_back(p.a);
 		b->event_pool.push_back(p.b);
 	}
@@ -1520,6 +1553,21 @@ int launch_step(pcg_batch* b)
 			batch_cells_internalize_kernel<T><<<std::max(b->internalize_blocks, 1u), 256, 0, b->stream>>>(
 				args_for(b, L_AGENTS, 3), static_cast<const uint32_t*>(b->d_iblocks.ptr), ndom);
 			PCG_CUDA_TRY(cudaGetLastError());
+		}
+		if (b->timing) // the internalize pass's bytes, once the lists' lengths are known
+		{
+			if (!b->h_shared_bytes)
+				b->h_shared_bytes = reinterpret_cast<double*>(pinned_words_get());
+			if (!b->h_shared_bytes)
+				return fail(PCG_ERR_NOMEM, "pinned host memory for the internalize byte count");
+			const int rc2 = balloc(b->d_shared_bytes, sizeof(double), b->stream, b->device);
+			if (rc2)
+				return rc2;
+			batch_shared_bytes_kernel<<<1, 256, 0, b->stream>>>(
+				static_cast<const BatchDomain*>(b->d_doms.ptr), static_cast<const uint32_t*>(b->d_steps_left.ptr),
+				(uint32_t)b->ctx.size(), (uint32_t)sizeof(T), static_cast<double*>(b->d_shared_bytes.ptr));
+			PCG_CUDA_TRY(cudaMemcpyAsync(b->h_shared_bytes, b->d_shared_bytes.ptr, sizeof(double),
+										 cudaMemcpyDeviceToHost, b->stream));
 		}
 	}
 	const uint32_t N = (uint32_t)b->ctx.size();
@@ -2027,7 +2075,7 @@ int pcg_batch_destroy(pcg_batch* b)
 	for (cudaEvent_t e : b->event_pool)
 		cudaEventDestroy(e);
 	DeviceBuffer* bufs[] = { &b->d_doms,	 &b->d_tmaps,	  &b->d_lists,		&b->d_counters,
-							 &b->d_err, &b->d_recompute, &b->d_steps_left, &b->d_iblocks };
+							 &b->d_err, &b->d_recompute, &b->d_steps_left, &b->d_iblocks, &b->d_shared_bytes };
 	for (DeviceBuffer* x : bufs)
 		pcg::free_buf(*x);
 	if (b->ev_sync)
@@ -2035,6 +2083,7 @@ int pcg_batch_destroy(pcg_batch* b)
 	if (b->stream)
 		cudaStreamDestroy(b->stream);
 	pcg::pinned_words_put(b->h_words);
+	pcg::pinned_words_put(reinterpret_cast<uint32_t*>(b->h_shared_bytes));
 	if (b->ev_block)
 		cudaEventDestroy(b->ev_block);
 	delete b;

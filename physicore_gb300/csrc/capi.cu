@@ -32,7 +32,8 @@ const char* kernel_name(int id)
 	static const char* names[K_COUNT] = { "sweep_x",	  "sweep_y",		"sweep_z",	   "dirichlet_faces",
 										  "dirichlet_interior", "bulk", "cells_locate", "cells_ballot",
 										  "cells_reduce", "cells_apply", "cells_internalize", "cells_release",
-										  "mass",		  "layout", "cells_clear", "mass_check", "cells_group" };
+										  "mass",		  "layout", "cells_clear", "mass_check", "cells_group",
+										  "sweep_xy" };
 	return (id >= 0 && id < K_COUNT) ? names[id] : "?";
 }
 
@@ -342,16 +343,20 @@ static void precompute_axis(uint64_t n, uint64_t S, uint64_t shape, uint64_t dim
 }
 
 // FP32 backward multipliers that keep the sweep's mass exact.  The FP32 solve uses
-// E = e and C = c rounded to FP32; the tridiagonal matrix that this factorisation
-// inverts is then M' = L'U' with L'[i][i-1] = -E[i-1] and U' = diag(1/B) - C on the
-// superdiagonal, whose column j sums to (1 - E[j]) / B[j] + E[j-1] C - C (the last
-// two terms for j > 0; E[n-1] = 0).  Choosing B[j] (in FP64) so that every column
-// sums exactly to the reference matrix's column sum (diffusion_solver.cpp:29-86:
-// the diagonal minus r for each neighbour) makes M' conserve mass exactly as the
-// reference does; with the exact e and c it gives b'[j] itself.  FP32 rounding of
-// b', e and c otherwise biases every step the same way, and over hundreds of steps
-// that drift dominates the FP32 error.  B is applied as a pair hi + lo with one
-// rounding (d = fma(t, hi, t * lo)).
+// E = e and c rounded to FP32 and evaluates each backward step as
+// d_i = B_i x_i + K_i d_{i+1}, with the coupling K_i = RN32(RN32(B_i) c) and B_i
+// applied as a pair hi + lo (sweep_solvers.cuh, bwd_step).  The tridiagonal matrix
+// this factorisation inverts is M' = L'U', L'[i][i-1] = -E[i-1], U'[i][i] = 1/B_i,
+// U'[i][i+1] = -K_i/B_i =: -C'_i, whose column j sums to
+// (1 - E[j]) / B[j] - (1 - E[j-1]) C'[j-1] (E[-1] = C'[-1] = 0, E[n-1] = 0).
+// Choosing B[j] in FP64, in order, so that every column sums exactly to the
+// reference matrix's column sum (diffusion_solver.cpp:29-86: the diagonal minus r
+// for each neighbour) makes M' conserve mass exactly as the reference does; with
+// the exact e and c it gives b'[j] itself.  Plain FP32 rounding of b', e and c
+// otherwise biases every step the same way, and over hundreds of steps that drift
+// dominates the FP32 error.  Where the sequence has converged to its middle value
+// (relative change below 1e-15) the middle value is kept, so that the compressed
+// tables hold a single constant there.
 static void colsum_multipliers(uint64_t n, uint64_t S, uint64_t shape, uint64_t dims, double dt, const double* D,
 							   const double* decay, const std::vector<double>& e, const std::vector<double>& cc,
 							   std::vector<double>& B)
@@ -361,7 +366,8 @@ static void colsum_multipliers(uint64_t n, uint64_t S, uint64_t shape, uint64_t 
 	for (uint64_t s = 0; s < S; s++)
 	{
 		const double r = dt * D[s] / h2;
-		const double C = (double)(float)cc[s];
+		const float C32 = (float)cc[s];
+		double Cp = 0.0; // C'[j-1]
 		for (uint64_t j = 0; j < n; j++)
 		{
 			double diag = 1 + decay[s] * dt / (double)dims + 2 * dt * D[s] / h2;
@@ -370,7 +376,20 @@ static void colsum_multipliers(uint64_t n, uint64_t S, uint64_t shape, uint64_t 
 			const double kappa = diag - (j > 0 ? r : 0.0) - (j + 1 < n ? r : 0.0);
 			const double Ej = j + 1 < n ? (double)(float)e[j * S + s] : 0.0;
 			const double Em = j > 0 ? (double)(float)e[(j - 1) * S + s] : 0.0;
-			B[j * S + s] = (1.0 - Ej) / (kappa - Em * C + (j > 0 ? C : 0.0));
+			const double b = (1.0 - Ej) / (kappa + (1.0 - Em) * Cp);
+			B[j * S + s] = b;
+			const volatile float K = (float)b * C32; // the device's FP32 product
+			Cp = (double)K / b;
+		}
+		if (n >= 3) // keep the converged middle value exactly constant
+		{
+			const double m = B[(n - 2) * S + s];
+			for (uint64_t j = n - 2; j-- > 1;)
+			{
+				if (std::fabs(B[j * S + s] / m - 1.0) >= 1e-15)
+					break;
+				B[j * S + s] = m;
+			}
 		}
 	}
 }
@@ -593,10 +612,18 @@ static int run_phases(Context* c, uint32_t phases, bool recompute)
 	const bool fuse = (phases & PCG_PHASE_DIFFUSION) && (phases & PCG_PHASE_DIRICHLET) && faces_fusable(c);
 	if (phases & PCG_PHASE_DIFFUSION)
 	{
-		if ((rc = launch_sweep_x(c, check)))
-			return rc;
-		if (c->dims >= 2 && (rc = launch_sweep_yz(c, 1, fuse && c->dims == 2, check && c->dims == 2)))
-			return rc;
+		if (xy_fusable(c))
+		{
+			if ((rc = launch_sweep_xy(c, check)))
+				return rc;
+		}
+		else
+		{
+			if ((rc = launch_sweep_x(c, check)))
+				return rc;
+			if (c->dims >= 2 && (rc = launch_sweep_yz(c, 1, fuse && c->dims == 2, check && c->dims == 2)))
+				return rc;
+		}
 		if (c->dims >= 3 && (rc = launch_sweep_yz(c, 2, fuse, check)))
 			return rc;
 		if (check && (rc = launch_mass_check_finish(c)))
@@ -964,7 +991,7 @@ int pcg_destroy(pcg_context* c)
 								 &c->a_active,	 &c->a_internal, &c->a_frac,	&c->a_foff,		 &c->a_num,
 								 &c->a_den,		 &c->a_fac,		&c->a_rnum,		&c->a_rden,		 &c->a_rfac,
 								 &c->owner,		 &c->counts,	&c->a_role,		&c->a_shared,	 &c->rb_staging[0],
-								 &c->rb_staging[1], &c->a_rank,	&c->a_sorted };
+								 &c->rb_staging[1], &c->a_rank,	&c->a_sorted,	&c->xy_segs,	 &c->xy_done };
 	for (auto* b : all)
 		pcg::dfree(*b);
 	pcg::dfree(c->slab); // after the pieces carved from it
@@ -1552,6 +1579,17 @@ static int prepare_mass_check(Context* c)
 	PCG_CUDA_TRY(cudaMemcpyAsync(c->mc_out.ptr, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
 	PCG_CUDA_TRY(pcg::stream_wait(c));
 	c->mass_checked_steps = 0;
+	return PCG_OK;
+}
+
+int pcg_set_sweep_fusion(pcg_context* c, int enable, uint64_t slab_bytes, uint32_t lag)
+{
+	CTX_CHECK(c);
+	c->fuse_xy = enable != 0;
+	if (slab_bytes)
+		c->xy_slab_bytes = slab_bytes;
+	if (lag)
+		c->xy_lag = lag;
 	return PCG_OK;
 }
 

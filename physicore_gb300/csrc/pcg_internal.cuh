@@ -64,6 +64,7 @@ enum KernelId : int
 	K_CELLS_CLEAR,
 	K_MASS_CHECK,
 	K_CELLS_GROUP,
+	K_SWEEP_XY,
 	K_COUNT
 };
 
@@ -223,7 +224,15 @@ struct Context
 	DeviceBuffer err;      // uint32 device error word
 	uint32_t* h_words = nullptr; // pinned host words for reading it
 	cudaEvent_t ev_block = nullptr; // blocking-sync event for host waits on the stream
-	DeviceBuffer tickets;  // uint32 [4]: tile counters of the persistent sweeps
+	DeviceBuffer tickets;  // uint32 [4]: tile counters of the persistent sweeps ([3]: fused x/y)
+	// fused x/y sweeps: on/off (pcg_set_sweep_fusion), slab size, lag, and the
+	// segment table and per-slab counters of the current plan
+	bool fuse_xy = true;
+	uint64_t xy_slab_bytes = 8ull << 20;
+	uint32_t xy_lag = 2;
+	uint64_t xy_key = 0;
+	uint32_t xy_nseg = 0, xy_total = 0, xy_nslab = 0;
+	DeviceBuffer xy_segs, xy_done;
 	DeviceBuffer flags;    // uint32 [4]: [0] ballot conflict, [1] agents in shared voxels
 	DeviceBuffer mass;     // double [S]
 	// per-step mass check (pcg_set_mass_check): FP64 totals [2 * S] before the
@@ -312,6 +321,9 @@ void collect_timings(Context* c);
 // ------------------------------------------------------------------ kernel launchers (defined in .cu files)
 
 int launch_sweep_x(Context* c, bool mass_check = false);
+// x and y sweeps of a 3-D mesh fused slab by slab (sweeps.cu), when xy_fusable
+bool xy_fusable(const Context* c);
+int launch_sweep_xy(Context* c, bool mass_check = false);
 int launch_sweep_yz(Context* c, int axis, bool fuse_faces = false, bool mass_check = false);
 // Dirichlet faces (unless the last sweep already wrote them) and interior nodes
 int launch_dirichlet(Context* c, bool faces_done = false);

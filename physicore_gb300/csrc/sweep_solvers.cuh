@@ -133,13 +133,17 @@ struct LineCoef
 	T mBl, lBl; // FP32: lo parts of the middle and last multipliers
 };
 
-// One backward step d = (x + c d) b'.  FP32 tables give the multiplier as a pair
-// hi + lo (the column-sum-exact multiplier of the host tables), applied with one
-// rounding; FP64 tables hold b' itself (lo unused).
+// One backward step d = (x + c d) b'.  FP32: evaluated as d = (b' c) d + b' x, with
+// the FP32 coupling b' c = RN(bh * c) and the product b' x taken with the
+// multiplier's pair bh + lo (the host's column-sum-exact multipliers account for
+// the coupling's rounding), so the chain from one point to the next is a single
+// fma (b' x does not depend on the chain).  FP64 tables hold b' itself (lo
+// unused) and keep the reference's form.
 __device__ __forceinline__ float bwd_step(float c, float d, float x, float bh, float bl)
 {
-	const float t = dev::fmadd(c, d, x);
-	return dev::fmadd(t, bh, t * bl);
+	const float bc = bh * c;
+	const float xb = dev::fmadd(x, bh, x * bl);
+	return dev::fmadd(bc, d, xb);
 }
 __device__ __forceinline__ double bwd_step(double c, double d, double x, double bh, double)
 {

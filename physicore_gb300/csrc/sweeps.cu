@@ -314,6 +314,210 @@ __global__ void __launch_bounds__(kLanes) sweep_x_sub_kernel(SweepArgs a)
 	dev::bulk_wait_all();
 }
 
+// ------------------------------------------------------------------ fused x + y
+
+// The x and y sweeps of a 3-D mesh in one persistent launch, z-slab by z-slab.
+// x lines and y lines of a z-plane both lie in that plane, so once the x sweep
+// has written the planes of a slab, the y sweep of that slab can start -- while
+// the x output is still in L2 (the slabs are a few MB and the y sweep reads
+// them a slab or two later).  The y tiles then load from L2 instead of HBM and
+// the x output is overwritten in L2 before most of it is ever written back: per
+// step the field crosses HBM four times instead of six.  The arithmetic of each
+// line is unchanged.
+//
+// Work items are tickets over a table of segments in ticket order: the x tiles
+// of slab k (segment X(k)), and the y tiles of slab k - L after X(k) (lag L).
+// A y tile waits until every x tile of its slab has signalled (a per-slab
+// counter, released by an x tile after its stores completed and acquired by the
+// y tile before its tensor loads).  Tickets are handed out in order and an x
+// tile never waits, so every awaited x tile belongs to a running CTA and every
+// wait ends; the wait is bounded all the same (DEV_ERR_WAIT_TIMEOUT).  An x tile
+// signals once the next tile's loads are in flight (its stores had that long to
+// land), and before its CTA waits for any slab.
+struct XYArgs
+{
+	const uint4* segs; // {first ticket, slab | kYSeg, tiles, x tiles of the slab (y segments)}
+	uint32_t nseg;
+	uint32_t total;    // tickets
+	uint32_t planes;   // z-planes per slab
+	uint32_t* done;    // [slabs] x tiles signalled, zeroed before the launch
+	uint32_t* ticket;
+	uint64_t ny, nz;
+};
+constexpr uint32_t kYSeg = 0x80000000u;
+
+__device__ __forceinline__ uint32_t load_acquire(const uint32_t* p)
+{
+	uint32_t v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
+// Bounded wait for *p >= target (the calling lane only).
+__device__ __forceinline__ bool wait_at_least(const uint32_t* p, uint32_t target)
+{
+	const uint64_t t0 = dev::global_ns();
+	while (load_acquire(p) < target)
+	{
+		if (dev::global_ns() - t0 > dev::kWaitNs)
+			return false;
+		__nanosleep(100);
+	}
+	return true;
+}
+
+template <typename T, int ST, int MC>
+__global__ void __launch_bounds__(kLanes)
+	sweep_xy_kernel(SweepArgs ax, SweepArgs ay, const __grid_constant__ CUtensorMap tmap, XYArgs f)
+{
+	extern __shared__ __align__(128) unsigned char smem[];
+	uint64_t* bar_x = reinterpret_cast<uint64_t*>(smem);
+	uint64_t* bar_y = reinterpret_cast<uint64_t*>(smem + 8);
+	uint32_t* s_ticket = reinterpret_cast<uint32_t*>(smem + 16);
+	T* buf = reinterpret_cast<T*>(smem + 128);
+	const uint32_t tid = threadIdx.x;
+	// x: lane (r, s) solves substrate s of row r of the tile
+	const uint32_t S = ST ? (uint32_t)ST : ax.S, nx_pts = ax.n, R = ax.rows_per_tile;
+	const uint32_t r_local = tid / S, s = tid % S;
+	const uint32_t row_bytes = (uint32_t)round_up(ax.row_len * sizeof(T), 16);
+	const LineCoef<T> Lx = line_coef<T>(static_cast<const T*>(ax.coef) + ax.comp_off, S, ax.head, nx_pts, s);
+	MassAcc<T> ai, ao;
+	ai.zero();
+	ao.zero();
+	// y
+	const uint32_t ny_pts = ay.n, Ry = ay.box_rows, nc = ay.boxes, chunk_elems = Ry * kLanes;
+	const T* ycomp = static_cast<const T*>(ay.coef) + ay.comp_off;
+	if (tid == 0)
+	{
+		dev::mbar_init(bar_x, 1);
+		dev::mbar_init(bar_y, 1);
+		dev::fence_mbar_init();
+	}
+	__syncthreads();
+	uint32_t phase_x = 0, phase_y = 0;
+	int pending = -1; // slab of this CTA's last x tile, not yet signalled
+	bool ok = true;
+	// signals the pending x tile once its stores have completed
+	auto signal = [&]() {
+		if (pending < 0)
+			return;
+		dev::bulk_wait_all();
+		fence_proxy_async_global();
+		__syncthreads();
+		if (tid == 0)
+		{
+			__threadfence();
+			atomicAdd(f.done + pending, 1u);
+		}
+		pending = -1;
+	};
+	for (;;)
+	{
+		if (tid == 0)
+			*s_ticket = atomicAdd(f.ticket, 1u);
+		__syncthreads();
+		const uint32_t t = *s_ticket;
+		__syncthreads();
+		if (t >= f.total)
+			break;
+		// the segment holding t (segments are in ticket order)
+		uint32_t lo = 0, hi = f.nseg;
+		while (hi - lo > 1)
+		{
+			const uint32_t mid = (lo + hi) / 2;
+			if (__ldg(&f.segs[mid].x) <= t)
+				lo = mid;
+			else
+				hi = mid;
+		}
+		const uint4 seg = __ldg(f.segs + lo);
+		const uint32_t u = t - seg.x, slab = seg.y & ~kYSeg;
+		if (!(seg.y & kYSeg))
+		{
+			// x tile u of the slab: rows [r0, r0 + nrows)
+			const uint64_t slab_r0 = (uint64_t)slab * f.planes * f.ny;
+			const uint64_t slab_r1 = min((uint64_t)(slab + 1) * f.planes, f.nz) * f.ny;
+			const uint64_t r0 = slab_r0 + (uint64_t)u * R;
+			const uint32_t nrows = (uint32_t)min((uint64_t)R, slab_r1 - r0);
+			T* g = static_cast<T*>(ax.field) + r0 * ax.pitch;
+			if (tid == 0)
+				dev::mbar_arrive_expect_tx(bar_x, nrows * row_bytes);
+			__syncthreads();
+			if (tid < nrows)
+				dev::bulk_g2s(buf + tid * ax.smem_pitch, g + tid * ax.pitch, row_bytes, bar_x);
+			signal(); // the previous x tile's stores had this long to complete
+			if (!__syncthreads_and(dev::mbar_wait(bar_x, phase_x)))
+			{
+				ok = false;
+				break;
+			}
+			phase_x ^= 1;
+			if (r_local < nrows)
+				solve_line<T, ST, MC>(buf + r_local * ax.smem_pitch + s, nx_pts, S, Lx, &ai, &ao);
+			dev::fence_proxy_async_smem();
+			__syncthreads();
+			if (tid < nrows)
+				dev::bulk_s2g(g + tid * ax.pitch, buf + tid * ax.smem_pitch, row_bytes);
+			dev::bulk_commit();
+			dev::bulk_wait_read();
+			__syncthreads();
+			pending = (int)slab;
+		}
+		else
+		{
+			signal(); // never wait on a slab while holding an unsignalled x tile
+			bool ready = true;
+			if (tid == 0)
+			{
+				ready = wait_at_least(f.done + slab, seg.w);
+				fence_proxy_async_global(); // the tensor loads below follow the acquire
+			}
+			if (!__syncthreads_and(ready))
+			{
+				ok = false;
+				break;
+			}
+			// y tile u of the slab: 32 columns at every y of one plane
+			const uint32_t xblocks = (uint32_t)ay.xblocks;
+			const int x0 = (int)((u % xblocks) * kLanes);
+			const int o = (int)((uint64_t)slab * f.planes + u / xblocks);
+			if (tid == 0)
+			{
+				dev::mbar_arrive_expect_tx(bar_y, nc * chunk_elems * (uint32_t)sizeof(T));
+				for (uint32_t c = 0; c < nc; c++)
+					dev::tma_load_3d(buf + c * chunk_elems, &tmap, x0, (int)(c * Ry), o, bar_y);
+			}
+			const uint32_t sy = (uint64_t)(x0 + tid) < ay.row_len ? (uint32_t)((x0 + tid) % ay.S) : 0;
+			const LineCoef<T> Ly = line_coef<T>(ycomp, ay.S, ay.head, ny_pts, sy);
+			if (!__all_sync(0xffffffffu, dev::mbar_wait(bar_y, phase_y)))
+			{
+				ok = false;
+				break;
+			}
+			phase_y ^= 1;
+			solve_line<T, kLanes>(buf + tid, ny_pts, 0, Ly);
+			dev::fence_proxy_async_smem();
+			__syncwarp();
+			if (tid == 0)
+			{
+				for (uint32_t c = 0; c < nc; c++)
+					dev::tma_store_3d(&tmap, x0, (int)(c * Ry), o, buf + c * chunk_elems);
+				dev::bulk_commit();
+				dev::bulk_wait_read();
+			}
+			__syncthreads();
+		}
+	}
+	signal();
+	if (!ok && tid == 0)
+		atomicOr(ax.err, DEV_ERR_WAIT_TIMEOUT);
+	if constexpr (MC != 0)
+		flush_classes(ai.value(), S, kLanes, ax.mc_tot + s);
+	dev::bulk_wait_all();
+}
+
 struct Plan
 {
 	uint64_t smem;
@@ -442,6 +646,111 @@ int run_sweep_x(Context* c, bool mass_check)
 	a.mc_x_out = c->dims == 1 ? 1u : 0u;
 	// on a 1-D mesh x is also the last sweep: it sums its outputs as well
 	return c->dims == 1 ? dispatch_sweep_x<T, kMcIn | kMcOut>(c, a, p, sub) : dispatch_sweep_x<T, kMcIn>(c, a, p, sub);
+}
+
+// The fused x + y launch (sweep_xy_kernel): slabs of about c->xy_slab_bytes of
+// planes, y lagging x by c->xy_lag slabs.  The segment table is rebuilt when the
+// slab plan changes.
+template <typename T>
+int run_sweep_xy(Context* c, bool mass_check)
+{
+	SweepArgs ax = base_args(c, 0);
+	ax.smem_pitch = sweep_x_sub_pitch(c->row_len, c->S, sizeof(T));
+	ax.comp_off = c->coef_comp_off[0];
+	ax.head = c->coef_head[0];
+	const Plan px = plan<T>(c, 0);
+	ax.rows_per_tile = (uint32_t)px.rows_per_tile;
+	if (mass_check)
+		ax.mc_tot = static_cast<double*>(c->mc_tot.ptr);
+	SweepArgs ay = base_args(c, 1);
+	ay.xblocks = (c->row_len + kLanes - 1) / kLanes;
+	ay.box_rows = c->tmap_box_rows[1];
+	ay.boxes = c->tmap_boxes[1];
+	ay.comp_off = c->coef_comp_off[1];
+	ay.head = c->coef_head[1];
+	const Plan py = plan<T>(c, 1);
+	const uint64_t R = px.rows_per_tile, ny = c->n[1], nz = c->n[2];
+	const uint64_t plane_bytes = ny * c->pitch * sizeof(T);
+	const uint64_t P = std::max<uint64_t>(1, std::min<uint64_t>(nz, c->xy_slab_bytes / plane_bytes));
+	const uint64_t nslab = (nz + P - 1) / P, L = std::max<uint32_t>(1, c->xy_lag);
+	const uint64_t key = P | (L << 20) | (R << 40);
+	if (c->xy_key != key || !c->xy_segs.ptr)
+	{
+		std::vector<uint4> segs;
+		uint64_t first = 0;
+		std::vector<uint32_t> tx(nslab);
+		for (uint64_t k = 0; k < nslab + L; k++)
+		{
+			if (k < nslab)
+			{
+				const uint64_t rows_k = (std::min((k + 1) * P, nz) - k * P) * ny;
+				tx[k] = (uint32_t)((rows_k + R - 1) / R);
+				segs.push_back({ (uint32_t)first, (uint32_t)k, tx[k], 0u });
+				first += tx[k];
+			}
+			if (k >= L)
+			{
+				const uint64_t j = k - L;
+				const uint64_t ty = (std::min((j + 1) * P, nz) - j * P) * ay.xblocks;
+				segs.push_back({ (uint32_t)first, (uint32_t)j | kYSeg, (uint32_t)ty, tx[j] });
+				first += ty;
+			}
+		}
+		if (first >= 0xffffffffull)
+			return fail(PCG_ERR_UNSUPPORTED, "too many tiles for the fused x/y sweep");
+		int rc;
+		if ((rc = dalloc(c, c->xy_segs, segs.size() * sizeof(uint4))) ||
+			(rc = dalloc(c, c->xy_done, nslab * sizeof(uint32_t))))
+			return rc;
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->xy_segs.ptr, segs.data(), segs.size() * sizeof(uint4), cudaMemcpyHostToDevice,
+									 c->stream));
+		PCG_CUDA_TRY(stream_wait(c)); // the host table dies at scope exit
+		c->xy_key = key;
+		c->xy_nseg = (uint32_t)segs.size();
+		c->xy_total = (uint32_t)first;
+		c->xy_nslab = (uint32_t)nslab;
+	}
+	XYArgs f {};
+	f.segs = static_cast<const uint4*>(c->xy_segs.ptr);
+	f.nseg = c->xy_nseg;
+	f.total = c->xy_total;
+	f.planes = (uint32_t)P;
+	f.done = static_cast<uint32_t*>(c->xy_done.ptr);
+	f.ticket = static_cast<uint32_t*>(c->tickets.ptr) + 3;
+	f.ny = ny;
+	f.nz = nz;
+	const uint64_t smem = 128 + std::max(px.smem - 16, py.smem - 128);
+	if (smem > kMaxSmemBytes)
+		return fail(PCG_ERR_UNSUPPORTED, "fused x/y tiles too large for shared memory");
+	auto kernel = [&]() -> void (*)(SweepArgs, SweepArgs, const CUtensorMap, XYArgs) {
+		const bool mc = mass_check;
+		switch (c->S)
+		{
+		case 3: return mc ? sweep_xy_kernel<T, 3, kMcIn> : sweep_xy_kernel<T, 3, 0>;
+		case 4: return mc ? sweep_xy_kernel<T, 4, kMcIn> : sweep_xy_kernel<T, 4, 0>;
+		case 5: return mc ? sweep_xy_kernel<T, 5, kMcIn> : sweep_xy_kernel<T, 5, 0>;
+		case 6: return mc ? sweep_xy_kernel<T, 6, kMcIn> : sweep_xy_kernel<T, 6, 0>;
+		case 7: return mc ? sweep_xy_kernel<T, 7, kMcIn> : sweep_xy_kernel<T, 7, 0>;
+		case 8: return mc ? sweep_xy_kernel<T, 8, kMcIn> : sweep_xy_kernel<T, 8, 0>;
+		default: return mc ? sweep_xy_kernel<T, 0, kMcIn> : sweep_xy_kernel<T, 0, 0>;
+		}
+	}();
+	PCG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	int per_sm = 0;
+	PCG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kLanes, smem));
+	if (per_sm < 1)
+		return fail(PCG_ERR_UNSUPPORTED, "fused x/y tile does not fit in shared memory");
+	const uint64_t grid = std::min<uint64_t>((uint64_t)per_sm * (uint64_t)c->sm_count, c->xy_total);
+	PCG_CUDA_TRY(cudaMemsetAsync(f.ticket, 0, sizeof(uint32_t), c->stream));
+	PCG_CUDA_TRY(cudaMemsetAsync(f.done, 0, c->xy_nslab * sizeof(uint32_t), c->stream));
+	// minimal traffic of the two sweeps: the field read once and written once
+	const double bytes = 2.0 * (double)(c->V * c->S) * (double)sizeof(T);
+	cudaEvent_t ev;
+	launch_begin(c, K_SWEEP_XY, bytes, &ev);
+	kernel<<<(unsigned)grid, kLanes, smem, c->stream>>>(ax, ay, c->tmap[1], f);
+	launch_end(c, K_SWEEP_XY, ev);
+	PCG_CUDA_TRY(cudaGetLastError());
+	return PCG_OK;
 }
 
 template <typename T>
@@ -618,6 +927,13 @@ uint64_t sweep_smem_bytes(const Context* c, int axis)
 int launch_sweep_x(Context* c, bool mass_check)
 {
 	return c->wsize == 4 ? run_sweep_x<float>(c, mass_check) : run_sweep_x<double>(c, mass_check);
+}
+
+bool xy_fusable(const Context* c) { return c->fuse_xy && c->dims == 3 && x_substrate_mapping(c->S) && c->n[2] > 1; }
+
+int launch_sweep_xy(Context* c, bool mass_check)
+{
+	return c->wsize == 4 ? run_sweep_xy<float>(c, mass_check) : run_sweep_xy<double>(c, mass_check);
 }
 
 int launch_sweep_yz(Context* c, int axis, bool fuse_faces, bool mass_check)
