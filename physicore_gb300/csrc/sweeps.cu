@@ -649,8 +649,9 @@ int run_sweep_x(Context* c, bool mass_check)
 }
 
 // The fused x + y launch (sweep_xy_kernel): slabs of about c->xy_slab_bytes of
-// planes, y lagging x by c->xy_lag slabs.  The segment table is rebuilt when the
-// slab plan changes.
+// planes, y lagging x by at least c->xy_lag slabs and by at least twice the
+// tiles the resident CTAs hold.  The segment table is rebuilt when the slab plan
+// changes.
 template <typename T>
 int run_sweep_xy(Context* c, bool mass_check)
 {
@@ -672,7 +673,35 @@ int run_sweep_xy(Context* c, bool mass_check)
 	const uint64_t R = px.rows_per_tile, ny = c->n[1], nz = c->n[2];
 	const uint64_t plane_bytes = ny * c->pitch * sizeof(T);
 	const uint64_t P = std::max<uint64_t>(1, std::min<uint64_t>(nz, c->xy_slab_bytes / plane_bytes));
-	const uint64_t nslab = (nz + P - 1) / P, L = std::max<uint32_t>(1, c->xy_lag);
+	const uint64_t nslab = (nz + P - 1) / P;
+	// the persistent grid (every CTA holds one tile at a time)
+	const uint64_t smem = 128 + std::max(px.smem - 16, py.smem - 128);
+	if (smem > kMaxSmemBytes)
+		return fail(PCG_ERR_UNSUPPORTED, "fused x/y tiles too large for shared memory");
+	auto kernel = [&]() -> void (*)(SweepArgs, SweepArgs, const CUtensorMap, XYArgs) {
+		const bool mc = mass_check;
+		switch (c->S)
+		{
+		case 3: return mc ? sweep_xy_kernel<T, 3, kMcIn> : sweep_xy_kernel<T, 3, 0>;
+		case 4: return mc ? sweep_xy_kernel<T, 4, kMcIn> : sweep_xy_kernel<T, 4, 0>;
+		case 5: return mc ? sweep_xy_kernel<T, 5, kMcIn> : sweep_xy_kernel<T, 5, 0>;
+		case 6: return mc ? sweep_xy_kernel<T, 6, kMcIn> : sweep_xy_kernel<T, 6, 0>;
+		case 7: return mc ? sweep_xy_kernel<T, 7, kMcIn> : sweep_xy_kernel<T, 7, 0>;
+		case 8: return mc ? sweep_xy_kernel<T, 8, kMcIn> : sweep_xy_kernel<T, 8, 0>;
+		default: return mc ? sweep_xy_kernel<T, 0, kMcIn> : sweep_xy_kernel<T, 0, 0>;
+		}
+	}();
+	PCG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	int per_sm = 0;
+	PCG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kLanes, smem));
+	if (per_sm < 1)
+		return fail(PCG_ERR_UNSUPPORTED, "fused x/y tile does not fit in shared memory");
+	const uint64_t resident = (uint64_t)per_sm * (uint64_t)c->sm_count;
+	// the lag must exceed the tiles in flight (about one per resident CTA), else y
+	// tiles are handed out while their slab's x tiles are still being solved
+	const uint64_t slab_tiles = (P * ny + R - 1) / R + P * ay.xblocks;
+	const uint64_t L =
+		std::max<uint64_t>(std::max<uint32_t>(1, c->xy_lag), (2 * resident + slab_tiles - 1) / slab_tiles);
 	const uint64_t key = P | (L << 20) | (R << 40);
 	if (c->xy_key != key || !c->xy_segs.ptr)
 	{
@@ -719,28 +748,7 @@ int run_sweep_xy(Context* c, bool mass_check)
 	f.ticket = static_cast<uint32_t*>(c->tickets.ptr) + 3;
 	f.ny = ny;
 	f.nz = nz;
-	const uint64_t smem = 128 + std::max(px.smem - 16, py.smem - 128);
-	if (smem > kMaxSmemBytes)
-		return fail(PCG_ERR_UNSUPPORTED, "fused x/y tiles too large for shared memory");
-	auto kernel = [&]() -> void (*)(SweepArgs, SweepArgs, const CUtensorMap, XYArgs) {
-		const bool mc = mass_check;
-		switch (c->S)
-		{
-		case 3: return mc ? sweep_xy_kernel<T, 3, kMcIn> : sweep_xy_kernel<T, 3, 0>;
-		case 4: return mc ? sweep_xy_kernel<T, 4, kMcIn> : sweep_xy_kernel<T, 4, 0>;
-		case 5: return mc ? sweep_xy_kernel<T, 5, kMcIn> : sweep_xy_kernel<T, 5, 0>;
-		case 6: return mc ? sweep_xy_kernel<T, 6, kMcIn> : sweep_xy_kernel<T, 6, 0>;
-		case 7: return mc ? sweep_xy_kernel<T, 7, kMcIn> : sweep_xy_kernel<T, 7, 0>;
-		case 8: return mc ? sweep_xy_kernel<T, 8, kMcIn> : sweep_xy_kernel<T, 8, 0>;
-		default: return mc ? sweep_xy_kernel<T, 0, kMcIn> : sweep_xy_kernel<T, 0, 0>;
-		}
-	}();
-	PCG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-	int per_sm = 0;
-	PCG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kLanes, smem));
-	if (per_sm < 1)
-		return fail(PCG_ERR_UNSUPPORTED, "fused x/y tile does not fit in shared memory");
-	const uint64_t grid = std::min<uint64_t>((uint64_t)per_sm * (uint64_t)c->sm_count, c->xy_total);
+	const uint64_t grid = std::min<uint64_t>(resident, c->xy_total);
 	PCG_CUDA_TRY(cudaMemsetAsync(f.ticket, 0, sizeof(uint32_t), c->stream));
 	PCG_CUDA_TRY(cudaMemsetAsync(f.done, 0, c->xy_nslab * sizeof(uint32_t), c->stream));
 	// minimal traffic of the two sweeps: the field read once and written once
