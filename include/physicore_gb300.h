@@ -192,12 +192,12 @@ int pcg_mass(pcg_context* ctx, double* host);
  * |after*f - before| / |before|.  Enabling resets the record.  Contexts stepped by
  * a batch keep their check (pcg_batch_solve checks every domain that has it on). */
 int pcg_set_mass_check(pcg_context* ctx, int enable);
-/* Tuning of the x and y sweeps of 3-D meshes (3 to 32 substrates), which by
- * default run as one launch over z-slabs of about slab_bytes of field, the y
- * sweep of a slab starting `lag` slabs after its x sweep, so that the y sweep
- * reads the x sweep's output from L2 (the arithmetic is unchanged).  enable = 0
- * runs them as two launches; slab_bytes / lag of 0 keep the current values
- * (defaults 8 MiB and 2). */
+/* Fusion of the x and y sweeps of 3-D meshes (3 to 32 substrates), off by
+ * default: with enable = 1 they run as one launch over z-slabs of about
+ * slab_bytes of field, the y sweep of a slab starting at least `lag` slabs after
+ * its x sweep, so that the y sweep reads the x sweep's output from L2 (the
+ * arithmetic is unchanged; the field crosses HBM four times per step instead of
+ * six).  slab_bytes / lag of 0 keep the current values (defaults 8 MiB and 2). */
 int pcg_set_sweep_fusion(pcg_context* ctx, int enable, uint64_t slab_bytes, uint32_t lag);
 /* The last checked step's totals before and after its sweeps, the worst residual
  * since the check was enabled (each [S], NULL to skip) and the steps checked. */

@@ -227,7 +227,7 @@ struct Context
 	DeviceBuffer tickets;  // uint32 [4]: tile counters of the persistent sweeps ([3]: fused x/y)
 	// fused x/y sweeps: on/off (pcg_set_sweep_fusion), slab size, lag, and the
 	// segment table and per-slab counters of the current plan
-	bool fuse_xy = true;
+	bool fuse_xy = false;
 	uint64_t xy_slab_bytes = 8ull << 20;
 	uint32_t xy_lag = 2;
 	uint64_t xy_key = 0;

@@ -226,37 +226,62 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 {
 	using V = typename Vec16<T>::type;
 	constexpr int P = kBlock, VN = Vec16<T>::N, NV = P / VN;
+	constexpr bool kLo = sizeof(T) == 4;
 	const uint32_t st = STRIDE ? (uint32_t)STRIDE : rt_stride;
 	const uint32_t nb = n / P;
 	const T c = L.c;
+	// A block of points is a head block (coefficients loaded), a middle block (the
+	// middle constants, no per-point selection) or the block holding point n-1.
+	// The test is the same for every lane of a warp (one n and H per launch).
+	auto is_mid = [&](uint32_t j0) { return j0 >= L.H && j0 + P <= n - 1; };
+	// the middle coupling of the backward step, as bwd_step forms it per point
+	const T mbc = kLo ? L.mB * c : T(0);
 	T d = T(0);
 	{
 		T x[P], xn[P];
 		V e[NV], en[NV];
+		bool mid = false;
 		if (nb)
 		{
 #pragma unroll
 			for (int q = 0; q < P; q++)
 				x[q] = col[q * st];
-			fetch_block<T, V, NV>(L.hE, L.H, L.mE, L.lE, n, 0, e);
+			mid = is_mid(0);
+			if (!mid)
+				fetch_block<T, V, NV>(L.hE, L.H, L.mE, L.lE, n, 0, e);
 		}
 		for (uint32_t b = 0; b < nb; b++)
 		{
 			T* blk = col + (uint64_t)b * P * st;
+			bool mid_next = false;
 			if (b + 1 < nb)
 			{
 #pragma unroll
 				for (int q = 0; q < P; q++)
 					xn[q] = blk[(P + q) * st];
-				fetch_block<T, V, NV>(L.hE, L.H, L.mE, L.lE, n, (b + 1) * P, en);
+				mid_next = is_mid((b + 1) * P);
+				if (!mid_next)
+					fetch_block<T, V, NV>(L.hE, L.H, L.mE, L.lE, n, (b + 1) * P, en);
 			}
 			if constexpr ((MC & kMcIn) != 0)
 				acc_in->add_block(x);
-#pragma unroll
-			for (int q = 0; q < P; q++)
+			if (mid)
 			{
-				d = dev::fmadd(vget<V, T>(e[q / VN], q % VN), d, x[q]);
-				blk[q * st] = d;
+#pragma unroll
+				for (int q = 0; q < P; q++)
+				{
+					d = dev::fmadd(L.mE, d, x[q]);
+					blk[q * st] = d;
+				}
+			}
+			else
+			{
+#pragma unroll
+				for (int q = 0; q < P; q++)
+				{
+					d = dev::fmadd(vget<V, T>(e[q / VN], q % VN), d, x[q]);
+					blk[q * st] = d;
+				}
 			}
 #pragma unroll
 			for (int q = 0; q < P; q++)
@@ -264,6 +289,7 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 #pragma unroll
 			for (int v = 0; v < NV; v++)
 				e[v] = en[v];
+			mid = mid_next;
 		}
 		for (uint32_t j = nb * P; j < n; j++)
 		{
@@ -275,7 +301,6 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 		}
 	}
 	d = T(0);
-	constexpr bool kLo = sizeof(T) == 4;
 	for (int j = (int)n - 1; j >= (int)(nb * P); j--)
 	{
 		const T bl = kLo ? coef_at(L.hBl, L.H, L.mBl, L.lBl, n, (uint32_t)j) : T(0);
@@ -287,35 +312,62 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 	{
 		T x[P], xn[P];
 		V bb[NV], bn[NV], bl[NV], bln[NV];
+		bool mid = false;
 		if (nb)
 		{
 			const T* blk = col + (uint64_t)(nb - 1) * P * st;
 #pragma unroll
 			for (int q = 0; q < P; q++)
 				x[q] = blk[q * st];
-			fetch_block<T, V, NV>(L.hB, L.H, L.mB, L.lB, n, (nb - 1) * P, bb);
-			if constexpr (kLo)
-				fetch_block<T, V, NV>(L.hBl, L.H, L.mBl, L.lBl, n, (nb - 1) * P, bl);
+			mid = is_mid((nb - 1) * P);
+			if (!mid)
+			{
+				fetch_block<T, V, NV>(L.hB, L.H, L.mB, L.lB, n, (nb - 1) * P, bb);
+				if constexpr (kLo)
+					fetch_block<T, V, NV>(L.hBl, L.H, L.mBl, L.lBl, n, (nb - 1) * P, bl);
+			}
 		}
 		for (int b = (int)nb - 1; b >= 0; b--)
 		{
 			T* blk = col + (uint64_t)b * P * st;
+			bool mid_next = false;
 			if (b > 0)
 			{
 #pragma unroll
 				for (int q = 0; q < P; q++)
 					xn[q] = blk[(q - P) * (int)st];
-				fetch_block<T, V, NV>(L.hB, L.H, L.mB, L.lB, n, (uint32_t)(b - 1) * P, bn);
-				if constexpr (kLo)
-					fetch_block<T, V, NV>(L.hBl, L.H, L.mBl, L.lBl, n, (uint32_t)(b - 1) * P, bln);
+				mid_next = is_mid((uint32_t)(b - 1) * P);
+				if (!mid_next)
+				{
+					fetch_block<T, V, NV>(L.hB, L.H, L.mB, L.lB, n, (uint32_t)(b - 1) * P, bn);
+					if constexpr (kLo)
+						fetch_block<T, V, NV>(L.hBl, L.H, L.mBl, L.lBl, n, (uint32_t)(b - 1) * P, bln);
+				}
 			}
 			T y[P];
-#pragma unroll
-			for (int q = P - 1; q >= 0; q--)
+			if (mid)
 			{
-				d = bwd_step(c, d, x[q], vget<V, T>(bb[q / VN], q % VN), kLo ? vget<V, T>(bl[q / VN], q % VN) : T(0));
-				blk[q * st] = d;
-				y[q] = d;
+#pragma unroll
+				for (int q = P - 1; q >= 0; q--)
+				{
+					if constexpr (kLo)
+						d = dev::fmadd(mbc, d, dev::fmadd(x[q], L.mB, x[q] * L.mBl));
+					else
+						d = dev::fmadd(c, d, x[q]) * L.mB;
+					blk[q * st] = d;
+					y[q] = d;
+				}
+			}
+			else
+			{
+#pragma unroll
+				for (int q = P - 1; q >= 0; q--)
+				{
+					d = bwd_step(c, d, x[q], vget<V, T>(bb[q / VN], q % VN),
+								 kLo ? vget<V, T>(bl[q / VN], q % VN) : T(0));
+					blk[q * st] = d;
+					y[q] = d;
+				}
 			}
 			if constexpr ((MC & kMcOut) != 0)
 				acc_out->add_block(y);
@@ -329,6 +381,7 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 				if constexpr (kLo)
 					bl[v] = bln[v];
 			}
+			mid = mid_next;
 		}
 	}
 }
