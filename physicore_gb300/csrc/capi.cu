@@ -354,42 +354,65 @@ static void precompute_axis(uint64_t n, uint64_t S, uint64_t shape, uint64_t dim
 // for each neighbour) makes M' conserve mass exactly as the reference does; with
 // the exact e and c it gives b'[j] itself.  Plain FP32 rounding of b', e and c
 // otherwise biases every step the same way, and over hundreds of steps that drift
-// dominates the FP32 error.  Where the sequence has converged to its middle value
-// (relative change below 1e-15) the middle value is kept, so that the compressed
-// tables hold a single constant there.
+// dominates the FP32 error.
 static void colsum_multipliers(uint64_t n, uint64_t S, uint64_t shape, uint64_t dims, double dt, const double* D,
 							   const double* decay, const std::vector<double>& e, const std::vector<double>& cc,
-							   std::vector<double>& B)
+							   std::vector<double>& B, std::vector<float>& Bhi)
 {
 	const double h2 = (double)(shape * shape);
 	B.assign(n * S, 0.0);
+	Bhi.assign(n * S, 0.0f);
 	for (uint64_t s = 0; s < S; s++)
 	{
 		const double r = dt * D[s] / h2;
 		const float C32 = (float)cc[s];
-		double Cp = 0.0; // C'[j-1]
-		for (uint64_t j = 0; j < n; j++)
-		{
+		auto kappa = [&](uint64_t j) {
 			double diag = 1 + decay[s] * dt / (double)dims + 2 * dt * D[s] / h2;
 			if (j == 0 || j == n - 1)
 				diag -= dt * D[s] / h2;
-			const double kappa = diag - (j > 0 ? r : 0.0) - (j + 1 < n ? r : 0.0);
-			const double Ej = j + 1 < n ? (double)(float)e[j * S + s] : 0.0;
-			const double Em = j > 0 ? (double)(float)e[(j - 1) * S + s] : 0.0;
-			const double b = (1.0 - Ej) / (kappa + (1.0 - Em) * Cp);
-			B[j * S + s] = b;
-			const volatile float K = (float)b * C32; // the device's FP32 product
-			Cp = (double)K / b;
-		}
-		if (n >= 3) // keep the converged middle value exactly constant
+			return diag - (j > 0 ? r : 0.0) - (j + 1 < n ? r : 0.0);
+		};
+		auto E = [&](int64_t j) { return j >= 0 && (uint64_t)j + 1 < n ? (double)(float)e[j * S + s] : 0.0; };
+		auto K = [&](float hi) {
+			const volatile float k = hi * C32; // the device's FP32 product
+			return (double)k;
+		};
+		double Cp = 0.0; // C'[j-1]
+		for (uint64_t j = 0; j < n; j++)
 		{
-			const double m = B[(n - 2) * S + s];
-			for (uint64_t j = n - 2; j-- > 1;)
+			const double b = (1.0 - E(j)) / (kappa(j) + (1.0 - E((int64_t)j - 1)) * Cp);
+			B[j * S + s] = b;
+			Bhi[j * S + s] = (float)b;
+			Cp = K((float)b) / b;
+		}
+		if (n < 3)
+			continue;
+		// The middle: FP32 rounding of B feeds back through the coupling, so the
+		// sequence can settle into a two-value cycle instead of a constant.  The
+		// middle instead takes the hi part Bh of the last middle value, the coupling
+		// K = RN32(Bh c) and the exact fixed point (1 - E)(1 - K) / kappa of the
+		// column-sum condition, stored as Bh + lo (lo may span a few ulps of Bh);
+		// the sequence hands over to it at the first point whose predecessor has
+		// the same hi part and lies within 1e-7 of it (that one column's sum is then
+		// off by at most about 1e-7; every other column is exact).
+		const double Em = E((int64_t)n - 3);
+		const float Bh = (float)B[(n - 2) * S + s];
+		const double Km = K(Bh);
+		const double Bmid = (1.0 - Em) * (1.0 - Km) / kappa(n - 2);
+		for (uint64_t j = 1; j + 1 < n; j++)
+		{
+			if (E(j) != Em || E((int64_t)j - 1) != Em || Bhi[(j - 1) * S + s] != Bh ||
+				!(std::fabs(B[(j - 1) * S + s] / Bmid - 1.0) < 1e-7))
+				continue;
+			for (uint64_t k = j; k + 1 < n; k++)
 			{
-				if (std::fabs(B[j * S + s] / m - 1.0) >= 1e-15)
-					break;
-				B[j * S + s] = m;
+				B[k * S + s] = Bmid;
+				Bhi[k * S + s] = Bh;
 			}
+			const double bl = 1.0 / (kappa(n - 1) + (1.0 - E((int64_t)n - 2)) * Km / Bmid);
+			B[(n - 1) * S + s] = bl;
+			Bhi[(n - 1) * S + s] = (float)bl;
+			break;
 		}
 	}
 }
@@ -409,14 +432,17 @@ static int upload_coefficients(Context* c)
 	{
 		const uint64_t n = c->n[axis];
 		std::vector<double> b, e, cc, B;
+		std::vector<float> Bhi;
 		precompute_axis(n, S, c->voxel[axis], (uint64_t)c->dims, c->dt, c->D.data(), c->decay.data(), b, e, cc);
 		if (kLo)
 		{
 			colsum_multipliers(n, S, c->voxel[axis], (uint64_t)c->dims, c->dt, c->D.data(), c->decay.data(), e, cc,
-							   B);
+							   B, Bhi);
 			b = B;
 		}
-		auto lo = [&](uint64_t k) { return kLo ? (T)(b[k] - (double)(T)b[k]) : T(0); };
+		// FP32: the multiplier's hi part (chosen by colsum_multipliers) and lo = B - hi
+		auto hi = [&](uint64_t k) { return kLo ? (T)Bhi[k] : (T)b[k]; };
+		auto lo = [&](uint64_t k) { return kLo ? (T)(b[k] - (double)Bhi[k]) : T(0); };
 		const uint64_t cp = coef_row_pitch(n);
 		const uint64_t len = axis == 0 ? coef_table_len(n, S, sizeof(T)) : S * cp;
 		const uint64_t blo_off = 2 * len + round_up(S, 16 / sizeof(T));
@@ -434,14 +460,14 @@ static int upload_coefficients(Context* c)
 				uint64_t h = n;
 				if (n >= 2)
 				{
-					const T bm = (T)b[(n - 2) * S + sub];
+					const T bm = hi((n - 2) * S + sub);
 					const T em = n >= 3 ? (T)e[(n - 3) * S + sub] : T(0);
 					h = n - 2;
 					const T blm = lo((n - 2) * S + sub);
 					while (h > 0)
 					{
 						const uint64_t i = h - 1;
-						const T bi = (T)b[i * S + sub];
+						const T bi = hi(i * S + sub);
 						const T ei = i == 0 ? T(0) : (T)e[(i - 1) * S + sub];
 						if (bi != bm || ei != em || lo(i * S + sub) != blm)
 							break;
@@ -466,7 +492,7 @@ static int upload_coefficients(Context* c)
 			for (uint64_t s = 0; s < S; s++)
 			{
 				const uint64_t at = axis == 0 ? i * S + s : s * cp + i;
-				tab[at] = (T)b[i * S + s];
+				tab[at] = hi(i * S + s);
 				tab[len + at] = i == 0 ? T(0) : (T)e[(i - 1) * S + s];
 				if (kLo)
 					tab[blo_off + at] = lo(i * S + s);
@@ -483,15 +509,15 @@ static int upload_coefficients(Context* c)
 			{
 				for (uint64_t i = 0; i < std::min(H, n); i++)
 				{
-					hB[sub * H + i] = (T)b[i * S + sub];
+					hB[sub * H + i] = hi(i * S + sub);
 					hE[sub * H + i] = i == 0 ? T(0) : (T)e[(i - 1) * S + sub];
 					if (kLo)
 						hBl[sub * H + i] = lo(i * S + sub);
 				}
 				const uint64_t m = n >= 2 ? n - 2 : 0;
-				k[sub] = (T)b[m * S + sub];
+				k[sub] = hi(m * S + sub);
 				k[kS + sub] = m == 0 ? T(0) : (T)e[(m - 1) * S + sub];
-				k[2 * kS + sub] = (T)b[(n - 1) * S + sub];
+				k[2 * kS + sub] = hi((n - 1) * S + sub);
 				k[3 * kS + sub] = n == 1 ? T(0) : (T)e[(n - 2) * S + sub];
 				k[4 * kS + sub] = (T)cc[sub];
 				if (kLo)
