@@ -389,7 +389,7 @@ int pcg_server_get_stats(pcg_server* server, pcg_server_stats* stats);
  *    done and cannot be recorded into a CUDA graph by stream capture.
  *  - Scratch comes from one fixed 16 MiB array in device memory that every GPU
  *    loading this library holds until the process exits; a problem that needs
- *    more (about 8 bytes per voxel plus 21 + 24*substrates bytes per agent) is
+ *    more (about 8 bytes per voxel plus 25 + 24*substrates bytes per agent) is
  *    rejected with PCG_ERR_UNSUPPORTED, as are meshes of 2^32 - 1 or more voxels,
  *    2^32 - 1 or more agents and fields of 2^32 or more elements (pitch * ny *
  *    nz).  grid_shape must be 1 on the axes beyond dims (PCG_ERR_INVALID).  The

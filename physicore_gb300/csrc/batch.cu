@@ -1035,6 +1035,7 @@ BatchDomain describe_domain(pcg_batch* b, size_t d)
 	D.dt = c->dt;
 	D.cells = make_cell_args(c);
 	D.cells.err = static_cast<uint32_t*>(b->d_err.ptr);
+	D.cells.list_word = 1; // the batch's per-warp ballot lists shared-voxel agents in word 1
 	if (c->mass_check && c->mc_tot.ptr && c->mc_out.ptr)
 	{
 		D.mc_tot = static_cast<double*>(c->mc_tot.ptr);

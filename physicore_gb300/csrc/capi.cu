@@ -825,7 +825,7 @@ static int alloc_agents(Context* c, uint64_t A)
 		return rc;
 	if ((rc = dalloc(c, c->a_rank, std::max<uint64_t>(A, 1) * sizeof(uint32_t))))
 		return rc;
-	if ((rc = dalloc(c, c->a_sorted, std::max<uint64_t>(A, 1) * sizeof(uint32_t))))
+	if ((rc = dalloc(c, c->a_sorted, std::max<uint64_t>(A, 1) * 2 * sizeof(uint32_t))))
 		return rc;
 	DeviceBuffer* rs[] = { &c->a_num, &c->a_den, &c->a_fac, &c->a_rnum, &c->a_rden, &c->a_rfac };
 	for (DeviceBuffer* b : rs)
@@ -929,7 +929,7 @@ uint64_t estimate_device_bytes(const Context* c)
 	else if (c->bulk_mode == PCG_BULK_PER_VOXEL)
 		b += 3 * rows * pitch * w;
 	if (A)
-		b += A * (c->dims * 8 + 6 * S * 8 + 8 + 1 + 8 + 5 + 8 + 6 * S * w) + V * 8;
+		b += A * (c->dims * 8 + 6 * S * 8 + 8 + 1 + 8 + 5 + 12 + 6 * S * w) + V * 8;
 	return b;
 }
 

@@ -42,7 +42,7 @@ __global__ void cells_place_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	if (i == 0)
-		a.flags[0] = a.flags[1] = a.flags[2] = 0;
+		a.flags[0] = a.flags[1] = a.flags[2] = a.flags[3] = 0;
 	uint32_t v = kNoAgent;
 	if (i < a.A)
 	{
@@ -53,13 +53,16 @@ __global__ void cells_place_kernel(CellArgs a)
 	count_rank(a, i, v);
 }
 
-constexpr unsigned kClassifyBlock = 512;
+constexpr unsigned kClassifyBlock = 1024;
 
 // classify: roles from count and rank (cell_solver.cpp:102-127: every agent but
 // the winner of a shared voxel is a conflict); the agents of shared voxels listed
-// in agent order (flags[1]); each winner reserves its voxel's group of slots
-// (owner[v] = first slot, flags[2] counts slots) and clears its reduced row.  One
-// atomic per block for each counter (block-wide scans).
+// in agent order (flags[2]); each winner reserves its voxel's group of slots
+// (owner[v] = first slot, flags[3] counts slots) and clears its reduced row.  A
+// block scans both counts and reserves its ranges with one 64-bit atomic on the
+// adjacent, 8-byte aligned words flags[2..3] (list entries low, slots high;
+// neither total reaches 2^32, so no carry crosses): same-address atomics that
+// return a value serialise, so there is one per 1024 agents.
 template <typename T>
 __global__ void __launch_bounds__(kClassifyBlock) cells_classify_kernel(CellArgs a)
 {
@@ -104,8 +107,12 @@ __global__ void __launch_bounds__(kClassifyBlock) cells_classify_kernel(CellArgs
 		}
 		if (lane == 31)
 		{
-			base[0] = p0 ? atomicAdd(a.flags + 1, p0) : 0u;
-			base[1] = p1 ? atomicAdd(a.flags + 2, p1) : 0u;
+			unsigned long long old = 0ull;
+			if (p0 | p1)
+				old = atomicAdd(reinterpret_cast<unsigned long long*>(a.flags + 2),
+								((unsigned long long)p1 << 32) | (unsigned long long)p0);
+			base[0] = (uint32_t)old;
+			base[1] = (uint32_t)(old >> 32);
 		}
 		uint32_t e0 = __shfl_up_sync(0xffffffffu, p0, 1), e1 = __shfl_up_sync(0xffffffffu, p1, 1);
 		if (lane == 0)
@@ -127,15 +134,16 @@ __global__ void __launch_bounds__(kClassifyBlock) cells_classify_kernel(CellArgs
 	}
 }
 
-// group: every agent of a shared voxel writes its index into its voxel's group.
+// group: every agent of a shared voxel writes (its index, its voxel) into its
+// voxel's group, so the group sums read their keys in slot order.
 __global__ void cells_group_kernel(CellArgs a)
 {
-	const uint32_t count = __ldg(a.flags + 1);
+	const uint32_t count = __ldg(a.flags + a.list_word);
 	for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < count; j += (uint64_t)gridDim.x * blockDim.x)
 	{
 		const uint32_t i = __ldg(a.shared + j);
 		const uint32_t v = __ldg(a.vox + i);
-		a.sorted[__ldg(a.owner + v) + __ldg(a.rank + i)] = i;
+		a.sorted[__ldg(a.owner + v) + __ldg(a.rank + i)] = make_uint2(i, v);
 	}
 }
 
@@ -147,7 +155,7 @@ __global__ void cells_group_kernel(CellArgs a)
 template <typename T>
 __global__ void cells_group_sum_kernel(CellArgs a)
 {
-	const uint32_t count = __ldg(a.flags + 1);
+	const uint32_t count = __ldg(a.flags + a.list_word);
 	const uint32_t lane = threadIdx.x & 31;
 	const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
 	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -165,8 +173,9 @@ __global__ void cells_group_sum_kernel(CellArgs a)
 		uint32_t i = 0, v = kNoAgent;
 		if (j < count)
 		{
-			i = __ldg(a.sorted + j);
-			v = __ldg(a.vox + i);
+			const uint2 iv = __ldg(a.sorted + j);
+			i = iv.x;
+			v = iv.y;
 		}
 		const uint32_t group = __match_any_sync(0xffffffffu, v);
 		const uint32_t first = __ffs(group) - 1, last = 31 - __clz(group);
@@ -176,7 +185,7 @@ __global__ void cells_group_sum_kernel(CellArgs a)
 		if (writer)
 		{
 			const uint32_t seg0 = __ldg(a.owner + v), cnt = __ldg(a.counts + v);
-			w = __ldg(a.sorted + seg0);
+			w = __ldg(&a.sorted[seg0].x);
 			head = j0 + first == seg0;
 			whole = head && j0 + last == (uint64_t)seg0 + cnt - 1;
 		}
@@ -253,7 +262,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) cells_apply_kerne
 template <typename T>
 __global__ void cells_internalize_kernel(CellArgs a)
 {
-	const uint32_t count = __ldg(a.flags + 1);
+	const uint32_t count = __ldg(a.flags + a.list_word);
 	for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < count; j += (uint64_t)gridDim.x * blockDim.x)
 		agent_internalize<T>(a, __ldg(a.shared + j));
 }
@@ -326,7 +335,8 @@ CellArgs make_cell_args(const Context* c)
 	a.terms = 1;
 	a.pairs = c->wsize == 4 ? 1 : 0; // FP32 contexts store internalized amounts as float pairs
 	a.rank = static_cast<uint32_t*>(c->a_rank.ptr);
-	a.sorted = static_cast<uint32_t*>(c->a_sorted.ptr);
+	a.sorted = static_cast<uint2*>(c->a_sorted.ptr);
+	a.list_word = 2; // the grouped ballot (a batch sets 1 for its per-warp ballot)
 	set_fast_locate(a);
 	return a;
 }
@@ -356,7 +366,8 @@ static int run_ballot(Context* c, const CellArgs& a, cudaStream_t stream, int sm
 		launch_begin(c, K_CELLS_BALLOT, A * (4 + 4 + 4 + 1), &ev);
 	cells_classify_kernel<T><<<cgrid, kClassifyBlock, 0, stream>>>(a);
 	if (c && c->timing && c->h_words) // list length for the per-agent byte counts
-		PCG_CUDA_TRY(cudaMemcpyAsync(c->h_words + 2, a.flags + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+		PCG_CUDA_TRY(
+			cudaMemcpyAsync(c->h_words + 2, a.flags + a.list_word, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
 	if (c)
 		launch_end(c, K_CELLS_BALLOT, ev, 4.0 + 3 * S * w);
 	PCG_CUDA_TRY(cudaGetLastError());
@@ -364,7 +375,7 @@ static int run_ballot(Context* c, const CellArgs& a, cudaStream_t stream, int sm
 		launch_begin(c, K_CELLS_GROUP, 0.0, &ev);
 	cells_group_kernel<<<lgrid, block, 0, stream>>>(a);
 	if (c)
-		launch_end(c, K_CELLS_GROUP, ev, 20.0);
+		launch_end(c, K_CELLS_GROUP, ev, 24.0);
 	PCG_CUDA_TRY(cudaGetLastError());
 	if (c)
 		launch_begin(c, K_CELLS_REDUCE, 0.0, &ev);
@@ -468,6 +479,7 @@ int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream)
 	a.pairs = 0; // the caller's FP64 amounts
 	a.rank = b.rank;
 	a.sorted = b.sorted;
+	a.list_word = 2;
 	set_fast_locate(a);
 	const uint64_t V = b.n[0] * b.n[1] * b.n[2];
 	const unsigned block = 256;

@@ -45,8 +45,9 @@ struct CellArgs
 	uint32_t* owner;
 	uint32_t* counts;
 	uint8_t* role;    // [A] ballot role
-	uint32_t* shared; // [A] agents of voxels that hold several, flags[1] of them
-	uint32_t* flags;  // [0] conflict, [1] entries of `shared`
+	uint32_t* shared; // [A] agents of voxels that hold several, flags[list_word] of them
+	uint32_t* flags;  // [0] conflict; entries of `shared` in word list_word; grouped ballot: [2..3]
+	uint32_t list_word; // 1 (batches: per-warp ballot) or 2 (grouped ballot: words 2, 3 = list, slots)
 	uint32_t* err;
 	void* field;
 	int internalized;
@@ -60,7 +61,7 @@ struct CellArgs
 	// voxel-grouped ballot (cells.cu): rank of each agent in its voxel, and the
 	// agents of shared voxels grouped by voxel (slot order)
 	uint32_t* rank;   // [A]
-	uint32_t* sorted; // [A]
+	uint2* sorted;    // [A] (agent, voxel) pairs
 };
 
 // The fast-location constants of a mesh: float bounds and reciprocal voxel edges,
@@ -300,7 +301,7 @@ __device__ __forceinline__ void list_shared(const CellArgs& a, uint64_t i, bool 
 //   classify:  roles from count and rank; the agents of shared voxels are listed
 //              in agent order (for the internalized pass) and each winner
 //              reserves its voxel's group of slots
-//   group:     every listed agent writes its index into its voxel's group
+//   group:     every listed agent writes (index, voxel) into its voxel's group
 //   group sum: warps reduce consecutive slots by voxel; a group that lies within
 //              one warp is stored once, a group split across warps adds its parts
 //              to the winner's row (cleared by classify) with atomics

@@ -14,9 +14,9 @@
 
 namespace {
 
-// 16 MiB of scratch: 8 bytes per voxel (group start + count) plus 21 + 24*S bytes
+// 16 MiB of scratch: 8 bytes per voxel (group start + count) plus 25 + 24*S bytes
 // per agent (voxel index, field offset, shared-voxel list entry, rank in the voxel,
-// grouped slot, ballot role, six FP32 terms per substrate).
+// grouped (agent, voxel) slot, ballot role, six FP32 terms per substrate).
 constexpr size_t kScratchBytes = size_t(16) << 20;
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
@@ -94,7 +94,7 @@ extern "C" int pcg_cells_noalloc(float* field, uint64_t pitch, int dims, const i
 	if (V > kScratchBytes || terms > kScratchBytes)
 		return fail(PCG_ERR_UNSUPPORTED,
 					"pcg_cells_noalloc: the mesh and agents need more than the fixed " + std::to_string(kScratchBytes) +
-						" bytes of scratch (about 8 bytes per voxel + (21 + 24*S) bytes per agent)");
+						" bytes of scratch (about 8 bytes per voxel + (25 + 24*S) bytes per agent)");
 
 	// scratch layout: flags | err | owner[V] | counts[V] | vox[A] | foff[A] | shared[A] | rank[A] | sorted[A] |
 	// role[A] | 6 x terms[A*S]
@@ -116,7 +116,7 @@ extern "C" int pcg_cells_noalloc(float* field, uint64_t pitch, int dims, const i
 	const size_t o_rank = off;
 	off = align256(off + agents * 4);
 	const size_t o_sorted = off;
-	off = align256(off + agents * 4);
+	off = align256(off + agents * 8);
 	const size_t o_role = off;
 	off = align256(off + agents);
 	size_t o_terms[6];
@@ -129,7 +129,7 @@ extern "C" int pcg_cells_noalloc(float* field, uint64_t pitch, int dims, const i
 		return fail(PCG_ERR_UNSUPPORTED,
 					"pcg_cells_noalloc: the mesh and agents need " + std::to_string(off) +
 						" bytes of scratch, more than the fixed " + std::to_string(kScratchBytes) +
-						" (about 8 bytes per voxel + (21 + 24*S) bytes per agent)");
+						" (about 8 bytes per voxel + (25 + 24*S) bytes per agent)");
 
 	int device = 0;
 	cudaError_t e = cudaGetDevice(&device);
@@ -170,7 +170,7 @@ extern "C" int pcg_cells_noalloc(float* field, uint64_t pitch, int dims, const i
 	b.foff = reinterpret_cast<uint32_t*>(base + o_foff);
 	b.shared = reinterpret_cast<uint32_t*>(base + o_shared);
 	b.rank = reinterpret_cast<uint32_t*>(base + o_rank);
-	b.sorted = reinterpret_cast<uint32_t*>(base + o_sorted);
+	b.sorted = reinterpret_cast<uint2*>(base + o_sorted);
 	b.role = base + o_role;
 	float** t[6] = { &b.num, &b.den, &b.fac, &b.rnum, &b.rden, &b.rfac };
 	for (int k = 0; k < 6; k++)

@@ -290,7 +290,7 @@ struct Context
 	DeviceBuffer a_role;                  // uint8 [A]: ballot role (cells_device.cuh)
 	DeviceBuffer a_shared;                // uint32 [A]: agents of voxels that hold several
 	DeviceBuffer a_rank;                  // uint32 [A]: rank of the agent in its voxel
-	DeviceBuffer a_sorted;                // uint32 [A]: agents of shared voxels grouped by voxel
+	DeviceBuffer a_sorted;                // uint2 [A]: (agent, voxel) of shared voxels grouped by voxel
 	DeviceBuffer a_num, a_den, a_fac;     // real [A*S]
 	DeviceBuffer a_rnum, a_rden, a_rfac;  // real [A*S]
 	DeviceBuffer owner;                   // uint32 [V]: winning agent per voxel (batches), or the first
@@ -358,8 +358,10 @@ struct CellStepBuffers
 	double* internal;
 	int internalized;
 	float* field;
-	// scratch: vox/foff/shared/rank/sorted/role [A], owner/counts [V], flags/err [4] each, terms [A*S] each
-	uint32_t *vox, *foff, *shared, *rank, *sorted, *owner, *counts, *flags, *err;
+	// scratch: vox/foff/shared/rank/role [A], sorted [A] pairs, owner/counts [V], flags/err [4] each,
+	// terms [A*S] each
+	uint32_t *vox, *foff, *shared, *rank, *owner, *counts, *flags, *err;
+	uint2* sorted;
 	uint8_t* role;
 	float *num, *den, *fac, *rnum, *rden, *rfac;
 };
