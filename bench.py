@@ -834,7 +834,10 @@ def run_serve(args, local):
     from physicore_gb300 import workloads as W
     stream = W.ServedStream(duration=args.serve_duration)
     n = len(stream)
-    srv = pcg.Server(pcg.FP32, device=local, steps_per_tick=args.serve_tick, reserve_bytes=1 << 30)
+    # a bounded queue sheds load under sustained overload (refused requests come
+    # back at once); 0 keeps the server's default (2^20)
+    srv = pcg.Server(pcg.FP32, device=local, steps_per_tick=args.serve_tick, reserve_bytes=1 << 30,
+                     max_queue=args.serve_max_queue)
     elems = [int(np.prod(stream.sides[i]) * stream.S[i]) for i in range(n)]
     # pinned slices for the fields of requests in flight; beyond 16 GB of them (a
     # backlog under overload) a request gets a pageable buffer instead
@@ -871,6 +874,7 @@ def run_serve(args, local):
     th.start()
     lat_dev, lat_host, statuses, vss_done, agent_steps = [], [], {}, 0, 0
     lat_by_req = {}
+    vss_admitted = [0]
     t_first = t_last = None
     got = 0
     profile, next_sample = [], 0.5  # [t, active, queued, cumulative vss, submitted] every half second
@@ -889,6 +893,7 @@ def run_serve(args, local):
             if off is not None:
                 arena.give(off, elems[i])
             if r["status"] == "done":
+                vss_admitted[0] += stream.vss(i)
                 lat_host.append(time.perf_counter() - submit_wall[i])
                 lat_dev.append(r["t_done"] - r["t_submit"])
                 lat_by_req[i] = r["t_done"] - r["t_submit"]
@@ -936,6 +941,8 @@ def run_serve(args, local):
                         "log-uniform [32,256] per axis, 1-8 substrates, 0-200,000 agents, steps log-uniform "
                         "[10,1000], FP32",
             "requests": n, "statuses": statuses, "offered_vss_per_s": offered,
+            "max_queue": args.serve_max_queue or None,
+            "completed_vss_per_arrival_s": vss_admitted[0] / args.serve_duration,
             "value": served, "unit": UNIT,
             "agent_steps_per_s": agent_steps / (t_last - t_first) if t_last else None,
             "plain": {"value": vss_plain / plain_s, "requests": len(sample),
@@ -1050,6 +1057,8 @@ def main():
     ap.add_argument("--serve-tick", type=int, default=8, help="steps between admission points")
     ap.add_argument("--only-serve", action="store_true", help="run only the served request stream")
     ap.add_argument("--serve-plain-sample", type=int, default=100, help="requests timed one after another")
+    ap.add_argument("--serve-max-queue", type=int, default=0,
+                    help="queued requests beyond which submissions are refused (0: no practical limit)")
     ap.add_argument("--dense-steps", type=int, default=100, help="steps of the dense-agent workload (0: skip)")
     ap.add_argument("--only-dense", action="store_true", help="run only the dense-agent workload")
     args = ap.parse_args()
