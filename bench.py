@@ -731,14 +731,26 @@ def run_batched(args, local, clock_sampler=None):
     batched_launches = b.launch_count()
 
     # parity: both sets have taken warm + steps steps
-    worst, worst_dom, counts_ok = 0.0, -1, True
+    worst, worst_dom, counts_ok, worst_fields = 0.0, -1, True, None
     for k, (sp, sb) in enumerate(zip(plain, batched)):
         fp = sp.get_field(dtype=np.float32)
         fb = sb.get_field(dtype=np.float32)
         e, _ = field_error(fb, fp)
         if e > worst:
-            worst, worst_dom = e, k
+            worst, worst_dom, worst_fields = e, k, (fp, fb)
         counts_ok &= bool(np.array_equal(sp.get_counts(), sb.get_counts()))
+    # the most different domain, both paths against the FP64 oracle after the same steps
+    vs_oracle = None
+    if worst_dom >= 0:
+        from oracle import oracle
+        import itertools
+        p_w = next(itertools.islice(W.batched_uneven(count=worst_dom + 1), worst_dom, None))
+        o = W.apply(oracle.OracleSolver(threads=cpu_threads()), p_w)
+        for _ in range(warm + steps):
+            o.solve(1)
+        fo = o.get_field()
+        vs_oracle = {"plain": field_error(worst_fields[0], fo), "batched": field_error(worst_fields[1], fo)}
+        vs_oracle = {k: {"max_rel": v[0], "l2_rel": v[1]} for k, v in vs_oracle.items()}
 
     # per-kernel times from a short run of direct (event-timed) launches
     b.set_kernel_timing(True)
@@ -773,6 +785,7 @@ def run_batched(args, local, clock_sampler=None):
                        "autotune_s": round(tune_s, 2)},
            "speedup": batched_v / plain_v, "unit": UNIT,
            "parity": {"max_rel_vs_plain": worst, "worst_domain": worst_dom, "counts_equal": counts_ok,
+                      "worst_domain_vs_fp64_oracle": vs_oracle,
                       "steps": warm + steps, "tolerance": FP32_RTOL,
                       "normaliser": "per domain and substrate: max |plain field|"},
            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(dgb, 1), "peak": peak, "unit": "GB/s",

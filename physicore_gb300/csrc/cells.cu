@@ -149,9 +149,9 @@ __global__ void cells_group_kernel(CellArgs a)
 
 // group sum: a warp takes 32 consecutive slots and sums each voxel's terms with a
 // segmented scan (lanes of one voxel are consecutive); the last lane of each
-// voxel's run writes the winner's row: sum num, 1 + sum den, sum fac -- stored
-// when the run is the voxel's whole group, else added with atomics (the part
-// holding the group's first slot adds the 1).
+// voxel's run writes the winner's row: sum num, sum den (plus 1 in FP64 builds),
+// sum fac -- stored when the run is the voxel's whole group, else added with
+// atomics (the part holding the group's first slot adds the 1).
 template <typename T>
 __global__ void cells_group_sum_kernel(CellArgs a)
 {
@@ -223,7 +223,7 @@ __global__ void cells_group_sum_kernel(CellArgs a)
 			}
 			if (writer)
 			{
-				if (head)
+				if (head && sizeof(T) == 8) // FP64 rows hold 1 + sum den; FP32 rows the bare sum (fp32_update)
 #pragma unroll
 					for (int q = 0; q < kSubBatch; q++)
 						d_[q] += T(1);

@@ -267,7 +267,9 @@ __device__ __forceinline__ uint8_t agent_reduce(const CellArgs& a, uint64_t i)
 		const uint64_t k = i * a.S + s;
 		const uint64_t kw = (uint64_t)w * a.S + s;
 		atomicAdd(rnum + kw, num[k]);
-		atomicAdd(rden + kw, conflict ? den[k] : den[k] + T(1));
+		// the winner adds the 1 of the denominator (FP64 builds; FP32 rows hold the
+		// bare sum of den, see fp32_update)
+		atomicAdd(rden + kw, (conflict || sizeof(T) == 4) ? den[k] : den[k] + T(1));
 		atomicAdd(rfac + kw, fac[k]);
 	}
 	return role;
@@ -435,12 +437,26 @@ __device__ __forceinline__ void row_store(T* __restrict__ p, uint32_t s0, uint32
 			p[s0 + q] = v[q];
 }
 
+// The FP32 density update of a voxel from its sums num, den, fac (den without the
+// reference's added 1): D' = D + ((num - D den) / (1 + den) + fac), the
+// reference's D' = (D + num) / (1 + den) + fac rearranged.  Formed as 1 + den in
+// FP32, the reference's denominator keeps only the leading bits of a small den
+// (den ~ 1e-3: about 14 of 24), and the density an agent drives its voxel towards
+// is about num / den, so that rounding would bias the voxel's value by up to
+// ~1e-4 relative every step in the same direction.  Here den keeps its full
+// precision and 1 + den only scales the (small) correction.
+__device__ __forceinline__ float fp32_update(float D, float num, float den, float fac)
+{
+	return D + (fmaf(-D, den, num) / (1.0f + den) + fac);
+}
+
 // compute_result (cell_solver.cpp:188-244) for agent i.  All loads of a batch of
 // substrates are issued before any store, so an agent's accesses overlap.
 //
 // The winner of a voxel writes its new density from the voxel's sums: for an
-// agent alone in its voxel these are its own terms (num, 1 + den, fac, with the
-// 1 added in T as the ballot does).  Internalized amounts: when no voxel holds two
+// agent alone in its voxel these are its own terms (num, den, fac; FP64 builds
+// add the 1 of the denominator in T as the ballot does, FP32 builds use
+// fp32_update).  Internalized amounts: when no voxel holds two
 // agents, the reference's fused update I += Vv (D - D'); otherwise every agent's
 // I -= Vv (num - D' den + fac) from the final density of its voxel
 // (cell_solver.cpp:229-243).  An agent alone in its voxel has just written that
@@ -477,7 +493,10 @@ __device__ __forceinline__ void agent_apply(const CellArgs& a, uint64_t i)
 		for (int q = 0; q < kSubBatch; q++)
 			if (s0 + q < S)
 			{
-				nx[q] = (dv[q] + n_[q]) / (alone ? d_[q] + T(1) : d_[q]) + f_[q];
+				if constexpr (sizeof(T) == 4)
+					nx[q] = fp32_update(dv[q], n_[q], d_[q], f_[q]);
+				else
+					nx[q] = (dv[q] + n_[q]) / (alone ? d_[q] + T(1) : d_[q]) + f_[q];
 				if constexpr (sizeof(T) == 4)
 				{
 					if (fused)

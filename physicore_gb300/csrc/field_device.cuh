@@ -126,7 +126,16 @@ __device__ __forceinline__ void bulk_row(T* field, const T* supply, const T* upt
 			U = uptake[s];
 			Tt = target[s];
 		}
-		row[k] = (row[k] + dt * Sr * Tt) / (T(1) + dt * (U + Sr));
+		// bulk_solver.cpp:12-49: D' = (D + dt S T) / (1 + dt (U + S)); FP32 as
+		// D + (dt S T - D dt (U + S)) / (1 + dt (U + S)), so that a small dt (U + S)
+		// keeps its precision (its sum with 1 only scales the correction)
+		if constexpr (sizeof(T) == 4)
+		{
+			const T a = dt * Sr * Tt, b = dt * (U + Sr);
+			row[k] = row[k] + fmaf(-row[k], b, a) / (T(1) + b);
+		}
+		else
+			row[k] = (row[k] + dt * Sr * Tt) / (T(1) + dt * (U + Sr));
 		s += s_step;
 		if (s >= S)
 			s -= S;
