@@ -253,6 +253,39 @@ class ClockSampler:
                 "samples": len(self.rows), "via": "nvml" if self.nvml is not None else "nvidia-smi"}
 
 
+def bind_near_gpu(device):
+    """Restricts this process to the CPUs that NVML reports as local to `device`
+    (pinned host buffers are then placed on the GPU's own host memory node);
+    returns the previous CPU set, or None when nothing was changed.  Reads the
+    GPU's topology only."""
+    try:
+        prev = os.sched_getaffinity(0)
+        L = ctypes.CDLL("libnvidia-ml.so.1")
+        if L.nvmlInit_v2() != 0:
+            return None
+        h = ctypes.c_void_p()
+        ok = False
+        try:
+            import torch
+            uuid = str(torch.cuda.get_device_properties(device).uuid)
+            ok = L.nvmlDeviceGetHandleByUUID(("GPU-" + uuid).encode(), ctypes.byref(h)) == 0
+        except Exception:
+            ok = False
+        if not ok:
+            return None
+        words = (ctypes.c_ulong * 16)()
+        if L.nvmlDeviceGetCpuAffinity(h, ctypes.c_uint(16), words) != 0:
+            return None
+        local = {64 * k + b for k in range(16) for b in range(64) if (words[k] >> b) & 1}
+        cpus = local & prev
+        if not cpus or cpus == prev:
+            return None
+        os.sched_setaffinity(0, cpus)
+        return prev
+    except Exception:
+        return None
+
+
 def build_problem(w):
     from physicore_gb300 import workloads as W
     return W.large(seed=w["seed"], n=w["n"], S=w["S"], agents=w["agents"], interior=w["interior"])
@@ -345,6 +378,7 @@ def run_gb300(args, w):
             torch.distributed.barrier()
 
     det = Details(args.detail_out if rank == 0 else None)
+    prev_cpus = bind_near_gpu(local)
     mass_on = args.mass_check == "on"
     p = build_problem(w)
     from physicore_gb300 import workloads as W
@@ -462,6 +496,7 @@ def run_gb300(args, w):
             torch.distributed.destroy_process_group()
         return
 
+    e2e["host_cpus"] = len(os.sched_getaffinity(0))
     head = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded PCG64)",
@@ -476,6 +511,8 @@ def run_gb300(args, w):
 
     # CPU baseline (the oracle on the machine's cores, a bounded sample) and the FP32
     # field's error against that FP64 run after the same solve calls
+    if prev_cpus:
+        os.sched_setaffinity(0, prev_cpus)
     if world == 1 and not args.no_cpu_baseline:
         threads = cpu_threads()
         v, done, secs, o, calls = time_reference(p, args.cpu_steps, 1, threads, budget_s=30.0)
