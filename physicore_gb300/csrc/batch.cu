@@ -1702,7 +1702,7 @@ int upload_recompute(pcg_batch* b)
 {
 	const size_t N = b->ctx.size();
 	for (size_t d = 0; d < N; d++)
-		b->h_recompute[d] = C(b, d)->recompute_cells ? 1 : 0;
+		b->h_recompute[d] = C(b, d)->recompute_cells || C(b, d)->ballot_kind != 2 ? 1 : 0;
 	static const int rebuild_kernels[4] = { K_CELLS_CLEAR, K_CELLS_LOCATE, K_CELLS_BALLOT, K_CELLS_REDUCE };
 	for (int k = 0; k < 4; k++)
 	{
@@ -2141,7 +2141,10 @@ int pcg_batch_solve_budgets(pcg_batch* b, uint64_t iterations, const uint64_t* b
 	{
 		Context* c = static_cast<Context*>(b->ctx[d]);
 		if (!budgets || budgets[d] > 0)
+		{
 			c->recompute_cells = false;
+			c->ballot_kind = 2; // the roles and lists are this batch's (rebuilt above if they were not)
+		}
 		if (b->h_doms[d].mc_tot)
 			c->mass_checked_steps += b->h_steps_left[d];
 	}

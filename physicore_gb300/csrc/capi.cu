@@ -239,24 +239,26 @@ void launch_begin(Context* c, int kid, double bytes, cudaEvent_t* ev)
 	}
 }
 
-void launch_end(Context* c, int kid, cudaEvent_t ev, double per_shared)
+void launch_end(Context* c, int kid, cudaEvent_t ev, double per_shared, double per_writer)
 {
 	if (!c->timing || !ev)
 		return;
 	cudaEvent_t stop = get_event(c);
 	cudaEventRecord(stop, c->stream);
-	c->pending.push_back({ kid, ev, stop, per_shared });
+	c->pending.push_back({ kid, ev, stop, per_shared, per_writer });
 }
 
-// In timing mode the cell step copies the number of agents in shared voxels to a
-// pinned word after every ballot; launches whose work is those agents add their
-// bytes per agent times that number once their events have completed.
+// In timing mode the cell step copies the number of agents in shared voxels and
+// of agents that write a voxel to pinned words after every ballot; launches whose
+// work is those agents add their bytes per agent times those numbers once their
+// events have completed.
 void collect_timings(Context* c)
 {
 	if (!c->pending.empty() && c->h_words)
 	{
 		cudaEventSynchronize(c->pending.back().b);
 		c->shared_agents = c->h_words[2];
+		c->writer_agents = c->h_words[3];
 	}
 	for (auto& p : c->pending)
 	{
@@ -264,7 +266,7 @@ void collect_timings(Context* c)
 		float ms = 0;
 		cudaEventElapsedTime(&ms, p.a, p.b);
 		c->stats[p.kid].total_ms += ms;
-		c->stats[p.kid].bytes += p.per_shared * c->shared_agents;
+		c->stats[p.kid].bytes += p.per_shared * c->shared_agents + p.per_writer * c->writer_agents;
 		c->event_pool.push_back(p.a);
 		c->event_pool.push_back(p.b);
 	}
@@ -701,7 +703,7 @@ int ensure_device_state(Context* c, bool defer_clear = false)
 	{
 		int rc = dalloc(c, c->err, sizeof(uint32_t) * 4);
 		if (!rc)
-			rc = dalloc(c, c->flags, sizeof(uint32_t) * 4);
+			rc = dalloc(c, c->flags, sizeof(uint32_t) * 8);
 		if (!rc)
 			rc = dalloc(c, c->tickets, sizeof(uint32_t) * 4);
 		if (rc)
@@ -711,7 +713,7 @@ int ensure_device_state(Context* c, bool defer_clear = false)
 	if (!c->words_cleared && !defer_clear)
 	{
 		PCG_CUDA_TRY(cudaMemsetAsync(c->err.ptr, 0, sizeof(uint32_t) * 4, c->stream));
-		PCG_CUDA_TRY(cudaMemsetAsync(c->flags.ptr, 0, sizeof(uint32_t) * 4, c->stream));
+		PCG_CUDA_TRY(cudaMemsetAsync(c->flags.ptr, 0, sizeof(uint32_t) * 8, c->stream));
 		c->words_cleared = true;
 	}
 	return PCG_OK;
@@ -825,11 +827,13 @@ static int alloc_agents(Context* c, uint64_t A)
 		return rc;
 	if ((rc = dalloc(c, c->a_rank, std::max<uint64_t>(A, 1) * sizeof(uint32_t))))
 		return rc;
+	if ((rc = dalloc(c, c->a_writers, std::max<uint64_t>(A, 1) * sizeof(uint32_t))))
+		return rc;
 	if ((rc = dalloc(c, c->a_sorted, std::max<uint64_t>(A, 1) * 2 * sizeof(uint32_t))))
 		return rc;
-	DeviceBuffer* rs[] = { &c->a_num, &c->a_den, &c->a_fac, &c->a_rnum, &c->a_rden, &c->a_rfac };
-	for (DeviceBuffer* b : rs)
-		if ((rc = dalloc(c, *b, std::max<uint64_t>(A * S, 1) * w)))
+	c->term_stride = term_stride(S, w);
+	for (DeviceBuffer* b : { &c->a_terms, &c->a_reduced })
+		if ((rc = dalloc(c, *b, std::max<uint64_t>(A * c->term_stride, 1) * w)))
 			return rc;
 	if ((rc = dalloc(c, c->owner, c->V * sizeof(uint32_t))))
 		return rc;
@@ -929,7 +933,7 @@ uint64_t estimate_device_bytes(const Context* c)
 	else if (c->bulk_mode == PCG_BULK_PER_VOXEL)
 		b += 3 * rows * pitch * w;
 	if (A)
-		b += A * (c->dims * 8 + 6 * S * 8 + 8 + 1 + 8 + 5 + 12 + 6 * S * w) + V * 8;
+		b += A * (c->dims * 8 + 6 * S * 8 + 8 + 1 + 8 + 5 + 16 + 2 * term_stride(S, w) * w) + V * 8;
 	return b;
 }
 
@@ -1014,10 +1018,11 @@ int pcg_destroy(pcg_context* c)
 								 &c->staging,	 &c->dir_offsets, &c->dir_values, &c->dir_conds, &c->face_values,
 								 &c->face_conds, &c->bulk[0],	&c->bulk[1],	&c->bulk[2],	 &c->a_pos,
 								 &c->a_sec,		 &c->a_sat,		&c->a_upt,		&c->a_net,		 &c->a_vol,
-								 &c->a_active,	 &c->a_internal, &c->a_frac,	&c->a_foff,		 &c->a_num,
-								 &c->a_den,		 &c->a_fac,		&c->a_rnum,		&c->a_rden,		 &c->a_rfac,
+								 &c->a_active,	 &c->a_internal, &c->a_frac,	&c->a_foff,		 &c->a_terms,
+								 &c->a_reduced,
 								 &c->owner,		 &c->counts,	&c->a_role,		&c->a_shared,	 &c->rb_staging[0],
-								 &c->rb_staging[1], &c->a_rank,	&c->a_sorted,	&c->xy_segs,	 &c->xy_done };
+								 &c->rb_staging[1], &c->a_rank,	&c->a_sorted,	&c->a_writers,	 &c->xy_segs,
+								 &c->xy_done };
 	for (auto* b : all)
 		pcg::dfree(*b);
 	pcg::dfree(c->slab); // after the pieces carved from it

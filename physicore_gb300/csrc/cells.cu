@@ -14,8 +14,8 @@
 //    cells_device.cuh: an FP32 estimate decides unless it lies within its error
 //    bound of a voxel boundary, where the FP64 division decides), so the
 //    agent->voxel maps and the per-voxel counts are bit-exact with the reference;
-//    lanes of one voxel count with one atomic (__match_any_sync), whose returned
-//    offset ranks the agents of the voxel.
+//    a run of lanes in one voxel counts with one atomic, whose returned offset
+//    ranks the agents of the voxel.
 //  * ballot: rank 0 wins the voxel (the reference's first compare-and-swap wins,
 //    cell_solver.cpp:79-101); the agents of shared voxels are grouped by voxel and
 //    each group is summed by a segmented warp reduction instead of every agent
@@ -23,7 +23,8 @@
 //    (cell_solver.cpp:102-127); the conflict flag stays on the device, so the step
 //    never waits on the host (the Thrust backend copies it back every step,
 //    thrust_solver/src/cell_solver.cpp:251-252).
-//  * apply/internalize read the flag on the device and take the reference's
+//  * apply (over the agents that write a voxel) and internalize (over the agents
+//    of shared voxels) read the flag on the device and take the reference's
 //    fused or two-pass branch.  A voxel's substrates are adjacent in the field, so
 //    each agent touches one 32-byte sector of densities (S <= 8, FP32).
 //  Batches keep the per-warp ballot with atomics (batch.cu).
@@ -42,7 +43,11 @@ __global__ void cells_place_kernel(CellArgs a)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	if (i == 0)
+	{
 		a.flags[0] = a.flags[1] = a.flags[2] = a.flags[3] = 0;
+		if (a.writers)
+			a.flags[4] = 0;
+	}
 	uint32_t v = kNoAgent;
 	if (i < a.A)
 	{
@@ -58,16 +63,18 @@ constexpr unsigned kClassifyBlock = 1024;
 // classify: roles from count and rank (cell_solver.cpp:102-127: every agent but
 // the winner of a shared voxel is a conflict); the agents of shared voxels listed
 // in agent order (flags[2]); each winner reserves its voxel's group of slots
-// (owner[v] = first slot, flags[3] counts slots) and clears its reduced row.  A
-// block scans both counts and reserves its ranges with one 64-bit atomic on the
-// adjacent, 8-byte aligned words flags[2..3] (list entries low, slots high;
-// neither total reaches 2^32, so no carry crosses): same-address atomics that
-// return a value serialise, so there is one per 1024 agents.
+// (owner[v] = first slot, flags[3] counts slots) and clears its reduced row; with
+// a writer list, the agents that write a voxel (alone or winner) listed in agent
+// order (flags[4]).  A block scans its counts and reserves its ranges with one
+// 64-bit atomic on the adjacent, 8-byte aligned words flags[2..3] (list entries
+// low, slots high; neither total reaches 2^32, so no carry crosses) and one on
+// flags[4]: same-address atomics that return a value serialise, so there is one
+// per 1024 agents and word.
 template <typename T>
 __global__ void __launch_bounds__(kClassifyBlock) cells_classify_kernel(CellArgs a)
 {
-	__shared__ uint32_t part[2][kClassifyBlock / 32];
-	__shared__ uint32_t base[2];
+	__shared__ uint32_t part[3][kClassifyBlock / 32];
+	__shared__ uint32_t base[3];
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 	uint32_t v = kNoAgent, cnt = 0;
@@ -77,108 +84,136 @@ __global__ void __launch_bounds__(kClassifyBlock) cells_classify_kernel(CellArgs
 		v = a.vox[i];
 		if (v != kNoAgent)
 		{
-			cnt = a.counts[v];
-			role = cnt == 1 ? kRoleAlone : (a.rank[i] == 0 ? kRoleWinner : kRoleLoser);
+			// an agent of rank > 0 shares its voxel: only rank 0 needs the count (a
+			// scattered read that the block's scans would wait for)
+			if (a.rank[i] == 0)
+			{
+				cnt = a.counts[v];
+				role = cnt == 1 ? kRoleAlone : kRoleWinner;
+			}
+			else
+				role = kRoleLoser;
 		}
 		a.role[i] = role;
 	}
 	if (__any_sync(0xffffffffu, role == kRoleLoser) && lane == 0)
 		atomicOr(a.flags, 1u);
-	const uint32_t sh = (role == kRoleWinner || role == kRoleLoser) ? 1u : 0u;
+	const bool sh = role == kRoleWinner || role == kRoleLoser;
+	const bool wr = a.writers && (role == kRoleAlone || role == kRoleWinner);
+	const uint32_t bsh = __ballot_sync(0xffffffffu, sh), bwr = __ballot_sync(0xffffffffu, wr);
+	const uint32_t below = (1u << lane) - 1u;
 	const uint32_t seg = role == kRoleWinner ? cnt : 0u;
-	uint32_t sh_inc = sh, seg_inc = seg;
+	uint32_t seg_inc = seg;
 	for (uint32_t o = 1; o < 32; o <<= 1)
 	{
-		const uint32_t t0 = __shfl_up_sync(0xffffffffu, sh_inc, o), t1 = __shfl_up_sync(0xffffffffu, seg_inc, o);
+		const uint32_t t = __shfl_up_sync(0xffffffffu, seg_inc, o);
 		if (lane >= o)
-			sh_inc += t0, seg_inc += t1;
+			seg_inc += t;
 	}
 	if (lane == 31)
-		part[0][warp] = sh_inc, part[1][warp] = seg_inc;
+		part[0][warp] = __popc(bsh), part[1][warp] = seg_inc, part[2][warp] = __popc(bwr);
 	__syncthreads();
 	if (warp == 0)
 	{
-		uint32_t p0 = lane < nw ? part[0][lane] : 0u, p1 = lane < nw ? part[1][lane] : 0u;
+		uint32_t p[3];
+#pragma unroll
+		for (int k = 0; k < 3; k++)
+			p[k] = lane < nw ? part[k][lane] : 0u;
 		for (uint32_t o = 1; o < 32; o <<= 1)
-		{
-			const uint32_t t0 = __shfl_up_sync(0xffffffffu, p0, o), t1 = __shfl_up_sync(0xffffffffu, p1, o);
-			if (lane >= o)
-				p0 += t0, p1 += t1;
-		}
+#pragma unroll
+			for (int k = 0; k < 3; k++)
+			{
+				const uint32_t t = __shfl_up_sync(0xffffffffu, p[k], o);
+				if (lane >= o)
+					p[k] += t;
+			}
 		if (lane == 31)
 		{
 			unsigned long long old = 0ull;
-			if (p0 | p1)
+			if (p[0] | p[1])
 				old = atomicAdd(reinterpret_cast<unsigned long long*>(a.flags + 2),
-								((unsigned long long)p1 << 32) | (unsigned long long)p0);
+								((unsigned long long)p[1] << 32) | (unsigned long long)p[0]);
 			base[0] = (uint32_t)old;
 			base[1] = (uint32_t)(old >> 32);
+			base[2] = p[2] ? atomicAdd(a.flags + 4, p[2]) : 0u;
 		}
-		uint32_t e0 = __shfl_up_sync(0xffffffffu, p0, 1), e1 = __shfl_up_sync(0xffffffffu, p1, 1);
-		if (lane == 0)
-			e0 = e1 = 0u;
-		if (lane < nw)
-			part[0][lane] = e0, part[1][lane] = e1;
+#pragma unroll
+		for (int k = 0; k < 3; k++)
+		{
+			const uint32_t e = __shfl_up_sync(0xffffffffu, p[k], 1);
+			if (lane < nw)
+				part[k][lane] = lane == 0 ? 0u : e;
+		}
 	}
 	__syncthreads();
 	if (sh)
-		a.shared[base[0] + part[0][warp] + sh_inc - 1] = (uint32_t)i;
+		a.shared[base[0] + part[0][warp] + __popc(bsh & below)] = (uint32_t)i;
+	if (wr)
+		a.writers[base[2] + part[2][warp] + __popc(bwr & below)] = (uint32_t)i;
 	if (role == kRoleWinner)
 	{
 		a.owner[v] = base[1] + part[1][warp] + seg_inc - seg;
-		T* rn = static_cast<T*>(a.rnum) + i * a.S;
-		T* rd = static_cast<T*>(a.rden) + i * a.S;
-		T* rf = static_cast<T*>(a.rfac) + i * a.S;
+		T* rn = static_cast<T*>(a.rnum) + i * a.ts;
+		T* rd = static_cast<T*>(a.rden) + i * a.ts;
+		T* rf = static_cast<T*>(a.rfac) + i * a.ts;
 		for (uint64_t s = 0; s < a.S; s++)
 			rn[s] = rd[s] = rf[s] = T(0);
 	}
 }
 
-// group: every agent of a shared voxel writes (its index, its voxel) into its
-// voxel's group, so the group sums read their keys in slot order.
+// group: every agent of a shared voxel (role from classify) writes (its index,
+// its voxel) into its voxel's group of slots.  One thread per agent: with many
+// agents per voxel nearly all of them write, and the loads of one agent (role,
+// voxel, rank, then its voxel's first slot) form a chain that only more threads in
+// flight hide.
 __global__ void cells_group_kernel(CellArgs a)
 {
-	const uint32_t count = __ldg(a.flags + a.list_word);
-	for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < count; j += (uint64_t)gridDim.x * blockDim.x)
-	{
-		const uint32_t i = __ldg(a.shared + j);
-		const uint32_t v = __ldg(a.vox + i);
-		a.sorted[__ldg(a.owner + v) + __ldg(a.rank + i)] = make_uint2(i, v);
-	}
+	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+	if (i >= a.A)
+		return;
+	const uint8_t role = a.role[i];
+	if (role != kRoleWinner && role != kRoleLoser)
+		return;
+	const uint32_t v = a.vox[i];
+	a.sorted[(uint64_t)__ldg(a.owner + v) + a.rank[i]] = make_uint2((uint32_t)i, v);
 }
 
 // group sum: a warp takes 32 consecutive slots and sums each voxel's terms with a
 // segmented scan (lanes of one voxel are consecutive); the last lane of each
 // voxel's run writes the winner's row: sum num, sum den (plus 1 in FP64 builds),
 // sum fac -- stored when the run is the voxel's whole group, else added with
-// atomics (the part holding the group's first slot adds the 1).
-template <typename T>
+// atomics (the part holding the group's first slot adds the 1).  SC is S when
+// the launch fixes it at compile time (1-8: the per-substrate guards fold away),
+// else 0.
+template <typename T, int SC>
 __global__ void cells_group_sum_kernel(CellArgs a)
 {
 	const uint32_t count = __ldg(a.flags + a.list_word);
 	const uint32_t lane = threadIdx.x & 31;
 	const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
 	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-	const uint32_t S = (uint32_t)a.S;
+	const uint32_t S = SC ? (uint32_t)SC : (uint32_t)a.S;
 	const bool vec = a.vec;
-	const T* num = static_cast<const T*>(a.num);
-	const T* den = static_cast<const T*>(a.den);
-	const T* fac = static_cast<const T*>(a.fac);
 	T* rnum = static_cast<T*>(a.rnum);
 	T* rden = static_cast<T*>(a.rden);
 	T* rfac = static_cast<T*>(a.rfac);
 	for (uint64_t j0 = gw * 32; j0 < count; j0 += nwarps * 32)
 	{
 		const uint64_t j = j0 + lane;
-		uint32_t i = 0, v = kNoAgent;
+		uint32_t v = kNoAgent;
+		const T *pn = nullptr, *pd = nullptr, *pf = nullptr;
 		if (j < count)
 		{
+			// the agent's three rows lie side by side in a context's term rows
 			const uint2 iv = __ldg(a.sorted + j);
-			i = iv.x;
 			v = iv.y;
+			pn = static_cast<const T*>(a.num) + (uint64_t)iv.x * a.ts;
+			pd = static_cast<const T*>(a.den) + (uint64_t)iv.x * a.ts;
+			pf = static_cast<const T*>(a.fac) + (uint64_t)iv.x * a.ts;
 		}
-		const uint32_t group = __match_any_sync(0xffffffffu, v);
-		const uint32_t first = __ffs(group) - 1, last = 31 - __clz(group);
+		uint32_t first, end;
+		key_run(v, first, end);
+		const uint32_t last = end - 1;
 		const bool writer = v != kNoAgent && lane == last;
 		uint32_t w = 0;
 		bool head = false, whole = false;
@@ -201,9 +236,9 @@ __global__ void cells_group_sum_kernel(CellArgs a)
 				n_[q] = d_[q] = f_[q] = T(0);
 			if (v != kNoAgent)
 			{
-				row_load(num + (uint64_t)i * S, s0, S, vec, n_);
-				row_load(den + (uint64_t)i * S, s0, S, vec, d_);
-				row_load(fac + (uint64_t)i * S, s0, S, vec, f_);
+				row_load(pn, s0, S, vec, n_);
+				row_load(pd, s0, S, vec, d_);
+				row_load(pf, s0, S, vec, f_);
 			}
 #pragma unroll
 			for (int k = 0; k < 5; k++)
@@ -227,7 +262,7 @@ __global__ void cells_group_sum_kernel(CellArgs a)
 #pragma unroll
 					for (int q = 0; q < kSubBatch; q++)
 						d_[q] += T(1);
-				const uint64_t r = (uint64_t)w * S;
+				const uint64_t r = (uint64_t)w * a.ts;
 				if (whole)
 				{
 					row_store(rnum + r, s0, S, vec, n_);
@@ -256,6 +291,21 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) cells_apply_kerne
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	if (i < a.A)
 		agent_apply<T>(a, i);
+}
+
+// Over the agents that write a voxel (alone or winner; flags[4] of them, listed
+// by classify) when they are fewer than half the agents, else over every agent
+// (agent_apply returns at once for the others): with many agents per voxel most
+// agents only lose their ballot, and a thread per agent would mostly wait on its
+// role byte.  Grid-stride, so the grid need not match the device-side count.
+template <typename T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) cells_apply_writers_kernel(CellArgs a)
+{
+	const uint32_t count = __ldg(a.flags + 4);
+	const bool list = 2ull * count < a.A;
+	const uint64_t n = list ? count : a.A;
+	for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x)
+		agent_apply<T>(a, list ? __ldg(a.writers + j) : j);
 }
 
 // Over the list of agents in shared voxels (empty when there was no conflict).
@@ -317,12 +367,15 @@ CellArgs make_cell_args(const Context* c)
 	a.internal = static_cast<double*>(c->a_internal.ptr);
 	a.vox = static_cast<uint32_t*>(c->a_vox.ptr);
 	a.foff = static_cast<uint32_t*>(c->a_foff.ptr);
-	a.num = c->a_num.ptr;
-	a.den = c->a_den.ptr;
-	a.fac = c->a_fac.ptr;
-	a.rnum = c->a_rnum.ptr;
-	a.rden = c->a_rden.ptr;
-	a.rfac = c->a_rfac.ptr;
+	// num, den and fac side by side in each agent's row
+	const size_t rb = c->S * c->wsize;
+	a.ts = c->term_stride;
+	a.num = c->a_terms.ptr;
+	a.den = static_cast<char*>(c->a_terms.ptr) + rb;
+	a.fac = static_cast<char*>(c->a_terms.ptr) + 2 * rb;
+	a.rnum = c->a_reduced.ptr;
+	a.rden = static_cast<char*>(c->a_reduced.ptr) + rb;
+	a.rfac = static_cast<char*>(c->a_reduced.ptr) + 2 * rb;
 	a.owner = static_cast<uint32_t*>(c->owner.ptr);
 	a.counts = static_cast<uint32_t*>(c->counts.ptr);
 	a.role = static_cast<uint8_t*>(c->a_role.ptr);
@@ -336,6 +389,7 @@ CellArgs make_cell_args(const Context* c)
 	a.pairs = c->wsize == 4 ? 1 : 0; // FP32 contexts store internalized amounts as float pairs
 	a.rank = static_cast<uint32_t*>(c->a_rank.ptr);
 	a.sorted = static_cast<uint2*>(c->a_sorted.ptr);
+	a.writers = static_cast<uint32_t*>(c->a_writers.ptr);
 	a.list_word = 2; // the grouped ballot (a batch sets 1 for its per-warp ballot)
 	set_fast_locate(a);
 	return a;
@@ -365,21 +419,46 @@ static int run_ballot(Context* c, const CellArgs& a, cudaStream_t stream, int sm
 	if (c)
 		launch_begin(c, K_CELLS_BALLOT, A * (4 + 4 + 4 + 1), &ev);
 	cells_classify_kernel<T><<<cgrid, kClassifyBlock, 0, stream>>>(a);
-	if (c && c->timing && c->h_words) // list length for the per-agent byte counts
+	if (c && c->timing && c->h_words) // list lengths for the per-agent byte counts
+	{
 		PCG_CUDA_TRY(
 			cudaMemcpyAsync(c->h_words + 2, a.flags + a.list_word, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+		PCG_CUDA_TRY(cudaMemcpyAsync(c->h_words + 3, a.flags + 4, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	}
+	// shared-voxel agents: list entry, winner's row cleared; writers: list entry
 	if (c)
-		launch_end(c, K_CELLS_BALLOT, ev, 4.0 + 3 * S * w);
+		launch_end(c, K_CELLS_BALLOT, ev, 4.0 + 3 * S * w, 4.0);
 	PCG_CUDA_TRY(cudaGetLastError());
+	// per agent its role; per shared-voxel agent its voxel, rank and voxel's first
+	// slot, and the pair written
 	if (c)
-		launch_begin(c, K_CELLS_GROUP, 0.0, &ev);
-	cells_group_kernel<<<lgrid, block, 0, stream>>>(a);
+		launch_begin(c, K_CELLS_GROUP, A, &ev);
+	cells_group_kernel<<<grid, block, 0, stream>>>(a);
 	if (c)
-		launch_end(c, K_CELLS_GROUP, ev, 24.0);
+		launch_end(c, K_CELLS_GROUP, ev, 20.0);
 	PCG_CUDA_TRY(cudaGetLastError());
+	// per slot: the pair and the agent's three rows (one gathered term row in a
+	// context)
 	if (c)
 		launch_begin(c, K_CELLS_REDUCE, 0.0, &ev);
-	cells_group_sum_kernel<T><<<lgrid, block, 0, stream>>>(a);
+	switch (a.S)
+	{
+#define PCG_GROUP_SUM(SV)                                                                                              \
+	case SV:                                                                                                           \
+		cells_group_sum_kernel<T, SV><<<lgrid, block, 0, stream>>>(a);                                                 \
+		break;
+		PCG_GROUP_SUM(1)
+		PCG_GROUP_SUM(2)
+		PCG_GROUP_SUM(3)
+		PCG_GROUP_SUM(4)
+		PCG_GROUP_SUM(5)
+		PCG_GROUP_SUM(6)
+		PCG_GROUP_SUM(7)
+		PCG_GROUP_SUM(8)
+#undef PCG_GROUP_SUM
+	default:
+		cells_group_sum_kernel<T, 0><<<lgrid, block, 0, stream>>>(a);
+	}
 	if (c)
 		launch_end(c, K_CELLS_REDUCE, ev, 8.0 + 3 * S * w);
 	PCG_CUDA_TRY(cudaGetLastError());
@@ -396,6 +475,10 @@ static int run_cells(Context* c, bool recompute)
 	const unsigned grid = (unsigned)((c->A + block - 1) / block);
 	const double S = (double)c->S, A = (double)c->A, w = (double)sizeof(T);
 	cudaEvent_t ev;
+	// the cached roles and lists must come from this kind of ballot (a batch keeps
+	// its own list and counts)
+	if (c->ballot_kind != 1)
+		recompute = true;
 	if (recompute)
 	{
 		PCG_CUDA_TRY(cudaMemsetAsync(c->counts.ptr, 0, c->V * sizeof(uint32_t), c->stream));
@@ -407,11 +490,14 @@ static int run_cells(Context* c, bool recompute)
 		if (rc)
 			return rc;
 		c->terms_dirty = false;
+		c->ballot_kind = 1;
 	}
-	// per agent: role, offset, summed (or own) terms, density read+write
-	launch_begin(c, K_CELLS_APPLY, A * (5 + 3 * S * w + 2 * S * w + (c->compute_internalized ? 16 * S : 0)), &ev);
-	cells_apply_kernel<T><<<grid, block, 0, c->stream>>>(a);
-	launch_end(c, K_CELLS_APPLY, ev);
+	// per writer: list entry, role, offset, summed (or own) terms, density read and
+	// write, internalized amounts read and written
+	launch_begin(c, K_CELLS_APPLY, 0.0, &ev);
+	cells_apply_writers_kernel<T>
+		<<<std::min<unsigned>(grid, 12 * std::max(c->sm_count, 1)), block, 0, c->stream>>>(a);
+	launch_end(c, K_CELLS_APPLY, ev, 0.0, 9 + 3 * S * w + 2 * S * w + (c->compute_internalized ? 16 * S : 0));
 	PCG_CUDA_TRY(cudaGetLastError());
 	if (c->compute_internalized)
 	{
@@ -466,6 +552,7 @@ int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream)
 	a.rnum = b.rnum;
 	a.rden = b.rden;
 	a.rfac = b.rfac;
+	a.ts = b.S; // separate arrays
 	a.owner = b.owner;
 	a.counts = b.counts;
 	a.role = b.role;

@@ -41,13 +41,18 @@ struct CellArgs
 	double* internal;
 	uint32_t* vox;
 	uint32_t* foff;
+	// cell terms of agent i at num/den/fac + i * ts (S values each), the winner's
+	// sums at rnum/rden/rfac + i * ts: a context keeps the three side by side in
+	// one row (ts = term_stride(S)), caller-owned buffers as separate arrays (ts = S)
 	void *num, *den, *fac, *rnum, *rden, *rfac;
+	uint64_t ts;
 	uint32_t* owner;
 	uint32_t* counts;
 	uint8_t* role;    // [A] ballot role
 	uint32_t* shared; // [A] agents of voxels that hold several, flags[list_word] of them
-	uint32_t* flags;  // [0] conflict; entries of `shared` in word list_word; grouped ballot: [2..3]
-	uint32_t list_word; // 1 (batches: per-warp ballot) or 2 (grouped ballot: words 2, 3 = list, slots)
+	uint32_t* flags;  // [0] conflict; entries of `shared` in word list_word; grouped ballot: [2..4]
+	uint32_t list_word; // 1 (batches: per-warp ballot) or 2 (grouped ballot: words 2, 3 = list, slots;
+	                    // 4 = writers)
 	uint32_t* err;
 	void* field;
 	int internalized;
@@ -62,6 +67,10 @@ struct CellArgs
 	// agents of shared voxels grouped by voxel (slot order)
 	uint32_t* rank;   // [A]
 	uint2* sorted;    // [A] (agent, voxel) pairs
+	// a context's grouped ballot (null for caller-owned buffers): the agents that
+	// write a voxel, flags[4] of them, in agent order (apply walks them instead of
+	// every agent)
+	uint32_t* writers;
 };
 
 // The fast-location constants of a mesh: float bounds and reciprocal voxel edges,
@@ -88,7 +97,8 @@ CellArgs make_cell_args(const Context* c);
 inline int rows_vectorizable(const CellArgs& a, size_t wsize)
 {
 	auto al = [](const void* p) { return p == nullptr || reinterpret_cast<uintptr_t>(p) % 16 == 0; };
-	return a.S % (16 / wsize) == 0 && (a.pitch * wsize) % 16 == 0 && al(a.field) && al(a.internal) && al(a.num) &&
+	return a.S % (16 / wsize) == 0 && (a.pitch * wsize) % 16 == 0 && (a.ts * wsize) % 16 == 0 && al(a.field) &&
+		   al(a.internal) && al(a.num) &&
 		   al(a.den) && al(a.fac) && al(a.rnum) && al(a.rden) && al(a.rfac);
 }
 
@@ -159,18 +169,18 @@ __device__ __forceinline__ void agent_terms(const CellArgs& a, uint64_t i)
 		const double fv = a.dt * vol / a.Vv, ft = a.dt / a.Vv;
 		for (uint64_t s = 0; s < a.S; s++)
 		{
-			const uint64_t k = i * a.S + s;
+			const uint64_t k = i * a.S + s, t = i * a.ts + s;
 			if constexpr (sizeof(T) == 4)
 			{
-				num[k] = (T)(a.sec[k] * a.sat[k] * fv);
-				den[k] = (T)((a.upt[k] + a.sec[k]) * fv);
-				fac[k] = (T)(a.net[k] * ft);
+				num[t] = (T)(a.sec[k] * a.sat[k] * fv);
+				den[t] = (T)((a.upt[k] + a.sec[k]) * fv);
+				fac[t] = (T)(a.net[k] * ft);
 			}
 			else
 			{
-				num[k] = (T)(a.sec[k] * a.sat[k] * a.dt * vol / a.Vv);
-				den[k] = (T)((a.upt[k] + a.sec[k]) * a.dt * vol / a.Vv);
-				fac[k] = (T)(a.net[k] * a.dt / a.Vv);
+				num[t] = (T)(a.sec[k] * a.sat[k] * a.dt * vol / a.Vv);
+				den[t] = (T)((a.upt[k] + a.sec[k]) * a.dt * vol / a.Vv);
+				fac[t] = (T)(a.net[k] * a.dt / a.Vv);
 			}
 		}
 	}
@@ -212,7 +222,7 @@ __device__ __forceinline__ void agent_locate(const CellArgs& a, uint64_t i)
 	T* rfac = static_cast<T*>(a.rfac);
 	for (uint64_t s = 0; s < a.S; s++)
 	{
-		const uint64_t k = i * a.S + s;
+		const uint64_t k = i * a.ts + s;
 		rnum[k] = T(0);
 		rden[k] = T(0);
 		rfac[k] = T(0);
@@ -264,8 +274,8 @@ __device__ __forceinline__ uint8_t agent_reduce(const CellArgs& a, uint64_t i)
 	T* rfac = static_cast<T*>(a.rfac);
 	for (uint64_t s = 0; s < a.S; s++)
 	{
-		const uint64_t k = i * a.S + s;
-		const uint64_t kw = (uint64_t)w * a.S + s;
+		const uint64_t k = i * a.ts + s;
+		const uint64_t kw = (uint64_t)w * a.ts + s;
 		atomicAdd(rnum + kw, num[k]);
 		// the winner adds the 1 of the denominator (FP64 builds; FP32 rows hold the
 		// bare sum of den, see fp32_update)
@@ -296,31 +306,47 @@ __device__ __forceinline__ void list_shared(const CellArgs& a, uint64_t i, bool 
 // (cell_solver.cpp:79-129).  When tens of agents share a voxel those atomics
 // serialise on the winner's row, so here the ballot groups the agents of shared
 // voxels by voxel instead and sums each group with a segmented warp reduction:
-//   place:     voxel of each agent; a warp-aggregated count per voxel whose
-//              returned offset gives the agent's rank in its voxel (rank 0, the
-//              agent whose atomic landed first, is the winner, as the first
-//              compare-and-swap wins in the reference)
+//   place:     voxel of each agent; a count per voxel (one atomic per run of
+//              lanes in the voxel) whose returned offset gives the agent's rank
+//              in its voxel (rank 0, the agent whose atomic landed first, is the
+//              winner, as the first compare-and-swap wins in the reference)
 //   classify:  roles from count and rank; the agents of shared voxels are listed
-//              in agent order (for the internalized pass) and each winner
-//              reserves its voxel's group of slots
-//   group:     every listed agent writes (index, voxel) into its voxel's group
+//              in agent order (for the internalized pass), so are the agents that
+//              write a voxel (for apply), and each winner reserves its voxel's
+//              group of slots
+//   group:     every agent of a shared voxel writes (index, voxel) into its
+//              voxel's group
 //   group sum: warps reduce consecutive slots by voxel; a group that lies within
 //              one warp is stored once, a group split across warps adds its parts
 //              to the winner's row (cleared by classify) with atomics
 
-// Counts agent i into voxel v (one atomic per voxel and warp) and records its rank
-// in the voxel.  All lanes of the warp call it (v = kNoAgent for none).
+// Runs of equal keys among the lanes of a warp: the first lane of the caller's run
+// and the first lane after it (32 at the end of the warp).  All lanes call it.
+__device__ __forceinline__ void key_run(uint32_t key, uint32_t& first, uint32_t& end)
+{
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+	const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0 || prev != key);
+	first = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+	const uint32_t later = heads & (0xfffffffeu << lane);
+	end = later ? __ffs(later) - 1 : 32;
+}
+
+// Counts agent i into voxel v and records its rank in the voxel: one atomic per run
+// of lanes with the same voxel (agents given in voxel order share one; in random
+// order each lane has its own, which costs less than grouping the lanes by voxel).
+// All lanes of the warp call it (v = kNoAgent for none).
 __device__ __forceinline__ void count_rank(const CellArgs& a, uint64_t i, uint32_t v)
 {
-	const uint32_t group = __match_any_sync(0xffffffffu, v);
-	if (v == kNoAgent)
-		return;
-	const uint32_t lane = threadIdx.x & 31, leader = __ffs(group) - 1;
+	const uint32_t lane = threadIdx.x & 31;
+	uint32_t first, end;
+	key_run(v, first, end);
 	uint32_t base = 0;
-	if (lane == leader)
-		base = atomicAdd(a.counts + v, (uint32_t)__popc(group));
-	base = __shfl_sync(group, base, leader);
-	a.rank[i] = base + __popc(group & ((1u << lane) - 1));
+	if (v != kNoAgent && lane == first)
+		base = atomicAdd(a.counts + v, end - first);
+	base = __shfl_sync(0xffffffffu, base, first);
+	if (v != kNoAgent)
+		a.rank[i] = base + (lane - first);
 }
 
 // Change of an internalized amount.  The FP64 build evaluates the reference's
@@ -475,9 +501,9 @@ __device__ __forceinline__ void agent_apply(const CellArgs& a, uint64_t i)
 	const bool vec = a.vec;
 	const uint32_t S = (uint32_t)a.S;
 	T* __restrict__ D = static_cast<T*>(a.field) + off;
-	const T* __restrict__ rn = static_cast<const T*>(alone ? a.num : a.rnum) + i * S;
-	const T* __restrict__ rd = static_cast<const T*>(alone ? a.den : a.rden) + i * S;
-	const T* __restrict__ rf = static_cast<const T*>(alone ? a.fac : a.rfac) + i * S;
+	const T* __restrict__ rn = static_cast<const T*>(alone ? a.num : a.rnum) + i * a.ts;
+	const T* __restrict__ rd = static_cast<const T*>(alone ? a.den : a.rden) + i * a.ts;
+	const T* __restrict__ rf = static_cast<const T*>(alone ? a.fac : a.rfac) + i * a.ts;
 	double* __restrict__ I = a.internal + i * S;
 	for (uint32_t s0 = 0; s0 < S; s0 += kSubBatch)
 	{
@@ -526,9 +552,9 @@ __device__ __forceinline__ void agent_internalize(const CellArgs& a, uint64_t i)
 	const bool vec = a.vec;
 	const uint32_t S = (uint32_t)a.S;
 	const T* __restrict__ D = static_cast<const T*>(a.field) + a.foff[i];
-	const T* __restrict__ nu = static_cast<const T*>(a.num) + i * S;
-	const T* __restrict__ de = static_cast<const T*>(a.den) + i * S;
-	const T* __restrict__ fa = static_cast<const T*>(a.fac) + i * S;
+	const T* __restrict__ nu = static_cast<const T*>(a.num) + i * a.ts;
+	const T* __restrict__ de = static_cast<const T*>(a.den) + i * a.ts;
+	const T* __restrict__ fa = static_cast<const T*>(a.fac) + i * a.ts;
 	double* __restrict__ I = a.internal + i * S;
 	for (uint32_t s0 = 0; s0 < S; s0 += kSubBatch)
 	{

@@ -80,6 +80,11 @@ constexpr uint64_t kBlockPoints = 8;           // line points per pipelined solv
 constexpr uint64_t kXTileBytes = 32 * 1024;    // shared memory of a substrate-mapped x tile
 
 __host__ __device__ constexpr uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
+
+// Values per agent row of the cell terms (num, den and fac of S substrates side by
+// side, cells_device.cuh): 3 S values of w bytes in whole 16-byte units, so that a
+// gather of one agent's terms touches one short run of memory, not three rows.
+__host__ __device__ constexpr uint64_t term_stride(uint64_t S, uint64_t w) { return round_up(3 * S * w, 16) / w; }
 __host__ __device__ constexpr int gcd_i(int a, int b) { return b == 0 ? a : gcd_i(b, a % b); }
 // Elements per x-sweep vector group: the smallest multiple of both S and a 16-byte chunk.
 __host__ __device__ constexpr int group_elems(int S, int vn) { return S <= 8 ? S / gcd_i(S, vn) * vn : vn; }
@@ -233,7 +238,8 @@ struct Context
 	uint64_t xy_key = 0;
 	uint32_t xy_nseg = 0, xy_total = 0, xy_nslab = 0;
 	DeviceBuffer xy_segs, xy_done;
-	DeviceBuffer flags;    // uint32 [4]: [0] ballot conflict, [1] agents in shared voxels
+	DeviceBuffer flags;    // uint32 [8]: [0] ballot conflict, [1] agents in shared voxels (batches),
+	                       // [2..3] and [4] the grouped ballot's counts (cells_device.cuh)
 	DeviceBuffer mass;     // double [S]
 	// per-step mass check (pcg_set_mass_check): FP64 totals [2 * S] before the
 	// first sweep and after the last one, added by the sweeps themselves, and
@@ -291,8 +297,14 @@ struct Context
 	DeviceBuffer a_shared;                // uint32 [A]: agents of voxels that hold several
 	DeviceBuffer a_rank;                  // uint32 [A]: rank of the agent in its voxel
 	DeviceBuffer a_sorted;                // uint2 [A]: (agent, voxel) of shared voxels grouped by voxel
-	DeviceBuffer a_num, a_den, a_fac;     // real [A*S]
-	DeviceBuffer a_rnum, a_rden, a_rfac;  // real [A*S]
+	DeviceBuffer a_writers;               // uint32 [A]: agents that write a voxel (alone or winner)
+	// the ballot behind the cached roles, lists and reduced rows: 0 none, 1 the
+	// grouped ballot of a single-domain step, 2 a batch's per-warp ballot (their
+	// lists and counts differ, so a step of the other kind rebuilds)
+	uint8_t ballot_kind = 0;
+	uint64_t term_stride = 0;             // values per agent row of a_terms and a_reduced
+	DeviceBuffer a_terms;                 // real [A][term_stride]: num, den, fac of the agent (S each)
+	DeviceBuffer a_reduced;               // real [A][term_stride]: a winner's sums over its voxel
 	DeviceBuffer owner;                   // uint32 [V]: winning agent per voxel (batches), or the first
 										  // slot of the voxel's group in a_sorted (single domain)
 	DeviceBuffer counts;                  // uint32 [V]: active agents per voxel
@@ -307,15 +319,17 @@ struct Context
 		int kid;
 		cudaEvent_t a, b;
 		double per_shared; // algorithmic bytes per agent in a shared voxel (a count known on the device)
+		double per_writer; // and per agent that writes a voxel (alone or winner)
 	};
 	uint32_t shared_agents = 0; // agents in shared voxels after the last timed ballot (timing mode)
+	uint32_t writer_agents = 0; // agents that write a voxel after it
 	std::vector<PendingTiming> pending;
 };
 
 // Launch bookkeeping: every kernel launch goes through begin/end so that the
 // context can count launches and (optionally) time them with CUDA events.
 void launch_begin(Context* c, int kid, double bytes, cudaEvent_t* ev);
-void launch_end(Context* c, int kid, cudaEvent_t ev, double per_shared = 0.0);
+void launch_end(Context* c, int kid, cudaEvent_t ev, double per_shared = 0.0, double per_writer = 0.0);
 void collect_timings(Context* c);
 
 // ------------------------------------------------------------------ kernel launchers (defined in .cu files)

@@ -128,6 +128,36 @@ def test_batch_step_budgets(pcg, oracle_mod, graph):
             assert np.array_equal(g.get_counts(), o.get_counts()), p["name"]
 
 
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp32", "fp64"])
+def test_batch_and_single_steps_interleave(pcg, oracle_mod, precision):
+    """The same contexts stepped in a batch, then alone, then in the batch again,
+    without a recompute request in between: the two kinds of step keep different
+    ballot lists, so each rebuilds the ballot left by the other, and every stage
+    matches the oracle, internalized amounts included."""
+    problems = [p for p in _problems(range(40)) if p["agents"] is not None and p["compute_internalized"]
+                and len(p["agents"]["volumes"]) > 4][:6]
+    assert len(problems) >= 4
+    ctx = [W.apply(pcg.Solver(precision), p) for p in problems]
+    oracle = [W.apply(oracle_mod.OracleSolver(threads=2), p) for p in problems]
+    rtol = FP64_RTOL if precision == 1 else FP32_RTOL
+    b = pcg.Batch(ctx)
+    for stage, alone in (("batch", False), ("single", True), ("batch again", False), ("single again", True)):
+        if alone:
+            for s in ctx:
+                s.solve(2)
+        else:
+            b.solve(2)
+            b.synchronize()
+        for o in oracle:
+            o.solve(2)
+        for p, g, o in zip(problems, ctx, oracle):
+            gs, os_ = _snap(g), _snap(o)
+            vv = None if precision == 1 else float(np.prod(p["voxel"]))
+            check([{key: (gs[key], os_[key]) for key in gs}], rtol, f"{p['name']} after {stage}", voxel_volume=vv,
+                  den_max=max_denominator(p))
+    b.close()
+
+
 def test_batch_direct_launches(pcg, oracle_mod):
     problems = _problems(range(16, 24))
     _verify(problems, _run(pcg, oracle_mod, problems, 0, graph=False), 0)
