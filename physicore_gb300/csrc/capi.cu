@@ -1706,6 +1706,22 @@ int pcg_set_kernel_timing(pcg_context* c, int enable)
 {
 	CTX_CHECK(c);
 	c->timing = enable != 0;
+	// The cell kernels' bytes scale with device-side counts (agents of shared
+	// voxels, agents that write a voxel), copied to pinned words after every timed
+	// ballot.  A ballot built before timing was enabled leaves them here.
+	if (c->timing && c->initialized && c->A && c->ballot_kind == 1 && c->flags.ptr)
+	{
+		pcg::DeviceGuard g(c->device);
+		if (!c->h_words && !(c->h_words = pcg::pinned_words_get()))
+			return fail(PCG_ERR_NOMEM, "pinned host memory for the device words");
+		PCG_CUDA_TRY(stream_wait(c));
+		PCG_CUDA_TRY(cudaMemcpy(c->h_words + 2, static_cast<uint32_t*>(c->flags.ptr) + 2, sizeof(uint32_t),
+								cudaMemcpyDeviceToHost));
+		PCG_CUDA_TRY(cudaMemcpy(c->h_words + 3, static_cast<uint32_t*>(c->flags.ptr) + 4, sizeof(uint32_t),
+								cudaMemcpyDeviceToHost));
+		c->shared_agents = c->h_words[2];
+		c->writer_agents = c->h_words[3];
+	}
 	return PCG_OK;
 }
 

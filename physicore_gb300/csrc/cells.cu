@@ -37,7 +37,9 @@ namespace {
 using namespace cellsdev;
 
 // place: terms (after new agent data), voxel, count and rank; the step's words
-// (conflict flag, list length, reserved group slots) start at zero.
+// (conflict flag, list length, reserved group slots) start at zero.  One agent
+// per thread: two per thread (both chunks' loads and atomics in flight together)
+// measured slower on the dense workload, 78 -> 107 us.
 template <typename T>
 __global__ void cells_place_kernel(CellArgs a)
 {
@@ -48,84 +50,101 @@ __global__ void cells_place_kernel(CellArgs a)
 		if (a.writers)
 			a.flags[4] = 0;
 	}
-	uint32_t v = kNoAgent;
+	uint32_t v[1] = { kNoAgent };
 	if (i < a.A)
 	{
 		if (a.terms)
 			agent_terms<T>(a, i);
-		v = agent_place(a, i);
+		v[0] = agent_place(a, i);
 	}
-	count_rank(a, i, v);
+	count_rank<1>(a, i, v);
 }
 
 constexpr unsigned kClassifyBlock = 1024;
+constexpr unsigned kClassifyChunks = 4; // 32-agent chunks per warp
 
 // classify: roles from count and rank (cell_solver.cpp:102-127: every agent but
 // the winner of a shared voxel is a conflict); the agents of shared voxels listed
 // in agent order (flags[2]); each winner reserves its voxel's group of slots
 // (owner[v] = first slot, flags[3] counts slots) and clears its reduced row; with
 // a writer list, the agents that write a voxel (alone or winner) listed in agent
-// order (flags[4]).  A block scans its counts and reserves its ranges with one
-// 64-bit atomic on the adjacent, 8-byte aligned words flags[2..3] (list entries
-// low, slots high; neither total reaches 2^32, so no carry crosses) and one on
-// flags[4]: same-address atomics that return a value serialise, so there is one
-// per 1024 agents and word.
+// order (flags[4]).  A warp takes kClassifyChunks consecutive chunks of 32 agents
+// (their loads in flight together).  A block scans its counts and reserves its
+// ranges with one 64-bit atomic on the adjacent, 8-byte aligned words flags[2..3]
+// (list entries low, slots high; neither total reaches 2^32, so no carry crosses)
+// and one on flags[4]: same-address atomics that return a value serialise, so
+// there is one per 4096 agents and word.
 template <typename T>
-__global__ void __launch_bounds__(kClassifyBlock) cells_classify_kernel(CellArgs a)
+__global__ void __launch_bounds__(kClassifyBlock, 2) cells_classify_kernel(CellArgs a)
 {
+	constexpr int K = kClassifyChunks;
 	__shared__ uint32_t part[3][kClassifyBlock / 32];
 	__shared__ uint32_t base[3];
-	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-	uint32_t v = kNoAgent, cnt = 0;
-	uint8_t role = kRoleNone;
-	if (i < a.A)
+	const uint64_t i0 = ((uint64_t)blockIdx.x * nw + warp) * (K * 32) + lane;
+	uint32_t v[K], cnt[K];
+	uint8_t role[K];
+#pragma unroll
+	for (int k = 0; k < K; k++)
 	{
-		v = a.vox[i];
-		if (v != kNoAgent)
-		{
-			// an agent of rank > 0 shares its voxel: only rank 0 needs the count (a
-			// scattered read that the block's scans would wait for)
-			if (a.rank[i] == 0)
-			{
-				cnt = a.counts[v];
-				role = cnt == 1 ? kRoleAlone : kRoleWinner;
-			}
-			else
-				role = kRoleLoser;
-		}
-		a.role[i] = role;
+		const uint64_t i = i0 + k * 32;
+		v[k] = i < a.A ? a.vox[i] : kNoAgent;
+		cnt[k] = v[k] != kNoAgent ? a.rank[i] : 0u; // the rank, for now
 	}
-	if (__any_sync(0xffffffffu, role == kRoleLoser) && lane == 0)
-		atomicOr(a.flags, 1u);
-	const bool sh = role == kRoleWinner || role == kRoleLoser;
-	const bool wr = a.writers && (role == kRoleAlone || role == kRoleWinner);
-	const uint32_t bsh = __ballot_sync(0xffffffffu, sh), bwr = __ballot_sync(0xffffffffu, wr);
+	// an agent of rank > 0 shares its voxel: only rank 0 needs the count (a
+	// scattered read that the block's scans would wait for)
+#pragma unroll
+	for (int k = 0; k < K; k++)
+	{
+		const bool first = v[k] != kNoAgent && cnt[k] == 0;
+		role[k] = v[k] == kNoAgent ? kRoleNone : (first ? kRoleWinner : kRoleLoser);
+		cnt[k] = first ? a.counts[v[k]] : 0u;
+	}
+	bool loser = false;
+	uint32_t bsh[K], bwr[K], seg_inc[K], tsh = 0, twr = 0, tseg = 0;
 	const uint32_t below = (1u << lane) - 1u;
-	const uint32_t seg = role == kRoleWinner ? cnt : 0u;
-	uint32_t seg_inc = seg;
-	for (uint32_t o = 1; o < 32; o <<= 1)
+#pragma unroll
+	for (int k = 0; k < K; k++)
 	{
-		const uint32_t t = __shfl_up_sync(0xffffffffu, seg_inc, o);
-		if (lane >= o)
-			seg_inc += t;
+		const uint64_t i = i0 + k * 32;
+		if (role[k] == kRoleWinner && cnt[k] == 1)
+			role[k] = kRoleAlone;
+		if (i < a.A)
+			a.role[i] = role[k];
+		loser |= role[k] == kRoleLoser;
+		bsh[k] = __ballot_sync(0xffffffffu, role[k] == kRoleWinner || role[k] == kRoleLoser);
+		bwr[k] = __ballot_sync(0xffffffffu, a.writers && (role[k] == kRoleAlone || role[k] == kRoleWinner));
+		// slots before this lane's in the warp's agent order (chunk-major)
+		uint32_t x = role[k] == kRoleWinner ? cnt[k] : 0u;
+		for (uint32_t o = 1; o < 32; o <<= 1)
+		{
+			const uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+			if (lane >= o)
+				x += t;
+		}
+		seg_inc[k] = tseg + x;
+		tseg += __shfl_sync(0xffffffffu, x, 31);
+		tsh += __popc(bsh[k]);
+		twr += __popc(bwr[k]);
 	}
-	if (lane == 31)
-		part[0][warp] = __popc(bsh), part[1][warp] = seg_inc, part[2][warp] = __popc(bwr);
+	if (__any_sync(0xffffffffu, loser) && lane == 0)
+		atomicOr(a.flags, 1u);
+	if (lane == 0)
+		part[0][warp] = tsh, part[1][warp] = tseg, part[2][warp] = twr;
 	__syncthreads();
 	if (warp == 0)
 	{
 		uint32_t p[3];
 #pragma unroll
-		for (int k = 0; k < 3; k++)
-			p[k] = lane < nw ? part[k][lane] : 0u;
+		for (int q = 0; q < 3; q++)
+			p[q] = lane < nw ? part[q][lane] : 0u;
 		for (uint32_t o = 1; o < 32; o <<= 1)
 #pragma unroll
-			for (int k = 0; k < 3; k++)
+			for (int q = 0; q < 3; q++)
 			{
-				const uint32_t t = __shfl_up_sync(0xffffffffu, p[k], o);
+				const uint32_t t = __shfl_up_sync(0xffffffffu, p[q], o);
 				if (lane >= o)
-					p[k] += t;
+					p[q] += t;
 			}
 		if (lane == 31)
 		{
@@ -138,26 +157,35 @@ __global__ void __launch_bounds__(kClassifyBlock) cells_classify_kernel(CellArgs
 			base[2] = p[2] ? atomicAdd(a.flags + 4, p[2]) : 0u;
 		}
 #pragma unroll
-		for (int k = 0; k < 3; k++)
+		for (int q = 0; q < 3; q++)
 		{
-			const uint32_t e = __shfl_up_sync(0xffffffffu, p[k], 1);
+			const uint32_t e = __shfl_up_sync(0xffffffffu, p[q], 1);
 			if (lane < nw)
-				part[k][lane] = lane == 0 ? 0u : e;
+				part[q][lane] = lane == 0 ? 0u : e;
 		}
 	}
 	__syncthreads();
-	if (sh)
-		a.shared[base[0] + part[0][warp] + __popc(bsh & below)] = (uint32_t)i;
-	if (wr)
-		a.writers[base[2] + part[2][warp] + __popc(bwr & below)] = (uint32_t)i;
-	if (role == kRoleWinner)
+	uint32_t osh = base[0] + part[0][warp], owr = base[2] + part[2][warp];
+	const uint32_t oseg = base[1] + part[1][warp];
+#pragma unroll
+	for (int k = 0; k < K; k++)
 	{
-		a.owner[v] = base[1] + part[1][warp] + seg_inc - seg;
-		T* rn = static_cast<T*>(a.rnum) + i * a.ts;
-		T* rd = static_cast<T*>(a.rden) + i * a.ts;
-		T* rf = static_cast<T*>(a.rfac) + i * a.ts;
-		for (uint64_t s = 0; s < a.S; s++)
-			rn[s] = rd[s] = rf[s] = T(0);
+		const uint64_t i = i0 + k * 32;
+		if ((bsh[k] >> lane) & 1u)
+			a.shared[osh + __popc(bsh[k] & below)] = (uint32_t)i;
+		if ((bwr[k] >> lane) & 1u)
+			a.writers[owr + __popc(bwr[k] & below)] = (uint32_t)i;
+		osh += __popc(bsh[k]);
+		owr += __popc(bwr[k]);
+		if (role[k] == kRoleWinner)
+		{
+			a.owner[v[k]] = oseg + seg_inc[k] - cnt[k];
+			T* rn = static_cast<T*>(a.rnum) + i * a.ts;
+			T* rd = static_cast<T*>(a.rden) + i * a.ts;
+			T* rf = static_cast<T*>(a.rfac) + i * a.ts;
+			for (uint64_t s = 0; s < a.S; s++)
+				rn[s] = rd[s] = rf[s] = T(0);
+		}
 	}
 }
 
@@ -404,7 +432,8 @@ static int run_ballot(Context* c, const CellArgs& a, cudaStream_t stream, int sm
 {
 	const unsigned block = 256;
 	const unsigned grid = (unsigned)((a.A + block - 1) / block);
-	const unsigned cgrid = (unsigned)((a.A + kClassifyBlock - 1) / kClassifyBlock);
+	const uint64_t per_block = (uint64_t)kClassifyBlock * kClassifyChunks;
+	const unsigned cgrid = (unsigned)((a.A + per_block - 1) / per_block);
 	// the list of shared-voxel agents is only known on the device: grid-stride
 	const unsigned lgrid = std::min<unsigned>(grid, 16 * std::max(sm_count, 1));
 	const double S = (double)a.S, A = (double)a.A, w = (double)sizeof(T);

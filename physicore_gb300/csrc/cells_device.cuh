@@ -332,21 +332,29 @@ __device__ __forceinline__ void key_run(uint32_t key, uint32_t& first, uint32_t&
 	end = later ? __ffs(later) - 1 : 32;
 }
 
-// Counts agent i into voxel v and records its rank in the voxel: one atomic per run
-// of lanes with the same voxel (agents given in voxel order share one; in random
-// order each lane has its own, which costs less than grouping the lanes by voxel).
-// All lanes of the warp call it (v = kNoAgent for none).
-__device__ __forceinline__ void count_rank(const CellArgs& a, uint64_t i, uint32_t v)
+// Counts agents i0 + 32 k into voxels v[k] (k < K) and records their ranks in
+// their voxels: one atomic per run of lanes with the same voxel (agents given in
+// voxel order share one; in random order each lane has its own, which costs less
+// than grouping the lanes by voxel); the K chunks' atomics are in flight together.
+// All lanes of the warp call it (v[k] = kNoAgent for none).
+template <int K>
+__device__ __forceinline__ void count_rank(const CellArgs& a, uint64_t i0, const uint32_t (&v)[K])
 {
 	const uint32_t lane = threadIdx.x & 31;
-	uint32_t first, end;
-	key_run(v, first, end);
-	uint32_t base = 0;
-	if (v != kNoAgent && lane == first)
-		base = atomicAdd(a.counts + v, end - first);
-	base = __shfl_sync(0xffffffffu, base, first);
-	if (v != kNoAgent)
-		a.rank[i] = base + (lane - first);
+	uint32_t first[K], end[K], base[K];
+#pragma unroll
+	for (int k = 0; k < K; k++)
+		key_run(v[k], first[k], end[k]);
+#pragma unroll
+	for (int k = 0; k < K; k++)
+		base[k] = v[k] != kNoAgent && lane == first[k] ? atomicAdd(a.counts + v[k], end[k] - first[k]) : 0u;
+#pragma unroll
+	for (int k = 0; k < K; k++)
+	{
+		const uint32_t b = __shfl_sync(0xffffffffu, base[k], first[k]);
+		if (v[k] != kNoAgent)
+			a.rank[i0 + 32 * k] = b + (lane - first[k]);
+	}
 }
 
 // Change of an internalized amount.  The FP64 build evaluates the reference's
