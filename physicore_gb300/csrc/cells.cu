@@ -326,24 +326,40 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) cells_apply_kerne
 // (agent_apply returns at once for the others): with many agents per voxel most
 // agents only lose their ballot, and a thread per agent would mostly wait on its
 // role byte.  Grid-stride, so the grid need not match the device-side count.
-template <typename T>
+// SC: S fixed at compile time (1-8), else 0.
+template <typename T, int SC>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) cells_apply_writers_kernel(CellArgs a)
 {
 	const uint32_t count = __ldg(a.flags + 4);
 	const bool list = 2ull * count < a.A;
 	const uint64_t n = list ? count : a.A;
 	for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x)
-		agent_apply<T>(a, list ? __ldg(a.writers + j) : j);
+		agent_apply<T, SC>(a, list ? __ldg(a.writers + j) : j);
 }
 
 // Over the list of agents in shared voxels (empty when there was no conflict).
-template <typename T>
+template <typename T, int SC>
 __global__ void cells_internalize_kernel(CellArgs a)
 {
 	const uint32_t count = __ldg(a.flags + a.list_word);
 	for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < count; j += (uint64_t)gridDim.x * blockDim.x)
-		agent_internalize<T>(a, __ldg(a.shared + j));
+		agent_internalize<T, SC>(a, __ldg(a.shared + j));
 }
+
+// Launches KERNEL<T, S> for S = 1..8, KERNEL<T, 0> otherwise.
+#define PCG_LAUNCH_BY_S(KERNEL, T, S, GRID, BLOCK, STREAM, ARGS)                                                       \
+	switch (S)                                                                                                         \
+	{                                                                                                                  \
+	case 1: KERNEL<T, 1><<<GRID, BLOCK, 0, STREAM>>>(ARGS); break;                                                   \
+	case 2: KERNEL<T, 2><<<GRID, BLOCK, 0, STREAM>>>(ARGS); break;                                                   \
+	case 3: KERNEL<T, 3><<<GRID, BLOCK, 0, STREAM>>>(ARGS); break;                                                   \
+	case 4: KERNEL<T, 4><<<GRID, BLOCK, 0, STREAM>>>(ARGS); break;                                                   \
+	case 5: KERNEL<T, 5><<<GRID, BLOCK, 0, STREAM>>>(ARGS); break;                                                   \
+	case 6: KERNEL<T, 6><<<GRID, BLOCK, 0, STREAM>>>(ARGS); break;                                                   \
+	case 7: KERNEL<T, 7><<<GRID, BLOCK, 0, STREAM>>>(ARGS); break;                                                   \
+	case 8: KERNEL<T, 8><<<GRID, BLOCK, 0, STREAM>>>(ARGS); break;                                                   \
+	default: KERNEL<T, 0><<<GRID, BLOCK, 0, STREAM>>>(ARGS);                                                         \
+	}
 
 // release_internal (cell_solver.cpp:274-289) for one agent
 template <typename T>
@@ -524,8 +540,8 @@ static int run_cells(Context* c, bool recompute)
 	// per writer: list entry, role, offset, summed (or own) terms, density read and
 	// write, internalized amounts read and written
 	launch_begin(c, K_CELLS_APPLY, 0.0, &ev);
-	cells_apply_writers_kernel<T>
-		<<<std::min<unsigned>(grid, 12 * std::max(c->sm_count, 1)), block, 0, c->stream>>>(a);
+	const unsigned agrid = std::min<unsigned>(grid, 24 * std::max(c->sm_count, 1));
+	PCG_LAUNCH_BY_S(cells_apply_writers_kernel, T, c->S, agrid, block, c->stream, a);
 	launch_end(c, K_CELLS_APPLY, ev, 0.0, 9 + 3 * S * w + 2 * S * w + (c->compute_internalized ? 16 * S : 0));
 	PCG_CUDA_TRY(cudaGetLastError());
 	if (c->compute_internalized)
@@ -533,7 +549,8 @@ static int run_cells(Context* c, bool recompute)
 		// the agents that share a voxel (a few percent at 1e6 agents in 320^3 voxels):
 		// list entry, offset, density, own terms, internalized read and write each
 		launch_begin(c, K_CELLS_INTERNALIZE, 0.0, &ev);
-		cells_internalize_kernel<T><<<std::min<unsigned>(grid, 8 * std::max(c->sm_count, 1)), block, 0, c->stream>>>(a);
+		const unsigned igrid = std::min<unsigned>(grid, 24 * std::max(c->sm_count, 1));
+		PCG_LAUNCH_BY_S(cells_internalize_kernel, T, c->S, igrid, block, c->stream, a);
 		launch_end(c, K_CELLS_INTERNALIZE, ev, 8.0 + 4 * S * w + 16 * S);
 		PCG_CUDA_TRY(cudaGetLastError());
 	}
@@ -610,7 +627,7 @@ int launch_cells_fp32_buffers(const CellStepBuffers& b, cudaStream_t stream)
 		return rc;
 	cells_apply_kernel<float><<<grid, block, 0, stream>>>(a);
 	if (b.internalized)
-		cells_internalize_kernel<float><<<grid, block, 0, stream>>>(a);
+		cells_internalize_kernel<float, 0><<<grid, block, 0, stream>>>(a);
 	PCG_CUDA_TRY(cudaGetLastError());
 	return PCG_OK;
 }

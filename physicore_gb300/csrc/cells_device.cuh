@@ -496,7 +496,7 @@ __device__ __forceinline__ float fp32_update(float D, float num, float den, floa
 // (cell_solver.cpp:229-243).  An agent alone in its voxel has just written that
 // final density itself, so it applies the update here, from the same values, and
 // agent_internalize takes only the agents of shared voxels.
-template <typename T>
+template <typename T, int SC = 0>
 __device__ __forceinline__ void agent_apply(const CellArgs& a, uint64_t i)
 {
 	const uint8_t role = a.role[i];
@@ -507,7 +507,7 @@ __device__ __forceinline__ void agent_apply(const CellArgs& a, uint64_t i)
 	const bool track = alone && a.internalized;
 	const bool fused = track && __ldg(a.flags) == 0;
 	const bool vec = a.vec;
-	const uint32_t S = (uint32_t)a.S;
+	const uint32_t S = SC ? (uint32_t)SC : (uint32_t)a.S; // SC: S fixed at compile time (1-8), else 0
 	T* __restrict__ D = static_cast<T*>(a.field) + off;
 	const T* __restrict__ rn = static_cast<const T*>(alone ? a.num : a.rnum) + i * a.ts;
 	const T* __restrict__ rd = static_cast<const T*>(alone ? a.den : a.rden) + i * a.ts;
@@ -554,11 +554,11 @@ __device__ __forceinline__ void agent_apply(const CellArgs& a, uint64_t i)
 
 // compute_internalized after a conflict (cell_solver.cpp:132-143) for agent i of
 // a voxel that holds several agents (an entry of the shared list).
-template <typename T>
+template <typename T, int SC = 0>
 __device__ __forceinline__ void agent_internalize(const CellArgs& a, uint64_t i)
 {
 	const bool vec = a.vec;
-	const uint32_t S = (uint32_t)a.S;
+	const uint32_t S = SC ? (uint32_t)SC : (uint32_t)a.S;
 	const T* __restrict__ D = static_cast<const T*>(a.field) + a.foff[i];
 	const T* __restrict__ nu = static_cast<const T*>(a.num) + i * a.ts;
 	const T* __restrict__ de = static_cast<const T*>(a.den) + i * a.ts;

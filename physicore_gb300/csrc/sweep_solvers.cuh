@@ -184,28 +184,6 @@ __device__ __forceinline__ LineCoef<T> line_coef(const T* comp, uint32_t S, uint
 	return L;
 }
 
-// Coefficients of the block of kBlock points starting at j0 (a multiple of kBlock).
-template <typename T, typename V, int NV>
-__device__ __forceinline__ void fetch_block(const T* head, uint32_t H, T mid, T last, uint32_t n, uint32_t j0,
-											V (&out)[NV])
-{
-	constexpr int VN = Vec16<T>::N;
-	if (j0 + kBlock <= H)
-	{
-#pragma unroll
-		for (int v = 0; v < NV; v++)
-			out[v] = __ldg(reinterpret_cast<const V*>(head + j0) + v);
-	}
-	else
-	{
-#pragma unroll
-		for (int v = 0; v < NV; v++)
-#pragma unroll
-			for (int u = 0; u < VN; u++)
-				vset<V, T>(out[v], u, j0 + v * VN + u == n - 1 ? last : mid);
-	}
-}
-
 template <typename T>
 __device__ __forceinline__ T coef_at(const T* head, uint32_t H, T mid, T last, uint32_t n, uint32_t j)
 {
@@ -213,10 +191,15 @@ __device__ __forceinline__ T coef_at(const T* head, uint32_t H, T mid, T last, u
 }
 
 // One line of n points at col[j * stride] in shared memory (stride = STRIDE, or the
-// run-time value when STRIDE is 0) with the lane's coefficients L.  Blocks of
-// kBlock points are pipelined: the next block's points and coefficients are
-// requested before the current block's dependent chain, so load latency overlaps
-// it; most blocks take their coefficients from registers (the middle constants).
+// run-time value when STRIDE is 0) with the lane's coefficients L.  The line is
+// three runs: head blocks of kBlock points [0, hb) (coefficients from the head
+// rows), middle blocks [hb, q) (the middle constants, held in registers) and the
+// points from q * kBlock on, which hold point n-1 (coefficients chosen per point;
+// at most 2 kBlock - 1 of them).  Within a run the next block's points (and head
+// coefficients) are requested before the current block's dependent chain, so
+// their latency overlaps it; the middle run, nearly the whole line, alternates two
+// register sets, so that its blocks carry no copies or tests.  Which run a block
+// is in is the same for every lane of a warp (one n and H per launch).
 //
 // MC (kMcIn / kMcOut bits) adds the line's input values to *acc_in and its
 // solved values to *acc_out.
@@ -229,151 +212,175 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 	constexpr bool kLo = sizeof(T) == 4;
 	const uint32_t st = STRIDE ? (uint32_t)STRIDE : rt_stride;
 	const uint32_t nb = n / P;
+	const uint32_t hb = min(L.H / P, nb);
+	const uint32_t q = max((n - 1) / P, hb); // blocks [hb, q) have j0 >= H and j0 + P <= n - 1
 	const T c = L.c;
-	// A block of points is a head block (coefficients loaded), a middle block (the
-	// middle constants, no per-point selection) or the block holding point n-1.
-	// The test is the same for every lane of a warp (one n and H per launch).
-	auto is_mid = [&](uint32_t j0) { return j0 >= L.H && j0 + P <= n - 1; };
 	// the middle coupling of the backward step, as bwd_step forms it per point
 	const T mbc = kLo ? L.mB * c : T(0);
+	// offsets within the tile stay far below 2^32
+	auto load = [&](uint32_t b, T(&x)[P]) {
+		const T* blk = col + b * (uint32_t)P * st;
+#pragma unroll
+		for (int k = 0; k < P; k++)
+			x[k] = blk[k * st];
+	};
+	auto fetch_head = [&](const T* head, uint32_t b, V(&out)[NV]) {
+#pragma unroll
+		for (int v = 0; v < NV; v++)
+			out[v] = __ldg(reinterpret_cast<const V*>(head + b * P) + v);
+	};
 	T d = T(0);
+
+	// ---- forward elimination
+	auto fwd_mid = [&](uint32_t b, const T(&x)[P]) {
+		T* blk = col + b * (uint32_t)P * st;
+		if constexpr ((MC & kMcIn) != 0)
+			acc_in->add_block(x);
+#pragma unroll
+		for (int k = 0; k < P; k++)
+		{
+			d = dev::fmadd(L.mE, d, x[k]);
+			blk[k * st] = d;
+		}
+	};
+	if (hb)
 	{
 		T x[P], xn[P];
 		V e[NV], en[NV];
-		bool mid = false;
-		if (nb)
+		load(0, x);
+		fetch_head(L.hE, 0, e);
+		for (uint32_t b = 0; b < hb; b++)
 		{
-#pragma unroll
-			for (int q = 0; q < P; q++)
-				x[q] = col[q * st];
-			mid = is_mid(0);
-			if (!mid)
-				fetch_block<T, V, NV>(L.hE, L.H, L.mE, L.lE, n, 0, e);
-		}
-		for (uint32_t b = 0; b < nb; b++)
-		{
-			T* blk = col + (uint64_t)b * P * st;
-			bool mid_next = false;
-			if (b + 1 < nb)
+			if (b + 1 < hb)
 			{
-#pragma unroll
-				for (int q = 0; q < P; q++)
-					xn[q] = blk[(P + q) * st];
-				mid_next = is_mid((b + 1) * P);
-				if (!mid_next)
-					fetch_block<T, V, NV>(L.hE, L.H, L.mE, L.lE, n, (b + 1) * P, en);
+				load(b + 1, xn);
+				fetch_head(L.hE, b + 1, en);
 			}
 			if constexpr ((MC & kMcIn) != 0)
 				acc_in->add_block(x);
-			if (mid)
-			{
+			T* blk = col + b * (uint32_t)P * st;
 #pragma unroll
-				for (int q = 0; q < P; q++)
-				{
-					d = dev::fmadd(L.mE, d, x[q]);
-					blk[q * st] = d;
-				}
-			}
-			else
+			for (int k = 0; k < P; k++)
 			{
-#pragma unroll
-				for (int q = 0; q < P; q++)
-				{
-					d = dev::fmadd(vget<V, T>(e[q / VN], q % VN), d, x[q]);
-					blk[q * st] = d;
-				}
+				d = dev::fmadd(vget<V, T>(e[k / VN], k % VN), d, x[k]);
+				blk[k * st] = d;
 			}
 #pragma unroll
-			for (int q = 0; q < P; q++)
-				x[q] = xn[q];
+			for (int k = 0; k < P; k++)
+				x[k] = xn[k];
 #pragma unroll
 			for (int v = 0; v < NV; v++)
 				e[v] = en[v];
-			mid = mid_next;
-		}
-		for (uint32_t j = nb * P; j < n; j++)
-		{
-			const T xj = col[(uint64_t)j * st];
-			if constexpr ((MC & kMcIn) != 0)
-				acc_in->add(xj);
-			d = dev::fmadd(coef_at(L.hE, L.H, L.mE, L.lE, n, j), d, xj);
-			col[(uint64_t)j * st] = d;
 		}
 	}
+	if (hb < q)
+	{
+		T xa[P], xb[P];
+		uint32_t b = hb;
+		load(b, xa);
+		for (; b + 2 < q; b += 2)
+		{
+			load(b + 1, xb);
+			fwd_mid(b, xa);
+			load(b + 2, xa);
+			fwd_mid(b + 1, xb);
+		}
+		if (b + 1 < q)
+		{
+			load(b + 1, xb);
+			fwd_mid(b, xa);
+			fwd_mid(b + 1, xb);
+		}
+		else
+			fwd_mid(b, xa);
+	}
+	for (uint32_t j = q * P; j < n; j++)
+	{
+		const T xj = col[j * st];
+		if constexpr ((MC & kMcIn) != 0)
+			acc_in->add(xj);
+		d = dev::fmadd(coef_at(L.hE, L.H, L.mE, L.lE, n, j), d, xj);
+		col[j * st] = d;
+	}
+
+	// ---- back substitution
 	d = T(0);
-	for (int j = (int)n - 1; j >= (int)(nb * P); j--)
+	for (int j = (int)n - 1; j >= (int)(q * P); j--)
 	{
 		const T bl = kLo ? coef_at(L.hBl, L.H, L.mBl, L.lBl, n, (uint32_t)j) : T(0);
-		d = bwd_step(c, d, col[(uint64_t)j * st], coef_at(L.hB, L.H, L.mB, L.lB, n, (uint32_t)j), bl);
-		col[(uint64_t)j * st] = d;
+		d = bwd_step(c, d, col[(uint32_t)j * st], coef_at(L.hB, L.H, L.mB, L.lB, n, (uint32_t)j), bl);
+		col[(uint32_t)j * st] = d;
 		if constexpr ((MC & kMcOut) != 0)
 			acc_out->add(d);
 	}
+	auto bwd_mid = [&](uint32_t b, const T(&x)[P]) {
+		T* blk = col + b * (uint32_t)P * st;
+		T y[P];
+#pragma unroll
+		for (int k = P - 1; k >= 0; k--)
+		{
+			if constexpr (kLo)
+				d = dev::fmadd(mbc, d, dev::fmadd(x[k], L.mB, x[k] * L.mBl));
+			else
+				d = dev::fmadd(c, d, x[k]) * L.mB;
+			blk[k * st] = d;
+			y[k] = d;
+		}
+		if constexpr ((MC & kMcOut) != 0)
+			acc_out->add_block(y);
+	};
+	if (hb < q)
+	{
+		T xa[P], xb[P];
+		uint32_t b = q - 1;
+		load(b, xa);
+		for (; b >= hb + 2; b -= 2)
+		{
+			load(b - 1, xb);
+			bwd_mid(b, xa);
+			load(b - 2, xa);
+			bwd_mid(b - 1, xb);
+		}
+		if (b >= hb + 1)
+		{
+			load(b - 1, xb);
+			bwd_mid(b, xa);
+			bwd_mid(b - 1, xb);
+		}
+		else
+			bwd_mid(b, xa);
+	}
+	if (hb)
 	{
 		T x[P], xn[P];
 		V bb[NV], bn[NV], bl[NV], bln[NV];
-		bool mid = false;
-		if (nb)
+		load(hb - 1, x);
+		fetch_head(L.hB, hb - 1, bb);
+		if constexpr (kLo)
+			fetch_head(L.hBl, hb - 1, bl);
+		for (int b = (int)hb - 1; b >= 0; b--)
 		{
-			const T* blk = col + (uint64_t)(nb - 1) * P * st;
-#pragma unroll
-			for (int q = 0; q < P; q++)
-				x[q] = blk[q * st];
-			mid = is_mid((nb - 1) * P);
-			if (!mid)
-			{
-				fetch_block<T, V, NV>(L.hB, L.H, L.mB, L.lB, n, (nb - 1) * P, bb);
-				if constexpr (kLo)
-					fetch_block<T, V, NV>(L.hBl, L.H, L.mBl, L.lBl, n, (nb - 1) * P, bl);
-			}
-		}
-		for (int b = (int)nb - 1; b >= 0; b--)
-		{
-			T* blk = col + (uint64_t)b * P * st;
-			bool mid_next = false;
 			if (b > 0)
 			{
-#pragma unroll
-				for (int q = 0; q < P; q++)
-					xn[q] = blk[(q - P) * (int)st];
-				mid_next = is_mid((uint32_t)(b - 1) * P);
-				if (!mid_next)
-				{
-					fetch_block<T, V, NV>(L.hB, L.H, L.mB, L.lB, n, (uint32_t)(b - 1) * P, bn);
-					if constexpr (kLo)
-						fetch_block<T, V, NV>(L.hBl, L.H, L.mBl, L.lBl, n, (uint32_t)(b - 1) * P, bln);
-				}
+				load((uint32_t)b - 1, xn);
+				fetch_head(L.hB, (uint32_t)b - 1, bn);
+				if constexpr (kLo)
+					fetch_head(L.hBl, (uint32_t)b - 1, bln);
 			}
+			T* blk = col + (uint32_t)b * (uint32_t)P * st;
 			T y[P];
-			if (mid)
-			{
 #pragma unroll
-				for (int q = P - 1; q >= 0; q--)
-				{
-					if constexpr (kLo)
-						d = dev::fmadd(mbc, d, dev::fmadd(x[q], L.mB, x[q] * L.mBl));
-					else
-						d = dev::fmadd(c, d, x[q]) * L.mB;
-					blk[q * st] = d;
-					y[q] = d;
-				}
-			}
-			else
+			for (int k = P - 1; k >= 0; k--)
 			{
-#pragma unroll
-				for (int q = P - 1; q >= 0; q--)
-				{
-					d = bwd_step(c, d, x[q], vget<V, T>(bb[q / VN], q % VN),
-								 kLo ? vget<V, T>(bl[q / VN], q % VN) : T(0));
-					blk[q * st] = d;
-					y[q] = d;
-				}
+				d = bwd_step(c, d, x[k], vget<V, T>(bb[k / VN], k % VN), kLo ? vget<V, T>(bl[k / VN], k % VN) : T(0));
+				blk[k * st] = d;
+				y[k] = d;
 			}
 			if constexpr ((MC & kMcOut) != 0)
 				acc_out->add_block(y);
 #pragma unroll
-			for (int q = 0; q < P; q++)
-				x[q] = xn[q];
+			for (int k = 0; k < P; k++)
+				x[k] = xn[k];
 #pragma unroll
 			for (int v = 0; v < NV; v++)
 			{
@@ -381,11 +388,9 @@ __device__ __forceinline__ void solve_line(T* __restrict__ col, uint32_t n, uint
 				if constexpr (kLo)
 					bl[v] = bln[v];
 			}
-			mid = mid_next;
 		}
 	}
 }
-
 
 // S*sizeof(T) a multiple of 16 bytes: thread h of a row's TPR threads owns chunk
 // slot h of every x position (VN substrates, VN independent recurrences).
