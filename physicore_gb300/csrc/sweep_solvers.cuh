@@ -530,8 +530,12 @@ __device__ __forceinline__ void solve_row_chunks(T* row, const T* __restrict__ c
 
 // ST substrates (1..8) not filling whole chunks: the row is a stream of chunks,
 // element k of substrate k % ST.  Blocks of NB chunks hold whole groups of
-// lcm(ST, VN) elements, so each element's substrate is a compile-time index.
-// MC adds substrate s's inputs / outputs to acc_in[s] / acc_out[s].
+// lcm(ST, VN) elements, so each element's substrate is a compile-time index.  The
+// blocks that lie wholly inside the row run without per-element tests, two
+// register sets in turn (the next block's chunks and coefficients load while the
+// current block's chain runs, and no block is copied from one set to the other);
+// the chunks after them, at most NB + U - 1, test each element against the row's
+// end.  MC adds substrate s's inputs / outputs to acc_in[s] / acc_out[s].
 template <typename T, int ST, int MC = 0>
 __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, const T* __restrict__ cE,
 											  const T* __restrict__ cC, const T* __restrict__ cBl, uint32_t n,
@@ -543,7 +547,8 @@ __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, 
 	constexpr int U = GE / VN;
 	constexpr int NB = U * ((kChunkBlock + U - 1) / U); // chunks per block
 	const uint32_t total = n * ST;
-	const uint32_t nchunks = (total + GE - 1) / GE * U; // whole groups (tail elements predicated)
+	const uint32_t nchunks = (total + GE - 1) / GE * U; // whole groups (tail elements tested)
+	const uint32_t nfull = total / (NB * VN);           // blocks wholly inside the row
 	constexpr bool kLo = sizeof(T) == 4;
 	V* __restrict__ vrow = reinterpret_cast<V*>(row);
 	const V* vE = reinterpret_cast<const V*>(cE);
@@ -563,13 +568,14 @@ __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, 
 		c[s] = __ldg(cC + s);
 	}
 	// In a block or group starting at chunk k0 (k0*VN a multiple of ST), element
-	// k0*VN + q*VN + u has substrate (q*VN + u) % ST.
-	auto fwd_chunk = [&](V& v, const V& e, int q, uint32_t k) {
+	// k0*VN + q*VN + u has substrate (q*VN + u) % ST.  TEST: check the element
+	// against the row's end.
+	auto fwd_chunk = [&](V& v, const V& e, int q, uint32_t k, bool test) {
 #pragma unroll
 		for (int u = 0; u < VN; u++)
 		{
 			const int s = (q * VN + u) % ST;
-			if (k * VN + u < total)
+			if (!test || k * VN + u < total)
 			{
 				if constexpr ((MC & kMcIn) != 0)
 					acc_in[s].add(vget<V, T>(v, u));
@@ -578,12 +584,12 @@ __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, 
 			}
 		}
 	};
-	auto bwd_chunk = [&](V& v, const V& b, const V& bl, int q, uint32_t k) {
+	auto bwd_chunk = [&](V& v, const V& b, const V& bl, int q, uint32_t k, bool test) {
 #pragma unroll
 		for (int u = VN - 1; u >= 0; u--)
 		{
 			const int s = (q * VN + u) % ST;
-			if (k * VN + u < total)
+			if (!test || k * VN + u < total)
 			{
 				d[s] = bwd_step(c[s], d[s], vget<V, T>(v, u), vget<V, T>(b, u), kLo ? vget<V, T>(bl, u) : T(0));
 				vset<V, T>(v, u, d[s]);
@@ -592,99 +598,107 @@ __device__ __forceinline__ void solve_row_vec(T* row, const T* __restrict__ cB, 
 			}
 		}
 	};
-	const uint32_t nb = nchunks / NB;
-	{
-		V x[NB], xn[NB], e[NB], en[NB];
-		if (nb)
+
+	// ---- forward elimination
+	auto fwd_load = [&](uint32_t b, V(&x)[NB], V(&e)[NB]) {
 #pragma unroll
-			for (int q = 0; q < NB; q++)
-			{
-				x[q] = vrow[q];
-				e[q] = ldg_vec(vE + q);
-			}
-		for (uint32_t b = 0; b < nb; b++)
+		for (int q = 0; q < NB; q++)
 		{
-			const uint32_t k0 = b * NB;
-			if (b + 1 < nb)
-#pragma unroll
-				for (int q = 0; q < NB; q++)
-				{
-					xn[q] = vrow[k0 + NB + q];
-					en[q] = ldg_vec(vE + k0 + NB + q);
-				}
-#pragma unroll
-			for (int q = 0; q < NB; q++)
-			{
-				fwd_chunk(x[q], e[q], q, k0 + q);
-				vrow[k0 + q] = x[q];
-			}
-#pragma unroll
-			for (int q = 0; q < NB; q++)
-			{
-				x[q] = xn[q];
-				e[q] = en[q];
-			}
+			x[q] = vrow[b * NB + q];
+			e[q] = ldg_vec(vE + b * NB + q);
 		}
-		// remaining whole groups (fewer than NB chunks)
-		for (uint32_t k0 = nb * NB; k0 < nchunks; k0 += U)
-		{
+	};
+	auto fwd_block = [&](uint32_t b, V(&x)[NB], const V(&e)[NB]) {
 #pragma unroll
-			for (int q = 0; q < U; q++)
-			{
-				V v = vrow[k0 + q];
-				fwd_chunk(v, ldg_vec(vE + k0 + q), q, k0 + q);
-				vrow[k0 + q] = v;
-			}
+		for (int q = 0; q < NB; q++)
+		{
+			fwd_chunk(x[q], e[q], q, b * NB + q, false);
+			vrow[b * NB + q] = x[q];
+		}
+	};
+	if (nfull)
+	{
+		V xa[NB], ea[NB], xb[NB], eb[NB];
+		uint32_t b = 0;
+		fwd_load(0, xa, ea);
+		for (; b + 2 < nfull; b += 2)
+		{
+			fwd_load(b + 1, xb, eb);
+			fwd_block(b, xa, ea);
+			fwd_load(b + 2, xa, ea);
+			fwd_block(b + 1, xb, eb);
+		}
+		if (b + 1 < nfull)
+		{
+			fwd_load(b + 1, xb, eb);
+			fwd_block(b, xa, ea);
+			fwd_block(b + 1, xb, eb);
+		}
+		else
+			fwd_block(b, xa, ea);
+	}
+	for (uint32_t k0 = nfull * NB; k0 < nchunks; k0 += U)
+	{
+#pragma unroll
+		for (int q = 0; q < U; q++)
+		{
+			V v = vrow[k0 + q];
+			fwd_chunk(v, ldg_vec(vE + k0 + q), q, k0 + q, true);
+			vrow[k0 + q] = v;
 		}
 	}
+
+	// ---- back substitution
 #pragma unroll
 	for (int s = 0; s < ST; s++)
 		d[s] = T(0);
-	for (int k0 = (int)nchunks - U; k0 >= (int)(nb * NB); k0 -= U)
+	for (int k0 = (int)nchunks - U; k0 >= (int)(nfull * NB); k0 -= U)
 	{
 #pragma unroll
 		for (int q = U - 1; q >= 0; q--)
 		{
 			V v = vrow[k0 + q];
-			bwd_chunk(v, ldg_vec(vB + k0 + q), ldg_lo(k0 + q), q, (uint32_t)(k0 + q));
+			bwd_chunk(v, ldg_vec(vB + k0 + q), ldg_lo(k0 + q), q, (uint32_t)(k0 + q), true);
 			vrow[k0 + q] = v;
 		}
 	}
-	{
-		V x[NB], xn[NB], bb[NB], bn[NB], bl[NB], bln[NB];
-		if (nb)
+	auto bwd_load = [&](uint32_t b, V(&x)[NB], V(&bb)[NB], V(&bl)[NB]) {
 #pragma unroll
-			for (int q = 0; q < NB; q++)
-			{
-				x[q] = vrow[(nb - 1) * NB + q];
-				bb[q] = ldg_vec(vB + (nb - 1) * NB + q);
-				bl[q] = ldg_lo((nb - 1) * NB + q);
-			}
-		for (int b = (int)nb - 1; b >= 0; b--)
+		for (int q = 0; q < NB; q++)
 		{
-			const uint32_t k0 = (uint32_t)b * NB;
-			if (b > 0)
-#pragma unroll
-				for (int q = 0; q < NB; q++)
-				{
-					xn[q] = vrow[k0 - NB + q];
-					bn[q] = ldg_vec(vB + k0 - NB + q);
-					bln[q] = ldg_lo(k0 - NB + q);
-				}
-#pragma unroll
-			for (int q = NB - 1; q >= 0; q--)
-			{
-				bwd_chunk(x[q], bb[q], bl[q], q, k0 + q);
-				vrow[k0 + q] = x[q];
-			}
-#pragma unroll
-			for (int q = 0; q < NB; q++)
-			{
-				x[q] = xn[q];
-				bb[q] = bn[q];
-				bl[q] = bln[q];
-			}
+			x[q] = vrow[b * NB + q];
+			bb[q] = ldg_vec(vB + b * NB + q);
+			bl[q] = ldg_lo(b * NB + q);
 		}
+	};
+	auto bwd_block = [&](uint32_t b, V(&x)[NB], const V(&bb)[NB], const V(&bl)[NB]) {
+#pragma unroll
+		for (int q = NB - 1; q >= 0; q--)
+		{
+			bwd_chunk(x[q], bb[q], bl[q], q, b * NB + q, false);
+			vrow[b * NB + q] = x[q];
+		}
+	};
+	if (nfull)
+	{
+		V xa[NB], ba[NB], la[NB], xb[NB], bbb[NB], lb[NB];
+		uint32_t b = nfull - 1;
+		bwd_load(b, xa, ba, la);
+		for (; b >= 2; b -= 2)
+		{
+			bwd_load(b - 1, xb, bbb, lb);
+			bwd_block(b, xa, ba, la);
+			bwd_load(b - 2, xa, ba, la);
+			bwd_block(b - 1, xb, bbb, lb);
+		}
+		if (b >= 1)
+		{
+			bwd_load(b - 1, xb, bbb, lb);
+			bwd_block(b, xa, ba, la);
+			bwd_block(b - 1, xb, bbb, lb);
+		}
+		else
+			bwd_block(b, xa, ba, la);
 	}
 }
 
