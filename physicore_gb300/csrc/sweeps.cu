@@ -87,7 +87,9 @@ __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __g
 		if (t >= a.tiles)
 			break;
 		const int x0 = (int)((t % a.xblocks) * kLanes);
-		const int o = (int)(t / a.xblocks);
+		// y takes its z-planes from the last down: the x sweep that ran just before
+		// wrote the highest planes last, and their lines are still in L2
+		const int o = AXIS == 1 ? (int)(a.tiles / a.xblocks - 1 - t / a.xblocks) : (int)(t / a.xblocks);
 		if (lane == 0)
 		{
 			dev::mbar_arrive_expect_tx(full, nc * chunk_elems * (uint32_t)sizeof(T));
