@@ -1083,6 +1083,55 @@ def run_dense(args, local):
     return out
 
 
+def run_served_batch(args, local):
+    """A steady batch of the served mix: the first N requests of the served stream
+    (workloads.ServedStream), initialised and stepped together with every request
+    taking part in every step.  About the server's active set at its 1,024-request
+    cap for N = 990; it explains the served rate apart from admissions, ticks and
+    readbacks.  With --served-batch-direct the steps are launched directly instead
+    of replayed from a graph (so that a profiler sees each kernel)."""
+    import torch
+
+    import physicore_gb300 as pcg
+    from physicore_gb300 import workloads as W
+    N = args.only_served_batch
+    stream = W.ServedStream(duration=600)
+    t0 = time.perf_counter()
+    sol = []
+    for i in range(N):
+        s = stream.request(pcg.Solver(pcg.FP32, device=local), i)
+        s.initialize()
+        sol.append(s)
+    setup_s = time.perf_counter() - t0
+    vss = sum(int(np.prod(stream.sides[i])) * int(stream.S[i]) for i in range(N))
+    b = pcg.Batch(sol)
+    b.set_graph(not args.served_batch_direct)
+    b.solve(max(3, args.warmup))
+    b.synchronize()
+    bs = torch.cuda.ExternalStream(b.stream())
+    steps = args.served_batch_steps
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(bs)
+    b.solve(steps)
+    ev1.record(bs)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    b.set_kernel_timing(True)
+    b.reset_kernel_stats()
+    b.solve(min(steps, 8))
+    b.synchronize()
+    kt = kernel_table(b.kernel_stats())
+    b.set_kernel_timing(False)
+    b.close()
+    for s in sol:
+        s.close()
+    return {"workload": f"the first {N} requests of the served stream (sides log-uniform [32,256] per axis, "
+                        "1-8 substrates, 0-200,000 agents, FP32), every one stepping",
+            "requests": N, "vss_per_step": vss, "agents": int(sum(int(a) for a in stream.A[:N])),
+            "steps": steps, "ms_per_step": ms, "value": vss / (ms / 1e3), "unit": UNIT,
+            "graph": not args.served_batch_direct, "setup_s": round(setup_s, 1), "kernels": kt}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1111,6 +1160,10 @@ def main():
                     help="queued requests beyond which submissions are refused (0: no practical limit)")
     ap.add_argument("--dense-steps", type=int, default=100, help="steps of the dense-agent workload (0: skip)")
     ap.add_argument("--only-dense", action="store_true", help="run only the dense-agent workload")
+    ap.add_argument("--only-served-batch", type=int, default=0,
+                    help="run only a steady batch of the first N requests of the served stream")
+    ap.add_argument("--served-batch-steps", type=int, default=16)
+    ap.add_argument("--served-batch-direct", action="store_true", help="direct launches instead of a graph")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -1119,7 +1172,8 @@ def main():
         run_reference(args, w)
         return
     only = [(args.only_serve, "serve", run_serve), (args.only_dense, "dense", run_dense),
-            (args.only_batched, "batched", lambda a, l: run_batched(a, l, ClockSampler))]
+            (args.only_batched, "batched", lambda a, l: run_batched(a, l, ClockSampler)),
+            (args.only_served_batch > 0, "served_batch", run_served_batch)]
     for flag, name, fn in only:
         if flag:
             import torch
