@@ -448,14 +448,27 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 		const uint32_t R = D.box_rows[AXIS], nc = D.boxes[AXIS], n = D.n[AXIS], S = D.S;
 		const uint32_t chunk_elems = R * kLanes, tile_elems = nc * chunk_elems;
 		const CUtensorMap* map = b.tmaps + 2 * di + (AXIS - 1);
+		// the unit's first tile (x block, outer index) by one 32-bit division per unit
+		// (a domain has fewer than 2^32 tiles); the following tiles step from it, so
+		// no tile's load, solve or store divides
+		const uint32_t xblocks = (uint32_t)D.yz_xblocks;
+		const uint32_t xb0 = (uint32_t)lt0 % xblocks, ob0 = (uint32_t)lt0 / xblocks;
+		auto step_tile = [xblocks](uint32_t& xb, uint32_t& ob) {
+			if (++xb == xblocks)
+			{
+				xb = 0;
+				ob++;
+			}
+		};
 		if (lane == 0)
 		{
 			if (di != prev)
 				fence_tensormap_acquire(map);
 			dev::mbar_arrive_expect_tx(full, gcount * tile_elems * (uint32_t)sizeof(T));
-			for (uint32_t j = 0; j < gcount; j++)
+			uint32_t xb = xb0, ob = ob0;
+			for (uint32_t j = 0; j < gcount; j++, step_tile(xb, ob))
 			{
-				const int x0 = (int)(((lt0 + j) % D.yz_xblocks) * kLanes), o = (int)((lt0 + j) / D.yz_xblocks);
+				const int x0 = (int)(xb * kLanes), o = (int)ob;
 				for (uint32_t c = 0; c < nc; c++)
 				{
 					T* dst = base + j * tile_elems + c * chunk_elems;
@@ -469,7 +482,8 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 		prev = di;
 		const T* comp = static_cast<const T*>(D.coef[AXIS]) + D.coef_comp_off[AXIS];
 		// the first tile's coefficient loads overlap the group's arrival
-		int x0 = (int)((lt0 % D.yz_xblocks) * kLanes), o = (int)(lt0 / D.yz_xblocks);
+		uint32_t xb = xb0, ob = ob0;
+		int x0 = (int)(xb * kLanes), o = (int)ob;
 		LineCoef<T> L = line_coef<T>(comp, S, D.coef_head[AXIS], n,
 									 (uint64_t)(x0 + lane) < D.row_len ? (uint32_t)((x0 + lane) % S) : 0);
 		ok = __all_sync(0xffffffffu, dev::mbar_wait(full, phase));
@@ -482,7 +496,8 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 		{
 			if (j)
 			{
-				x0 = (int)(((lt0 + j) % D.yz_xblocks) * kLanes), o = (int)((lt0 + j) / D.yz_xblocks);
+				step_tile(xb, ob);
+				x0 = (int)(xb * kLanes), o = (int)ob;
 				L = line_coef<T>(comp, S, D.coef_head[AXIS], n,
 								 (uint64_t)(x0 + lane) < D.row_len ? (uint32_t)((x0 + lane) % S) : 0);
 			}
@@ -492,7 +507,7 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 			if constexpr (MC != 0)
 				if (D.mc_tot && D.dims == AXIS + 1)
 					flush_classes(acc.value(), S < kLanes ? S : kLanes, kLanes,
-								  D.mc_tot + S + ((uint64_t)x0 + lane) % S);
+								  D.mc_tot + S + ((uint32_t)x0 + lane) % S);
 			// the last sweep of the domain writes its boundary faces (the batch's
 			// Dirichlet launch then covers interior nodes and 1-D domains only)
 			if (D.dims == AXIS + 1)
@@ -503,9 +518,10 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 		__syncwarp();
 		if (lane == 0)
 		{
-			for (uint32_t j = 0; j < gcount; j++)
+			uint32_t xs_b = xb0, os_b = ob0;
+			for (uint32_t j = 0; j < gcount; j++, step_tile(xs_b, os_b))
 			{
-				const int xs = (int)(((lt0 + j) % D.yz_xblocks) * kLanes), os = (int)((lt0 + j) / D.yz_xblocks);
+				const int xs = (int)(xs_b * kLanes), os = (int)os_b;
 				for (uint32_t c = 0; c < nc; c++)
 				{
 					T* src = base + j * tile_elems + c * chunk_elems;

@@ -78,18 +78,20 @@ __global__ void __launch_bounds__(kLanes) sweep_yz_kernel(SweepArgs a, const __g
 	acc.zero();
 	const bool per_tile = (kLanes % S) != 0;
 	const uint32_t classes = S < kLanes ? S : kLanes;
+	// 32-bit tile arithmetic: a launch has fewer than 2^32 tiles
+	const uint32_t xblocks = (uint32_t)a.xblocks, nouter = (uint32_t)(a.tiles / a.xblocks);
 	for (uint32_t phase = 0;; phase ^= 1)
 	{
 		uint32_t t32 = 0;
 		if (lane == 0)
 			t32 = atomicAdd(a.ticket, 1u);
-		const uint64_t t = __shfl_sync(0xffffffffu, t32, 0);
+		const uint32_t t = __shfl_sync(0xffffffffu, t32, 0);
 		if (t >= a.tiles)
 			break;
-		const int x0 = (int)((t % a.xblocks) * kLanes);
+		const int x0 = (int)((t % xblocks) * kLanes);
 		// y takes its z-planes from the last down: the x sweep that ran just before
 		// wrote the highest planes last, and their lines are still in L2
-		const int o = AXIS == 1 ? (int)(a.tiles / a.xblocks - 1 - t / a.xblocks) : (int)(t / a.xblocks);
+		const int o = AXIS == 1 ? (int)(nouter - 1 - t / xblocks) : (int)(t / xblocks);
 		if (lane == 0)
 		{
 			dev::mbar_arrive_expect_tx(full, nc * chunk_elems * (uint32_t)sizeof(T));
