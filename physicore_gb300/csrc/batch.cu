@@ -424,18 +424,30 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 	uint32_t next = 0;
 	if (lane == 0)
 		next = atomicAdd(b.counter, 1u);
+	// A unit's work-list entry and domain are resolved while the previous unit's
+	// tiles load, and a new domain's descriptor is prefetched into L1 then.
+	auto resolve = [&](uint64_t u, uint32_t& k, uint32_t& di) {
+		k = di = 0;
+		if (u < b.list.total)
+		{
+			k = find_entry(b.list, u);
+			di = __ldg(b.list.dom + k);
+		}
+	};
+	uint64_t t = __shfl_sync(0xffffffffu, next, 0);
+	uint32_t k, di;
+	resolve(t, k, di);
 	for (;; phase ^= 1)
 	{
-		const uint64_t t = __shfl_sync(0xffffffffu, next, 0);
 		if (t >= b.list.total)
 			break;
 		if (lane == 0)
 			next = atomicAdd(b.counter, 1u); // the following tile's ticket, in flight meanwhile
-		const uint32_t k = find_entry(b.list, t);
-		const uint32_t di = __ldg(b.list.dom + k);
 		if (b.steps_left[di] == 0)
 		{
 			phase ^= 1; // no tile was loaded: keep the barrier's parity
+			t = __shfl_sync(0xffffffffu, next, 0);
+			resolve(t, k, di);
 			continue;
 		}
 		const BatchDomain& D = b.doms[di];
@@ -480,6 +492,11 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 			}
 		}
 		prev = di;
+		const uint64_t tn = __shfl_sync(0xffffffffu, next, 0);
+		uint32_t kn, dn;
+		resolve(tn, kn, dn);
+		if (dn != di && lane * 128 < sizeof(BatchDomain))
+			asm volatile("prefetch.global.L1 [%0];" ::"l"(reinterpret_cast<const char*>(b.doms + dn) + lane * 128));
 		const T* comp = static_cast<const T*>(D.coef[AXIS]) + D.coef_comp_off[AXIS];
 		// the first tile's coefficient loads overlap the group's arrival
 		uint32_t xb = xb0, ob = ob0;
@@ -535,6 +552,9 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_yz_kernel(BatchArgs b)
 			dev::bulk_wait_read();
 		}
 		__syncwarp();
+		t = tn;
+		k = kn;
+		di = dn;
 	}
 	if (!ok && lane == 0)
 		report(b, DEV_ERR_WAIT_TIMEOUT, bad);
