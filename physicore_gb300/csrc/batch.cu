@@ -311,7 +311,6 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 {
 	extern __shared__ __align__(128) unsigned char smem[];
 	uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
-	uint32_t& s_ticket = *reinterpret_cast<uint32_t*>(smem + 8);
 	T* tile = reinterpret_cast<T*>(smem + 16);
 	const uint32_t tid = threadIdx.x;
 	if (tid == 0)
@@ -324,21 +323,30 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 	uint32_t next = 0;
 	if (tid == 0)
 		next = atomicAdd(b.counter, 1u);
+	// A unit's work-list entry and domain are resolved while the previous unit's
+	// rows load, and a new domain's descriptor is prefetched into L1 then (the CTA
+	// is one warp).
+	auto resolve = [&](uint64_t u, uint32_t& k, uint32_t& di) {
+		k = di = 0;
+		if (u < b.list.total)
+		{
+			k = find_entry(b.list, u);
+			di = __ldg(b.list.dom + k);
+		}
+	};
+	uint64_t t = __shfl_sync(0xffffffffu, next, 0);
+	uint32_t k, di;
+	resolve(t, k, di);
 	for (;;)
 	{
-		if (tid == 0)
-			s_ticket = next;
-		__syncthreads();
-		const uint64_t t = s_ticket;
 		if (t >= b.list.total)
 			break;
 		if (tid == 0)
 			next = atomicAdd(b.counter, 1u); // the following tile's ticket, in flight meanwhile
-		const uint32_t k = find_entry(b.list, t);
-		const uint32_t di = __ldg(b.list.dom + k);
 		if (b.steps_left[di] == 0)
 		{
-			__syncthreads(); // everyone has read the ticket before thread 0 draws the next
+			t = __shfl_sync(0xffffffffu, next, 0);
+			resolve(t, k, di);
 			continue;
 		}
 		const BatchDomain& D = b.doms[di];
@@ -353,6 +361,11 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 		__syncthreads();
 		if (tid < nrows)
 			dev::bulk_g2s(tile + tid * spitch, g + tid * D.pitch, row_bytes, bar);
+		const uint64_t tn = __shfl_sync(0xffffffffu, next, 0);
+		uint32_t kn, dn;
+		resolve(tn, kn, dn);
+		if (dn != di && tid * 128 < sizeof(BatchDomain))
+			asm volatile("prefetch.global.L1 [%0];" ::"l"(reinterpret_cast<const char*>(b.doms + dn) + tid * 128));
 		const T* cB = static_cast<const T*>(D.coef[0]);
 		const T* cE = cB + D.coef_len[0];
 		const T* cC = cE + D.coef_len[0];
@@ -396,6 +409,9 @@ __global__ void __launch_bounds__(kLanes) batch_sweep_x_kernel(BatchArgs b)
 		dev::bulk_wait_read();
 		__syncthreads();
 		phase ^= 1;
+		t = tn;
+		k = kn;
+		di = dn;
 	}
 	dev::bulk_wait_all();
 }
