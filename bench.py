@@ -509,7 +509,7 @@ def run_gb300(args, w):
             "gpu_launches": int(launches), "clocks": clk.summary(), "e2e": e2e,
             "mass_check": {k: mass_check[k] for k in ("on_in_headline", "overhead", "worst_residual")}}
 
-    # CPU baseline (the oracle on the machine's cores, a bounded sample) and the FP32
+    # CPU baseline (the oracle on the host's cores, a bounded sample) and the FP32
     # field's error against that FP64 run after the same solve calls
     if prev_cpus:
         os.sched_setaffinity(0, prev_cpus)
