@@ -223,7 +223,11 @@ int pcg_get_agents_device(pcg_context* ctx, double** positions, uint8_t** is_act
 
 /* ---- measurement -------------------------------------------------------- */
 
-/* Wraps every kernel launch in CUDA events (per-kernel time) when enabled. */
+/* Wraps every kernel launch in CUDA events (per-kernel time) when enabled.  The
+ * cell kernels' algorithmic bytes scale with counts known on the device (agents
+ * of shared voxels, agents that write a voxel); they are read after every timed
+ * ballot, and when timing is enabled after a ballot (this call then waits for
+ * the context's stream). */
 int pcg_set_kernel_timing(pcg_context* ctx, int enable);
 /* Copies up to `cap` per-kernel records; *count receives how many exist. */
 int pcg_get_kernel_stats(pcg_context* ctx, pcg_kernel_stat* stats, uint64_t cap, uint64_t* count);
